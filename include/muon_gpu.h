@@ -1,0 +1,282 @@
+/*
+ * muon_gpu.h — C ABI of the GB300 rendering library (libmuon_gpu.so).
+ *
+ * The library replaces the body of the reference renderer's sample loop
+ * (muon/renderer.cc:41-76: per sample Camera::CastRay -> Integrator::Trace ->
+ * Film::SetPixel) with one call that renders a whole film on one GPU, and it
+ * exposes the reference's acceleration-structure seam
+ * (acceleration::Structure::Intersect / HasIntersection, muon/acceleration.h:
+ * 44-49) as batched ray queries. Host code above this ABI (the `.muon` parser,
+ * the `muon` CLI, film output) lives in the same library.
+ *
+ * Conventions
+ *   - Every entry point returns an int status: MUON_OK (0) or a MUON_ERR_*
+ *     code; muon_gpu_last_error() returns a thread-local message for the last
+ *     failure on the calling thread. No C++ exception crosses the ABI.
+ *   - Host arrays passed in are only read during the call; the library keeps
+ *     its own copies. Arrays passed out are caller-allocated.
+ *   - All vectors are float[3] in world space unless noted; matrices are
+ *     column-major float[16] (column c occupies m[4c..4c+3]).
+ *   - There is no CPU fallback: without a usable CUDA device the GPU entry
+ *     points fail with MUON_ERR_CUDA.
+ *   - Calls on one MuonScene are serialised by the caller; distinct scenes may
+ *     be used from different host threads. Each scene owns one CUDA stream.
+ */
+#ifndef MUON_GPU_H_
+#define MUON_GPU_H_
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---------------------------------------------------- */
+#define MUON_OK 0
+#define MUON_ERR_INVALID_ARG 1 /* bad handle, pointer, size or enum          */
+#define MUON_ERR_OOM 2         /* host or device allocation failed           */
+#define MUON_ERR_CUDA 3        /* CUDA runtime error / no device             */
+#define MUON_ERR_TIMEOUT 4     /* a bounded device wait gave up              */
+#define MUON_ERR_PARSE 5       /* scene file unreadable or unusable          */
+#define MUON_ERR_IO 6          /* output file could not be written           */
+
+/* ---- enums (values follow the reference's enum order) ----------------- */
+/* Integrator types selected by the `integrator` scene command
+ * (muon/parser.cc:330-355, classes in muon/integration.h:51-176). */
+#define MUON_INTEGRATOR_NORMALS 0
+#define MUON_INTEGRATOR_ALBEDO 1
+#define MUON_INTEGRATOR_DEPTH 2
+#define MUON_INTEGRATOR_RAYTRACER 3
+#define MUON_INTEGRATOR_ANALYTIC_DIRECT 4
+#define MUON_INTEGRATOR_PATHTRACER 5
+/* muon/nee.h:7-14 */
+#define MUON_NEE_OFF 0
+#define MUON_NEE_ON 1
+#define MUON_NEE_MIS 2
+/* muon/importance_sampling.h:7-14 */
+#define MUON_IS_HEMISPHERE 0
+#define MUON_IS_COSINE 1
+#define MUON_IS_BRDF 2
+/* muon/brdf_type.h:7-14 */
+#define MUON_BRDF_LAMBERTIAN 0
+#define MUON_BRDF_PHONG 1
+#define MUON_BRDF_GGX 2
+/* muon/lighting.h:49-83 */
+#define MUON_LIGHT_DIRECTIONAL 0
+#define MUON_LIGHT_POINT 1
+#define MUON_LIGHT_QUAD 2
+/* muon/acceleration_type.h:11-28 */
+#define MUON_ACCEL_LINEAR 0
+#define MUON_ACCEL_BVH 1
+#define MUON_PARTITION_UNIFORM 0
+#define MUON_PARTITION_MIDPOINT 1
+#define MUON_PARTITION_SAH 2
+/* Triangle test used by the traversal kernels. REFERENCE repeats the
+ * reference's plane + edge-function test (muon/objects.cc:58-175) on
+ * world-space vertices; WATERTIGHT is the watertight ray/triangle test of
+ * Woop, Benthin and Wald (JCGT 2013). */
+#define MUON_TRI_REFERENCE 0
+#define MUON_TRI_WATERTIGHT 1
+
+/* render flags */
+#define MUON_RENDER_STATS 1u      /* count bounds/object tests (slower)        */
+#define MUON_RENDER_ACCUMULATE 2u /* add into the caller's film, do not zero   */
+
+/* ---- scene description (flattened muon::Scene, muon/scene.h:22-95) ---- */
+typedef struct MuonTransformDesc {
+  float object_to_world[16]; /* Primitive::transform                     */
+  float world_to_object[16]; /* Primitive::inv_transform                 */
+  float normal_to_world[16]; /* Primitive::inv_transpose_transform       */
+} MuonTransformDesc;
+
+typedef struct MuonMaterialDesc { /* muon::Material, muon/materials.h:125-148 */
+  float ambient[3];
+  float diffuse[3];
+  float specular[3];
+  float emission[3];
+  float shininess;
+  float roughness;
+  int32_t brdf; /* MUON_BRDF_*: the BRDF actually instantiated */
+  int32_t pad;
+} MuonMaterialDesc;
+
+typedef struct MuonLightDesc { /* muon/lighting.h:36-83 */
+  int32_t type;                /* MUON_LIGHT_*                             */
+  float color[3];
+  float p0[3]; /* quad: corner | point: position | directional: direction */
+  float p1[3]; /* quad: edge0  | point: attenuation (const, lin, quad)    */
+  float p2[3]; /* quad: edge1                                             */
+} MuonLightDesc;
+
+typedef struct MuonTriangleDesc { /* muon::Tri, muon/objects.h:62-86 */
+  float v[3][3];      /* object-space vertex positions                 */
+  float n[3][3];      /* vertex normals, used when smooth != 0         */
+  int32_t transform;  /* index into transforms; -1 = identity          */
+  int32_t material;   /* index into materials                          */
+  int32_t light;      /* quad light this triangle represents; -1 = none */
+  int32_t smooth;     /* interpolate vertex normals                    */
+  int32_t prim_id;    /* primitive index in scene-file (parse) order   */
+  int32_t pad;
+} MuonTriangleDesc;
+
+typedef struct MuonSphereDesc { /* muon::Sphere, muon/objects.h:89-98 */
+  float center[3];
+  float radius;
+  int32_t transform;
+  int32_t material;
+  int32_t prim_id;
+  int32_t pad;
+} MuonSphereDesc;
+
+typedef struct MuonCameraDesc { /* muon::Camera, muon/camera.h:9-32 */
+  float eye[3];
+  float look_at[3];
+  float up[3];
+  float fov_y_degrees;
+  int32_t width; /* the film size in effect when the camera was declared */
+  int32_t height;
+} MuonCameraDesc;
+
+typedef struct MuonSceneDesc {
+  int32_t width, height; /* film size */
+  MuonCameraDesc camera;
+  const MuonTransformDesc *transforms;
+  int32_t num_transforms;
+  const MuonMaterialDesc *materials;
+  int32_t num_materials;
+  const MuonLightDesc *lights;
+  int32_t num_lights;
+  const MuonTriangleDesc *triangles;
+  int64_t num_triangles;
+  const MuonSphereDesc *spheres;
+  int64_t num_spheres;
+  int32_t acceleration;       /* MUON_ACCEL_*                       */
+  int32_t partition_strategy; /* MUON_PARTITION_*                   */
+  int32_t max_leaf_size;      /* 0 = default (4)                    */
+  int32_t pad;
+} MuonSceneDesc;
+
+/* Render settings: the integrator properties of muon::Scene
+ * (muon/scene.h:32-47) plus GPU-only knobs. */
+typedef struct MuonRenderParams {
+  int32_t integrator; /* MUON_INTEGRATOR_* */
+  int32_t pixel_samples;
+  int32_t light_samples;
+  int32_t light_stratify;
+  int32_t next_event_estimation; /* MUON_NEE_* */
+  int32_t russian_roulette;
+  int32_t importance_sampling; /* MUON_IS_* */
+  int32_t min_depth;
+  int32_t max_depth; /* -1 = unbounded */
+  int32_t sample_offset; /* index of the first sample (progressive runs) */
+  uint64_t seed;
+  int32_t triangle_test; /* MUON_TRI_* */
+  int32_t wave_paths;    /* paths in flight per wavefront; 0 = tuned     */
+  uint32_t flags;        /* MUON_RENDER_*                               */
+  int32_t pad;
+} MuonRenderParams;
+
+/* FP64 film: per pixel (row-major, y outer) the sum and sum of squares of the
+ * sample radiances (RGB) and the sample count. Caller-allocated, 3*W*H
+ * doubles for sum/sum_sq and W*H uint32 for count. */
+typedef struct MuonFilm {
+  int32_t width, height;
+  double *sum;
+  double *sum_sq;
+  uint32_t *count;
+} MuonFilm;
+
+typedef struct MuonRay {
+  float origin[3];
+  float direction[3]; /* unit length */
+} MuonRay;
+
+typedef struct MuonHit {
+  float distance;  /* world distance; +inf on a miss                 */
+  int32_t prim_id; /* parse-order primitive id; -1 on a miss         */
+  float position[3];
+  float normal[3];
+} MuonHit;
+
+/* muon::TraceStats (muon/stats.h:11-44) for the last render, plus the
+ * shadow rays the reference does not count as rays. */
+typedef struct MuonStats {
+  uint64_t primary_rays;
+  uint64_t secondary_rays;
+  uint64_t shadow_rays;
+  uint64_t object_tests; /* filled only with MUON_RENDER_STATS */
+  uint64_t object_hits;
+  uint64_t bounds_tests;
+  uint64_t bounds_hits;
+  uint64_t paths;
+  double render_ms;      /* device time of the last render               */
+  double extend_ms;      /* closest-hit traversal kernels               */
+  double occlude_ms;     /* any-hit traversal kernels                   */
+  double shade_ms;       /* camera, shading and film kernels            */
+  uint64_t kernel_launches;
+  uint64_t bvh_nodes;
+  uint64_t primitives;
+} MuonStats;
+
+/* ---- host side: scene files (muon/parser.{h,cc}) ---------------------- */
+typedef struct MuonParsedScene MuonParsedScene;
+
+/* Parses a .muon file with the reference parser's semantics
+ * (muon/parser.cc:230-880, Parser::Parse). Malformed lines are skipped with a
+ * warning, as in the reference. */
+int muon_parse_scene_file(const char *path, MuonParsedScene **out);
+/* Same, from an in-memory string; relative `load` paths resolve against
+ * base_dir (may be NULL). */
+int muon_parse_scene_string(const char *text, const char *base_dir, MuonParsedScene **out);
+/* Borrowed view of the parsed scene and its render settings; valid until
+ * muon_parsed_scene_free. */
+int muon_parsed_scene_desc(const MuonParsedScene *scene, MuonSceneDesc *desc, MuonRenderParams *params);
+/* Film post-process settings from the file: gamma (muon/film.cc:29-33) and
+ * the `output` path (NULL if none was given). */
+float muon_parsed_scene_gamma(const MuonParsedScene *scene);
+const char *muon_parsed_scene_output(const MuonParsedScene *scene);
+int32_t muon_parsed_scene_warnings(const MuonParsedScene *scene);
+void muon_parsed_scene_free(MuonParsedScene *scene);
+
+/* Tone-maps a film like Film::WriteOutput (muon/film.cc:21-43: mean over
+ * `count`, gamma, clamp to [0,1], x255 truncated) into 8-bit RGB (row-major,
+ * 3*W*H bytes) and optionally writes it as PNG (.png) or binary PPM. */
+int muon_film_tonemap(const MuonFilm *film, float gamma, uint8_t *rgb_out);
+int muon_film_write(const MuonFilm *film, float gamma, const char *path);
+
+/* ---- device side ------------------------------------------------------ */
+typedef struct MuonScene MuonScene;
+
+/* Builds the BVH on the host (muon/acceleration.cc:204-458 replaced by a
+ * binned-SAH builder) and uploads the scene to the current CUDA device once.
+ * Replaces Structure::AddPrimitive + Structure::Init (muon/acceleration.h:
+ * 30-35). */
+int muon_gpu_scene_create(const MuonSceneDesc *desc, MuonScene **out);
+void muon_gpu_scene_destroy(MuonScene *scene);
+
+/* Renders the whole film: replaces the per-thread sample loop of
+ * Renderer::Render (muon/renderer.cc:41-76). Host film in, host film out. */
+int muon_gpu_render(MuonScene *scene, const MuonRenderParams *params, MuonFilm *film);
+/* Same with the film in device memory (pointers from cudaMalloc: 3*W*H
+ * doubles each for sum/sum_sq, W*H uint32 for count). */
+int muon_gpu_render_device(MuonScene *scene, const MuonRenderParams *params, double *d_sum,
+                           double *d_sum_sq, uint32_t *d_count);
+
+/* Batched ray queries mirroring Structure::Intersect and
+ * Structure::HasIntersection (muon/acceleration.h:44-49) on host arrays. */
+int muon_gpu_intersect(MuonScene *scene, const MuonRay *rays, int64_t n, int32_t triangle_test,
+                       MuonHit *hits);
+int muon_gpu_occluded(MuonScene *scene, const MuonRay *rays, const float *max_distance, int64_t n,
+                      int32_t triangle_test, uint8_t *occluded);
+
+/* Counters and device timings of the last render (muon/stats.h:11-44). */
+int muon_gpu_stats(const MuonScene *scene, MuonStats *stats);
+
+/* Thread-local description of the last failure on this thread. */
+const char *muon_gpu_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MUON_GPU_H_ */

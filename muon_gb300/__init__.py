@@ -1,0 +1,229 @@
+"""GB300 rendering path of the muon path tracer.
+
+Python mirror of the reference renderer's interface for its hot path
+(muon/renderer.cc Renderer::Render, muon/parser.cc Parser::Parse,
+muon/acceleration.h Structure::Intersect/HasIntersection, muon/film.cc
+Film::WriteOutput) over the C ABI in include/muon_gpu.h.
+
+    scene = muon_gb300.Scene.from_file("cornell.muon")
+    film = scene.render()                 # settings from the scene file
+    film.write("out.png", scene.gamma)
+
+Rendering runs on the GPU only; a missing native library or CUDA device is an
+error, never a silent CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import native
+from .native import MuonError, check, load
+
+__all__ = ["Scene", "FilmResult", "MuonError", "render_file", "parse_file", "parse_string"]
+
+
+class ParsedScene:
+    """A parsed .muon scene (host memory), Parser::Parse's SceneConfig."""
+
+    def __init__(self, handle: int):
+        self._h = C.c_void_p(handle)
+        self.desc = native.SceneDesc()
+        self.params = native.RenderParams()
+        check(load().muon_parsed_scene_desc(self._h, C.byref(self.desc), C.byref(self.params)))
+
+    @property
+    def gamma(self) -> float:
+        return float(load().muon_parsed_scene_gamma(self._h))
+
+    @property
+    def output(self) -> str | None:
+        o = load().muon_parsed_scene_output(self._h)
+        return o.decode() if o else None
+
+    @property
+    def warnings(self) -> int:
+        return int(load().muon_parsed_scene_warnings(self._h))
+
+    def close(self) -> None:
+        if self._h:
+            load().muon_parsed_scene_free(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def parse_file(path: str) -> ParsedScene:
+    h = C.c_void_p()
+    check(load().muon_parse_scene_file(path.encode(), C.byref(h)))
+    return ParsedScene(h.value)
+
+
+def parse_string(text: str, base_dir: str = ".") -> ParsedScene:
+    h = C.c_void_p()
+    check(load().muon_parse_scene_string(text.encode(), base_dir.encode(), C.byref(h)))
+    return ParsedScene(h.value)
+
+
+@dataclass
+class FilmResult:
+    """FP64 film: per-pixel sums, sums of squares and sample counts."""
+
+    sum: np.ndarray     # (H, W, 3) float64
+    sum_sq: np.ndarray  # (H, W, 3) float64
+    count: np.ndarray   # (H, W) uint32
+
+    @property
+    def width(self) -> int:
+        return self.sum.shape[1]
+
+    @property
+    def height(self) -> int:
+        return self.sum.shape[0]
+
+    def mean(self) -> np.ndarray:
+        n = np.maximum(self.count, 1)[..., None].astype(np.float64)
+        return self.sum / n
+
+    def variance_of_mean(self) -> np.ndarray:
+        n = np.maximum(self.count, 1)[..., None].astype(np.float64)
+        m = self.sum / n
+        var = np.maximum(self.sum_sq / n - m * m, 0.0) * n / np.maximum(n - 1, 1)
+        return var / n
+
+    def _cfilm(self):
+        f = native.Film()
+        f.width, f.height = self.width, self.height
+        f.sum = self.sum.ctypes.data_as(C.POINTER(C.c_double))
+        f.sum_sq = self.sum_sq.ctypes.data_as(C.POINTER(C.c_double))
+        f.count = self.count.ctypes.data_as(C.POINTER(C.c_uint32))
+        return f
+
+    def tonemap(self, gamma: float = 1.0) -> np.ndarray:
+        """8-bit RGB exactly as Film::WriteOutput forms it (muon/film.cc:21-43)."""
+        out = np.zeros((self.height, self.width, 3), dtype=np.uint8)
+        f = self._cfilm()
+        check(load().muon_film_tonemap(C.byref(f), C.c_float(gamma), out.ctypes.data_as(C.POINTER(C.c_uint8))))
+        return out
+
+    def write(self, path: str, gamma: float = 1.0) -> None:
+        f = self._cfilm()
+        check(load().muon_film_write(C.byref(f), C.c_float(gamma), path.encode()))
+
+
+class Scene:
+    """A scene resident on the GPU (Structure::Init + upload)."""
+
+    def __init__(self, parsed: ParsedScene, acceleration: str = "bvh", partition_strategy: str = "sah",
+                 max_leaf_size: int = 0):
+        self.parsed = parsed
+        desc = parsed.desc
+        desc.acceleration = native.ACCEL_LINEAR if acceleration == "linear" else native.ACCEL_BVH
+        desc.partition_strategy = native.PARTITION[partition_strategy]
+        desc.max_leaf_size = max_leaf_size
+        h = C.c_void_p()
+        check(load().muon_gpu_scene_create(C.byref(desc), C.byref(h)))
+        self._h = h
+        self.width, self.height = desc.width, desc.height
+
+    @classmethod
+    def from_file(cls, path: str, **kw) -> "Scene":
+        return cls(parse_file(path), **kw)
+
+    @classmethod
+    def from_string(cls, text: str, **kw) -> "Scene":
+        return cls(parse_string(text), **kw)
+
+    @property
+    def gamma(self) -> float:
+        return self.parsed.gamma
+
+    def params(self, **overrides) -> native.RenderParams:
+        """The scene file's render settings with keyword overrides applied."""
+        p = native.RenderParams()
+        C.pointer(p)[0] = self.parsed.params
+        for k, v in overrides.items():
+            if k == "integrator" and isinstance(v, str):
+                v = native.INTEGRATORS[v]
+            elif k == "next_event_estimation" and isinstance(v, str):
+                v = native.NEE[v]
+            elif k == "importance_sampling" and isinstance(v, str):
+                v = native.IMPORTANCE[v]
+            elif k == "triangle_test" and isinstance(v, str):
+                v = native.TRI_WATERTIGHT if v == "watertight" else native.TRI_REFERENCE
+            setattr(p, k, v)
+        return p
+
+    def render(self, params: native.RenderParams | None = None, **overrides) -> FilmResult:
+        """Renders the whole film (Renderer::Render's sample loop) on the GPU."""
+        p = params if params is not None else self.params(**overrides)
+        h, w = self.height, self.width
+        film = FilmResult(np.zeros((h, w, 3)), np.zeros((h, w, 3)), np.zeros((h, w), dtype=np.uint32))
+        f = film._cfilm()
+        check(load().muon_gpu_render(self._h, C.byref(p), C.byref(f)))
+        return film
+
+    def render_device(self, params: native.RenderParams, d_sum: int, d_sum_sq: int, d_count: int) -> None:
+        """Renders into a film already in device memory (raw device pointers)."""
+        check(load().muon_gpu_render_device(self._h, C.byref(params), C.c_void_p(d_sum), C.c_void_p(d_sum_sq),
+                                             C.c_void_p(d_count)))
+
+    def intersect(self, origins: np.ndarray, directions: np.ndarray, triangle_test: int = native.TRI_REFERENCE):
+        """Closest hits (Structure::Intersect) for a batch of rays.
+
+        Returns (distance, prim_id, position, normal); prim_id is the primitive's
+        index in scene-file order, -1 on a miss.
+        """
+        n = len(origins)
+        rays = np.zeros((n, 6), dtype=np.float32)
+        rays[:, :3] = origins
+        rays[:, 3:] = directions
+        hits = np.zeros((n, 8), dtype=np.float32)
+        check(load().muon_gpu_intersect(self._h, rays.ctypes.data_as(C.POINTER(native.Ray)), n, triangle_test,
+                                        hits.ctypes.data_as(C.POINTER(native.Hit))))
+        return hits[:, 0].copy(), hits[:, 1].view(np.int32).copy(), hits[:, 2:5].copy(), hits[:, 5:8].copy()
+
+    def occluded(self, origins: np.ndarray, directions: np.ndarray, max_distance: np.ndarray,
+                 triangle_test: int = native.TRI_REFERENCE) -> np.ndarray:
+        """Any hit closer than max_distance (Structure::HasIntersection)."""
+        n = len(origins)
+        rays = np.zeros((n, 6), dtype=np.float32)
+        rays[:, :3] = origins
+        rays[:, 3:] = directions
+        md = np.ascontiguousarray(max_distance, dtype=np.float32)
+        out = np.zeros(n, dtype=np.uint8)
+        check(load().muon_gpu_occluded(self._h, rays.ctypes.data_as(C.POINTER(native.Ray)),
+                                       md.ctypes.data_as(C.POINTER(C.c_float)), n, triangle_test,
+                                       out.ctypes.data_as(C.POINTER(C.c_uint8))))
+        return out.astype(bool)
+
+    def stats(self) -> dict:
+        s = native.Stats()
+        check(load().muon_gpu_stats(self._h, C.byref(s)))
+        return {name: getattr(s, name) for name, _ in native.Stats._fields_}
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            load().muon_gpu_scene_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def render_file(path: str, **overrides) -> tuple[FilmResult, float]:
+    """Parses and renders a scene file; returns the film and the file's gamma."""
+    scene = Scene.from_file(path)
+    try:
+        return scene.render(**overrides), scene.gamma
+    finally:
+        scene.close()

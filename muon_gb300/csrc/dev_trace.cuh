@@ -1,0 +1,237 @@
+// Ray/primitive tests and BVH traversal (closest hit and any hit).
+//
+// Replaces BVH::Intersect / BVH::HasIntersection (muon/acceleration.cc:65-202)
+// and the primitive tests they call (muon/objects.cc:29-270). Acceptance
+// follows the reference: a primitive hit counts when 0 < distance < limit
+// (muon/acceleration.cc:120-124, muon/objects.cc:9-17).
+#pragma once
+
+#include "dev_common.cuh"
+
+namespace muon_gpu {
+
+constexpr int kStackSize = 64;
+
+struct RayPre {
+  float3 o, d, idir, ood;
+  // watertight-test shear
+  int kx, ky, kz;
+  float sx, sy, sz;
+};
+
+__device__ __forceinline__ float SafeInv(float x) {
+  const float tiny = 1e-30f;
+  return 1.0f / (fabsf(x) > tiny ? x : copysignf(tiny, x));
+}
+
+template <int kTriTest>
+__device__ __forceinline__ RayPre Prepare(float3 o, float3 d) {
+  RayPre r;
+  r.o = o;
+  r.d = d;
+  r.idir = f3(SafeInv(d.x), SafeInv(d.y), SafeInv(d.z));
+  r.ood = o * r.idir;
+  if (kTriTest == MUON_TRI_WATERTIGHT) {
+    float ax = fabsf(d.x), ay = fabsf(d.y), az = fabsf(d.z);
+    r.kz = ax > ay ? (ax > az ? 0 : 2) : (ay > az ? 1 : 2);
+    r.kx = r.kz == 2 ? 0 : r.kz + 1;
+    r.ky = r.kx == 2 ? 0 : r.kx + 1;
+    float dz = r.kz == 0 ? d.x : (r.kz == 1 ? d.y : d.z);
+    if (dz < 0.0f) {
+      int t = r.kx;
+      r.kx = r.ky;
+      r.ky = t;
+    }
+    float dx = r.kx == 0 ? d.x : (r.kx == 1 ? d.y : d.z);
+    float dy = r.ky == 0 ? d.x : (r.ky == 1 ? d.y : d.z);
+    r.sx = dx / dz;
+    r.sy = dy / dz;
+    r.sz = 1.0f / dz;
+  }
+  return r;
+}
+
+__device__ __forceinline__ float comp3(float3 v, int k) { return k == 0 ? v.x : (k == 1 ? v.y : v.z); }
+
+// The reference's triangle test (muon/objects.cc:103-158) on world-space
+// vertices: plane distance with the unnormalised normal, parallel rejection
+// against the per-triangle threshold, then three edge functions >= 0.
+__device__ __forceinline__ float TriReference(const RayPre &r, const PrimRecord &p) {
+  float3 n = f3(p.p3);
+  float dn = dot3(n, r.d);
+  float eps = p.p1.w;
+  if (dn > -eps && dn < eps) return -1.0f;
+  float t = (p.p0.w - dot3(r.o, n)) / dn;
+  if (!(t > 0.0f)) return -1.0f;
+  float3 a = f3(p.p0), b = f3(p.p1), c = f3(p.p2);
+  float3 q = r.o + r.d * t;
+  if (dot3(n, cross3(b - a, q - a)) < 0.0f) return -1.0f;
+  if (dot3(n, cross3(c - b, q - b)) < 0.0f) return -1.0f;
+  if (dot3(n, cross3(a - c, q - c)) < 0.0f) return -1.0f;
+  return t;
+}
+
+// Watertight ray/triangle test (Woop, Benthin, Wald, "Watertight
+// Ray/Triangle Intersection", JCGT 2(1), 2013); both faces count.
+__device__ __forceinline__ float TriWatertight(const RayPre &r, const PrimRecord &p) {
+  float3 A = f3(p.p0) - r.o, B = f3(p.p1) - r.o, C = f3(p.p2) - r.o;
+  float az = comp3(A, r.kz), bz = comp3(B, r.kz), cz = comp3(C, r.kz);
+  float ax = comp3(A, r.kx) - r.sx * az, ay = comp3(A, r.ky) - r.sy * az;
+  float bx = comp3(B, r.kx) - r.sx * bz, by = comp3(B, r.ky) - r.sy * bz;
+  float cx = comp3(C, r.kx) - r.sx * cz, cy = comp3(C, r.ky) - r.sy * cz;
+  float U = cx * by - cy * bx;
+  float V = ax * cy - ay * cx;
+  float W = bx * ay - by * ax;
+  if (U == 0.0f || V == 0.0f || W == 0.0f) {
+    double cxby = (double)cx * by, cybx = (double)cy * bx;
+    U = (float)(cxby - cybx);
+    double axcy = (double)ax * cy, aycx = (double)ay * cx;
+    V = (float)(axcy - aycx);
+    double bxay = (double)bx * ay, byax = (double)by * ax;
+    W = (float)(bxay - byax);
+  }
+  if ((U < 0.0f || V < 0.0f || W < 0.0f) && (U > 0.0f || V > 0.0f || W > 0.0f)) return -1.0f;
+  float det = U + V + W;
+  if (det == 0.0f) return -1.0f;
+  float T = U * (r.sz * az) + V * (r.sz * bz) + W * (r.sz * cz);
+  float t = T / det;
+  return t > 0.0f ? t : -1.0f;
+}
+
+// Sphere test (muon/objects.cc:195-270). Identity-transform spheres are
+// tested in world space; others in object space with the ray carried by the
+// inverse transform and the direction re-normalised (muon/transform.h:13-18),
+// the distance measured back in world space (muon/objects.cc:39-43).
+__device__ __forceinline__ float SphereTest(const DevScene &s, const RayPre &r, const PrimRecord &p) {
+  int xf = __float_as_int(p.p1.y);
+  float3 c = f3(p.p0);
+  float rad = p.p0.w;
+  float3 o = r.o, d = r.d;
+  if (xf >= 0) {
+    const DevTransform &T = s.transforms[xf];
+    o = xform_point3(T.w2o, r.o);
+    d = normalize3(xform_vec3(T.w2o, r.d));
+  }
+  float3 oc = o - c;
+  float b = dot3(d, oc);
+  float cc = dot3(oc, oc) - rad * rad;
+  float disc = b * b - cc;
+  if (disc < 0.0f) return -1.0f;
+  float sq = sqrtf(disc);
+  float r0 = -b + sq, r1 = -b - sq;
+  if (r0 < 0.0f && r1 < 0.0f) return -1.0f;
+  float t = fminf(r0, r1);
+  if (t < 0.0f) t = fmaxf(r0, r1);
+  if (xf >= 0) {
+    float3 pw = xform_point3(s.transforms[xf].o2w, o + d * t);
+    t = length3(pw - r.o);
+  }
+  return t > 0.0f ? t : -1.0f;
+}
+
+template <int kTriTest>
+__device__ __forceinline__ float PrimTest(const DevScene &s, const RayPre &r, const PrimRecord &p, uint32_t flags) {
+  if (flags & kPrimSphere) return SphereTest(s, r, p);
+  return kTriTest == MUON_TRI_WATERTIGHT ? TriWatertight(r, p) : TriReference(r, p);
+}
+
+__device__ __forceinline__ PrimRecord LoadPrim(const PrimRecord *prims, int i) {
+  const float4 *q = reinterpret_cast<const float4 *>(prims + i);
+  float4 a = __ldg(q), b = __ldg(q + 1), c = __ldg(q + 2), d = __ldg(q + 3);
+  PrimRecord p;
+  p.p0 = F4{a.x, a.y, a.z, a.w};
+  p.p1 = F4{b.x, b.y, b.z, b.w};
+  p.p2 = F4{c.x, c.y, c.z, c.w};
+  p.p3 = F4{d.x, d.y, d.z, d.w};
+  return p;
+}
+
+struct TraceCounters {
+  uint32_t box_tests = 0, box_hits = 0, prim_tests = 0, prim_hits = 0;
+};
+
+// Closest hit (kAnyHit = false) or first hit (kAnyHit = true) with
+// 0 < t < tmax. Returns the leaf slot of the primitive hit, or -1; *t_hit
+// receives its distance. A stack overflow sets *overflow.
+template <bool kAnyHit, bool kStats, int kTriTest>
+__device__ __forceinline__ int Trace(const DevScene &s, float3 o, float3 d, float tmax, float *t_hit,
+                                     TraceCounters *cnt, bool *overflow) {
+  int hit = -1;
+  if (s.num_nodes == 0) return -1;
+  const RayPre r = Prepare<kTriTest>(o, d);
+  int stack[kStackSize];
+  int sp = 0;
+  int node = 0;
+  while (true) {
+    // Interior nodes: test both child boxes, descend into the nearer hit child
+    // and defer the farther one.
+    while (node >= 0) {
+      const float4 *q = reinterpret_cast<const float4 *>(s.nodes + node);
+      float4 n0 = __ldg(q), n1 = __ldg(q + 1), n2 = __ldg(q + 2);
+      int4 n3 = __ldg(reinterpret_cast<const int4 *>(q + 3));
+      float c0lox = n0.x * r.idir.x - r.ood.x, c0hix = n0.y * r.idir.x - r.ood.x;
+      float c0loy = n0.z * r.idir.y - r.ood.y, c0hiy = n0.w * r.idir.y - r.ood.y;
+      float c0loz = n2.x * r.idir.z - r.ood.z, c0hiz = n2.y * r.idir.z - r.ood.z;
+      float c1lox = n1.x * r.idir.x - r.ood.x, c1hix = n1.y * r.idir.x - r.ood.x;
+      float c1loy = n1.z * r.idir.y - r.ood.y, c1hiy = n1.w * r.idir.y - r.ood.y;
+      float c1loz = n2.z * r.idir.z - r.ood.z, c1hiz = n2.w * r.idir.z - r.ood.z;
+      float c0min = fmaxf(fmaxf(fminf(c0lox, c0hix), fminf(c0loy, c0hiy)), fmaxf(fminf(c0loz, c0hiz), 0.0f));
+      float c0max = fminf(fminf(fmaxf(c0lox, c0hix), fmaxf(c0loy, c0hiy)), fminf(fmaxf(c0loz, c0hiz), tmax));
+      float c1min = fmaxf(fmaxf(fminf(c1lox, c1hix), fminf(c1loy, c1hiy)), fmaxf(fminf(c1loz, c1hiz), 0.0f));
+      float c1max = fminf(fminf(fmaxf(c1lox, c1hix), fmaxf(c1loy, c1hiy)), fminf(fmaxf(c1loz, c1hiz), tmax));
+      bool h0 = c0min <= c0max, h1 = c1min <= c1max;
+      if (kStats) {
+        cnt->box_tests += 2;
+        cnt->box_hits += (int)h0 + (int)h1;
+      }
+      if (!h0 && !h1) {
+        if (sp == 0) {
+          node = kEmptyLink;
+          break;
+        }
+        node = stack[--sp];
+      } else {
+        int near = h0 ? n3.x : n3.y;
+        if (h0 && h1) {
+          int far = n3.y;
+          if (c1min < c0min) {
+            near = n3.y;
+            far = n3.x;
+          }
+          if (sp < kStackSize) {
+            stack[sp++] = far;
+          } else {
+            *overflow = true;
+          }
+        }
+        node = near;
+      }
+    }
+    if (node == kEmptyLink) break;
+    // Leaf: test its primitives until the record flagged as last.
+    int i = ~node;
+    while (true) {
+      PrimRecord p = LoadPrim(s.prims, i);
+      uint32_t flags = __float_as_uint(p.p3.w);
+      float t = PrimTest<kTriTest>(s, r, p, flags);
+      if (kStats) cnt->prim_tests += 1;
+      if (t > 0.0f && t < tmax) {
+        if (kStats) cnt->prim_hits += 1;
+        tmax = t;
+        hit = i;
+        if (kAnyHit) {
+          *t_hit = t;
+          return hit;
+        }
+      }
+      if (flags & kPrimLast) break;
+      ++i;
+    }
+    if (sp == 0) break;
+    node = stack[--sp];
+  }
+  *t_hit = tmax;
+  return hit;
+}
+
+}  // namespace muon_gpu

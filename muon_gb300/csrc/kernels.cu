@@ -1,0 +1,563 @@
+// Wavefront path-tracing kernels for sm_103a.
+//
+// One wavefront holds a batch of camera samples. Per bounce:
+//   extend  closest-hit BVH traversal of the queued path rays
+//   shade   emission, next-event estimation, MIS and continuation sampling
+//           (PathTracer::Shade, muon/integration.cc:205-328); writes one
+//           contribution per shadow slot and appends shadow rays and
+//           continuation rays to compacted queues
+//   occlude any-hit traversal of the shadow queue; zeroes blocked slots
+// and at the end of the wave
+//   film    folds each sample's radiance and surviving slots into the FP64
+//           film (sum, sum of squares, count), pixel by pixel in sample order
+//
+// Queue compaction: each warp forms its offsets with a ballot/shuffle scan,
+// the block scans the warp totals in shared memory and one thread per block
+// reserves the block's range with a single atomicAdd.
+#include <cuda_runtime.h>
+
+#include "dev_shade.cuh"
+#include "dev_trace.cuh"
+#include "kernels.cuh"
+
+namespace muon_gpu {
+
+namespace {
+
+constexpr int kBlock = 256;
+constexpr int kWarps = kBlock / 32;
+
+__device__ __forceinline__ void AddStat(unsigned long long *stats, int idx, unsigned long long v) {
+  // one atomic per warp
+  unsigned long long s = v;
+  for (int off = 16; off > 0; off >>= 1) s += __shfl_down_sync(0xffffffffu, s, off);
+  if ((threadIdx.x & 31) == 0 && s) atomicAdd(stats + idx, s);
+}
+
+// Exclusive block-wide scan of a (count_a, count_b) pair; returns this
+// thread's offsets into two global queues whose tails are reserved with one
+// atomicAdd each per block. All threads of the block must call it.
+__device__ __forceinline__ void BlockReserve(uint32_t a, uint32_t b, uint32_t *ctr_a, uint32_t *ctr_b, uint32_t *off_a,
+                                             uint32_t *off_b) {
+  __shared__ unsigned long long warp_tot[kWarps];
+  __shared__ unsigned long long base;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  unsigned long long v = (static_cast<unsigned long long>(a) << 32) | b;
+  unsigned long long incl = v;
+  for (int off = 1; off < 32; off <<= 1) {
+    unsigned long long y = __shfl_up_sync(0xffffffffu, incl, off);
+    if (lane >= off) incl += y;
+  }
+  if (lane == 31) warp_tot[warp] = incl;
+  __syncthreads();
+  if (warp == 0) {
+    unsigned long long t = lane < kWarps ? warp_tot[lane] : 0ull;
+    unsigned long long ti = t;
+    for (int off = 1; off < kWarps; off <<= 1) {
+      unsigned long long y = __shfl_up_sync(0xffffffffu, ti, off);
+      if (lane >= off) ti += y;
+    }
+    if (lane < kWarps) warp_tot[lane] = ti - t;  // exclusive
+    if (lane == kWarps - 1) {
+      uint32_t ta = static_cast<uint32_t>(ti >> 32), tb = static_cast<uint32_t>(ti & 0xffffffffu);
+      uint32_t ba = ta ? atomicAdd(ctr_a, ta) : 0u;
+      uint32_t bb = tb ? atomicAdd(ctr_b, tb) : 0u;
+      base = (static_cast<unsigned long long>(ba) << 32) | bb;
+    }
+  }
+  __syncthreads();
+  unsigned long long excl = warp_tot[warp] + incl - v;
+  *off_a = static_cast<uint32_t>(base >> 32) + static_cast<uint32_t>(excl >> 32);
+  *off_b = static_cast<uint32_t>(base & 0xffffffffu) + static_cast<uint32_t>(excl & 0xffffffffu);
+}
+
+// Surface point, shading normal and material of a hit (Primitive::Intersect,
+// muon/objects.cc:29-46, and the normals of Tri/Sphere::IntersectObjectSpace).
+__device__ __forceinline__ void HitSurface(const DevScene &s, int slot, float3 o, float3 d, float t, float3 *p_out,
+                                           float3 *n_out, int *mat_out, int *light_out, int *prim_id_out) {
+  const float4 *q = reinterpret_cast<const float4 *>(s.shade + slot);
+  float4 s0 = __ldg(q);
+  int4 s1 = __ldg(reinterpret_cast<const int4 *>(q + 1));
+  float3 p = o + d * t;
+  float3 n;
+  if (s1.w & kPrimSphere) {
+    PrimRecord pr = LoadPrim(s.prims, slot);
+    float3 c = f3(pr.p0);
+    if (s1.z < 0) {
+      n = normalize3(p - c);
+    } else {
+      const DevTransform &T = s.transforms[s1.z];
+      float3 po = xform_point3(T.w2o, p);
+      n = normalize3(xform_vec3(T.n2w, normalize3(po - c)));
+    }
+  } else if (s1.w & kPrimSmooth) {
+    PrimRecord pr = LoadPrim(s.prims, slot);
+    float3 a = f3(pr.p0), b = f3(pr.p1), c = f3(pr.p2), nn = f3(pr.p3);
+    float inv = 1.0f / dot3(nn, nn);
+    float v = dot3(nn, cross3(b - a, p - a)) * inv;
+    float w = dot3(nn, cross3(c - b, p - b)) * inv;
+    float u = dot3(nn, cross3(a - c, p - c)) * inv;
+    const float4 *vn = reinterpret_cast<const float4 *>(s.smooth_normals) + 3 * slot;
+    n = normalize3(w * f3(__ldg(vn)) + u * f3(__ldg(vn + 1)) + v * f3(__ldg(vn + 2)));
+  } else {
+    n = f3(s0.x, s0.y, s0.z);
+  }
+  *p_out = p;
+  *n_out = n;
+  *mat_out = __float_as_int(s0.w);
+  *light_out = s1.x;
+  *prim_id_out = s1.y;
+}
+
+__device__ __forceinline__ Rng MakeRng(const WaveInfo &w, int path, uint32_t bounce) {
+  int pixel = w.p0 + path / w.ns;
+  uint32_t sample = w.sample_offset + static_cast<uint32_t>(w.s0 + path % w.ns);
+  Rng r(w.seed, 0, bounce);
+  r.ctr = make_uint4(sample, static_cast<uint32_t>(pixel), bounce, 0u);
+  return r;
+}
+
+// ---- camera ------------------------------------------------------------
+// Sampler::NextSample (muon/sampling.cc:80-121): sample 0 at the pixel centre,
+// later samples jittered uniformly inside the pixel.
+__global__ void __launch_bounds__(kBlock) CameraKernel(DevCamera cam, WaveInfo w, PathBuffers b, int slots) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= w.n) return;
+  int pixel = w.p0 + i / w.ns;
+  uint32_t sample = w.sample_offset + static_cast<uint32_t>(w.s0 + i % w.ns);
+  int px = pixel % w.width, py = pixel / w.width;
+  float x, y;
+  if (sample == 0) {
+    x = mm::add(static_cast<float>(px), 0.5f);
+    y = mm::add(static_cast<float>(py), 0.5f);
+  } else {
+    Rng rng(w.seed, 0, 0xffffffffu);
+    rng.ctr = make_uint4(sample, static_cast<uint32_t>(pixel), 0xffffffffu, 0u);
+    float u = rng.Next(), v = rng.Next();
+    float fx = static_cast<float>(px), fy = static_cast<float>(py);
+    x = mm::add(fx, u);
+    y = mm::add(fy, v);
+    if (x == mm::add(fx, 1.0f)) x = nextafterf(x, -INFINITY);
+    if (y == mm::add(fy, 1.0f)) y = nextafterf(y, -INFINITY);
+  }
+  float3 o, d;
+  CastRay(cam, x, y, &o, &d);
+  b.ray_o[0][i] = make_float4(o.x, o.y, o.z, __int_as_float(i));
+  b.ray_d[0][i] = make_float4(d.x, d.y, d.z, INFINITY);
+  b.tp[i] = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
+  b.rad[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+  for (int k = 0; k < slots; ++k) b.contrib[static_cast<int64_t>(i) * slots + k] = make_float4(0, 0, 0, 0);
+}
+
+// ---- extend / occlude ------------------------------------------------------
+template <bool kStats, int kTri>
+__global__ void __launch_bounds__(kBlock) ExtendKernel(DevScene s, const float4 *__restrict__ ray_o,
+                                                       const float4 *__restrict__ ray_d, int n, int2 *hits,
+                                                       unsigned long long *stats) {
+  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  TraceCounters c;
+  bool overflow = false;
+  if (j < n) {
+    float4 o4 = ray_o[j], d4 = ray_d[j];
+    float t;
+    int h = Trace<false, kStats, kTri>(s, f3(o4.x, o4.y, o4.z), f3(d4.x, d4.y, d4.z), d4.w, &t, &c, &overflow);
+    hits[j] = make_int2(__float_as_int(t), h);
+  }
+  if (kStats) {
+    AddStat(stats, kStatBoxTests, c.box_tests);
+    AddStat(stats, kStatBoxHits, c.box_hits);
+    AddStat(stats, kStatPrimTests, c.prim_tests);
+    AddStat(stats, kStatPrimHits, c.prim_hits);
+  }
+  if (overflow) atomicAdd(stats + kStatOverflow, 1ull);
+}
+
+// Shadow queue entries are slot indices; slot k of path p is p * S + k. A
+// blocked slot's contribution is zeroed.
+template <bool kStats, int kTri>
+__global__ void __launch_bounds__(kBlock) OccludeKernel(DevScene s, const uint32_t *__restrict__ shq, int slots,
+                                                        int n, const float4 *__restrict__ org,
+                                                        const float4 *__restrict__ slot_dir, float4 *contrib,
+                                                        unsigned long long *stats) {
+  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  TraceCounters c;
+  bool overflow = false;
+  if (j < n) {
+    uint32_t slot = shq[j];
+    float4 o4 = org[slot / slots], d4 = slot_dir[slot];
+    float t;
+    int h = Trace<true, kStats, kTri>(s, f3(o4.x, o4.y, o4.z), f3(d4.x, d4.y, d4.z), d4.w, &t, &c, &overflow);
+    if (h >= 0) contrib[slot] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+  }
+  if (kStats) {
+    AddStat(stats, kStatBoxTests, c.box_tests);
+    AddStat(stats, kStatBoxHits, c.box_hits);
+    AddStat(stats, kStatPrimTests, c.prim_tests);
+    AddStat(stats, kStatPrimHits, c.prim_hits);
+  }
+  if (overflow) atomicAdd(stats + kStatOverflow, 1ull);
+}
+
+// ---- deterministic integrators --------------------------------------------
+// NormalsTracer / AlbedoTracer / DepthTracer (muon/integration.cc:47-72).
+__global__ void __launch_bounds__(kBlock) ShadeDebugKernel(DevScene s, PathBuffers b, int integrator, int n) {
+  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= n) return;
+  float4 o4 = b.ray_o[0][j], d4 = b.ray_d[0][j];
+  int path = __float_as_int(o4.w);
+  int2 h = b.hits[j];
+  float4 out = make_float4(0, 0, 0, 0);
+  if (h.y >= 0) {
+    float3 p, nrm;
+    int mat, light, pid;
+    float t = __int_as_float(h.x);
+    HitSurface(s, h.y, f3(o4.x, o4.y, o4.z), f3(d4.x, d4.y, d4.z), t, &p, &nrm, &mat, &light, &pid);
+    if (integrator == MUON_INTEGRATOR_NORMALS) {
+      out = make_float4(nrm.x * 0.5f + 0.5f, nrm.y * 0.5f + 0.5f, nrm.z * 0.5f + 0.5f, 0.0f);
+    } else if (integrator == MUON_INTEGRATOR_ALBEDO) {
+      Mat m = LoadMat(s.materials, mat);
+      out = make_float4(m.kd.x + m.ks.x, m.kd.y + m.ks.y, m.kd.z + m.ks.z, 0.0f);
+    } else {
+      float v = 1.0f / (1.0f + t);
+      out = make_float4(v, v, v, 0.0f);
+    }
+  }
+  b.rad[path] = out;
+}
+
+
+// ---- path tracer shading ----------------------------------------------------
+// PathTracer::Shade for one path vertex at depth `bounce`
+// (muon/integration.cc:205-328). Each shadow slot receives the radiance it
+// adds if its shadow ray is unblocked; the shadow rays themselves go to the
+// compacted queue as slot indices. The previous bounce's slots (already
+// resolved by the occlusion pass) are folded into the path radiance first.
+constexpr int kMaskSlots = 64;
+
+__global__ void __launch_bounds__(kBlock) ShadePathKernel(DevScene s, WaveInfo w, ShadeParams sp, PathBuffers b,
+                                                          int buf, int n, int bounce) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool active = j < n;
+  const int S = sp.slots;
+  uint32_t want_cont = 0, nshadow = 0;
+  unsigned long long mask = 0;  // nonzero slots (first 64)
+  int path = 0;
+  float3 cont_o = f3(0, 0, 0), cont_d = f3(0, 0, 0);
+  unsigned long long counted = 0;  // secondary rays in the reference's sense
+
+  if (active) {
+    const float4 o4 = b.ray_o[buf][j], d4 = b.ray_d[buf][j];
+    path = __float_as_int(o4.w);
+    const float3 o = f3(o4.x, o4.y, o4.z), d = f3(d4.x, d4.y, d4.z);
+    const int2 h = b.hits[j];
+    float4 *contrib = b.contrib + static_cast<int64_t>(path) * S;
+    float4 *sdir = b.slot_dir + static_cast<int64_t>(path) * S;
+    float4 r4 = b.rad[path];
+    float3 L = f3(r4.x, r4.y, r4.z);
+    if (bounce > 0) {
+      for (int k = 0; k < S; ++k) {
+        float4 c = contrib[k];
+        L = L + f3(c.x, c.y, c.z);
+        contrib[k] = make_float4(0, 0, 0, 0);
+      }
+    }
+    const float4 t4 = b.tp[path];
+    const float3 tp = f3(t4.x, t4.y, t4.z);
+
+    if (h.y >= 0) {
+      float3 p, nrm;
+      int mat_id, light_id, pid;
+      HitSurface(s, h.y, o, d, __int_as_float(h.x), &p, &nrm, &mat_id, &light_id, &pid);
+      const Mat m = LoadMat(s.materials, mat_id);
+      const float3 shift = p + kEps * nrm;
+      Rng rng = MakeRng(w, path, static_cast<uint32_t>(bounce));
+      auto emit = [&](int slot, float3 c, float3 dir, float maxd) {
+        contrib[slot] = make_float4(c.x, c.y, c.z, 0.0f);
+        sdir[slot] = make_float4(dir.x, dir.y, dir.z, maxd);
+        ++nshadow;
+        if (slot < kMaskSlots) mask |= 1ull << slot;
+      };
+
+      if (bounce >= sp.min_depth) {
+        // Emission: only at the first vertex when lights are sampled, and only
+        // from the front face (muon/integration.cc:257-264).
+        if ((sp.nee == MUON_NEE_OFF || bounce == 0) && !(dot3(nrm, -d) < 0.0f)) L = L + tp * m.ke;
+        if (sp.nee != MUON_NEE_OFF) {
+          const bool mis = sp.nee == MUON_NEE_MIS;
+          int slot = 0;
+          // Area lights: ShadeDirectNEE (muon/integration.cc:371-462).
+          for (int li = 0; li < s.num_lights; ++li) {
+            const DevLight &l = s.lights[li];
+            const float3 corner = f3(l.corner), e0 = f3(l.edge0), e1 = f3(l.edge1), rev = f3(l.rev_normal);
+            const float3 lcol = f3(l.color);
+            const float scale = l.color.w / static_cast<float>(sp.light_samples);
+            const float inv_strata = 1.0f / static_cast<float>(sp.strata);
+            for (int si = 0; si < sp.strata; ++si) {
+              for (int sj = 0; sj < sp.strata; ++sj) {
+                for (int sk = 0; sk < sp.per_section; ++sk, ++slot) {
+                  float u = rng.Next(), v = rng.Next();
+                  float fu = (static_cast<float>(si) + u) * inv_strata;
+                  float fv = (static_cast<float>(sj) + v) * inv_strata;
+                  float3 lp = corner + fu * e0 + fv * e1 - kEps * rev;
+                  float3 ptl = lp - shift;
+                  float dist = sqrtf(dot3(ptl, ptl));
+                  float3 ldir = ptl * (1.0f / dist);
+                  float ci = fmaxf(dot3(nrm, ldir), 0.0f);
+                  float cl = fmaxf(dot3(rev, ldir), 0.0f);
+                  if (ci == 0.0f || cl == 0.0f) continue;
+                  float3 c = BrdfEval(m, ldir, d, nrm) * (ci * cl / (dist * dist));
+                  if (mis) {
+                    float lpdf = NeePdf(s, shift, ldir);
+                    float bpdf = IsPdf(sp.is_mode, m, ldir, d, nrm);
+                    c = c * PowerHeuristic(lpdf, bpdf);
+                  }
+                  c = tp * lcol * (c * scale);
+                  if (nonzero3(c)) emit(slot, c, ldir, dist);
+                }
+              }
+            }
+          }
+          // Point and directional lights (muon/integration.cc:350-369,
+          // muon/lighting.cc:38-64).
+          for (int li = 0; li < s.num_other_lights; ++li, ++slot) {
+            const DevLight &l = s.other_lights[li];
+            float3 lcol = f3(l.color);
+            float3 ldir;
+            float dist;
+            if (__float_as_int(l.corner.w) == MUON_LIGHT_POINT) {
+              float3 ptl = f3(l.corner) - p;
+              ldir = normalize3(ptl);
+              dist = length3(ptl);
+              float att = l.edge0.x + l.edge0.y * dist + l.edge0.z * dist * dist;
+              lcol = lcol / att;
+              lcol = lcol / (dist * dist);
+            } else {
+              ldir = f3(l.corner);
+              dist = INFINITY;
+            }
+            float ci = fmaxf(dot3(nrm, ldir), 0.0f);
+            float3 c = tp * lcol * BrdfEval(m, ldir, d, nrm) * ci;
+            if (nonzero3(c)) emit(slot, c, ldir, dist);
+          }
+          // BRDF-sampled light hit: ShadeDirectImportanceSampling
+          // (muon/integration.cc:468-501). The sampled ray's closest hit is a
+          // light triangle exactly when some light triangle is hit at t_L and
+          // no primitive is hit before t_L, so it becomes an any-hit query up
+          // to t_L, and needs no traversal at all when it meets no light.
+          if (mis) {
+            float3 dir, ntp;
+            float bpdf;
+            if (SampleReflection(sp.is_mode, m, nrm, d, tp, rng, &dir, &bpdf, &ntp)) {
+              ++counted;
+              float best = INFINITY;
+              int best_light = -1;
+              if (sp.tri_test == MUON_TRI_WATERTIGHT) {
+                RayPre rp = Prepare<MUON_TRI_WATERTIGHT>(shift, dir);
+                for (int lt = 0; lt < 2 * s.num_lights; ++lt) {
+                  if (!s.light_tri_ok[lt]) continue;
+                  float t = TriWatertight(rp, LoadPrim(s.light_tris, lt));
+                  if (t > 0.0f && t < best) best = t, best_light = lt >> 1;
+                }
+              } else {
+                RayPre rp = Prepare<MUON_TRI_REFERENCE>(shift, dir);
+                for (int lt = 0; lt < 2 * s.num_lights; ++lt) {
+                  if (!s.light_tri_ok[lt]) continue;
+                  float t = TriReference(rp, LoadPrim(s.light_tris, lt));
+                  if (t > 0.0f && t < best) best = t, best_light = lt >> 1;
+                }
+              }
+              if (best_light >= 0) {
+                float wgt = PowerHeuristic(bpdf, NeePdf(s, shift, dir));
+                float3 c = ntp * f3(s.lights[best_light].color) * wgt;
+                if (nonzero3(c)) emit(sp.mis_slot, c, dir, best);
+              }
+            }
+          }
+        }
+      }
+      // Indirect: ShadeIndirect (muon/integration.cc:294-328).
+      float3 dir, ntp;
+      float pdf;
+      if (SampleReflection(sp.is_mode, m, nrm, d, tp, rng, &dir, &pdf, &ntp)) {
+        bool survive = true;
+        if (sp.rr) {
+          float q = fminf(max3c(ntp), 1.0f);
+          if (q < rng.Next()) survive = false;
+          else ntp = ntp / q;
+        }
+        const int next_depth = bounce + 1;
+        const bool depth_ok = sp.max_trace_depth < 0 || next_depth <= sp.max_trace_depth;
+        if (survive && depth_ok && next_depth < sp.max_bounces) {
+          want_cont = 1;
+          ++counted;
+          cont_o = shift;
+          cont_d = dir;
+          b.tp[path] = make_float4(ntp.x, ntp.y, ntp.z, 0.0f);
+        }
+      }
+      if (nshadow) b.org[path] = make_float4(shift.x, shift.y, shift.z, 0.0f);
+    }
+    b.rad[path] = make_float4(L.x, L.y, L.z, 0.0f);
+  }
+
+  uint32_t off_c, off_s;
+  BlockReserve(want_cont, nshadow, b.counters + kCntNext, b.counters + kCntShadow, &off_c, &off_s);
+  if (want_cont) {
+    b.ray_o[buf ^ 1][off_c] = make_float4(cont_o.x, cont_o.y, cont_o.z, __int_as_float(path));
+    b.ray_d[buf ^ 1][off_c] = make_float4(cont_d.x, cont_d.y, cont_d.z, INFINITY);
+  }
+  if (nshadow) {
+    const uint32_t base = static_cast<uint32_t>(path) * static_cast<uint32_t>(S);
+    uint32_t k = off_s;
+    if (S <= kMaskSlots) {
+      while (mask) {
+        int slot = __ffsll(static_cast<long long>(mask)) - 1;
+        mask &= mask - 1;
+        b.shq[k++] = base + slot;
+      }
+    } else {
+      const float4 *contrib = b.contrib + static_cast<int64_t>(path) * S;
+      for (int slot = 0; slot < S; ++slot) {
+        float4 c = contrib[slot];
+        if (c.x != 0.0f || c.y != 0.0f || c.z != 0.0f) b.shq[k++] = base + slot;
+      }
+    }
+  }
+  AddStat(b.stats, kStatSecondary, counted);
+}
+
+// ---- film ----------------------------------------------------------------------
+// Film::SetPixel accumulation (muon/film.cc:10-19) in FP64: one thread per
+// pixel adds its samples in sample order, so the film is reproducible.
+__global__ void __launch_bounds__(kBlock) FilmKernel(WaveInfo w, PathBuffers b, int slots, double *sum,
+                                                     double *sum_sq, uint32_t *count) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= w.npix) return;
+  const int pixel = w.p0 + i;
+  double s0 = 0, s1 = 0, s2 = 0, q0 = 0, q1 = 0, q2 = 0;
+  for (int k = 0; k < w.ns; ++k) {
+    const int path = i * w.ns + k;
+    float4 r = b.rad[path];
+    float x = r.x, y = r.y, z = r.z;
+    const float4 *c = b.contrib + static_cast<int64_t>(path) * slots;
+    for (int q = 0; q < slots; ++q) {
+      float4 v = c[q];
+      x += v.x, y += v.y, z += v.z;
+    }
+    s0 += x, s1 += y, s2 += z;
+    q0 += static_cast<double>(x) * x, q1 += static_cast<double>(y) * y, q2 += static_cast<double>(z) * z;
+  }
+  sum[3 * pixel + 0] += s0;
+  sum[3 * pixel + 1] += s1;
+  sum[3 * pixel + 2] += s2;
+  sum_sq[3 * pixel + 0] += q0;
+  sum_sq[3 * pixel + 1] += q1;
+  sum_sq[3 * pixel + 2] += q2;
+  count[pixel] += static_cast<uint32_t>(w.ns);
+}
+
+// ---- ray-level queries -----------------------------------------------------------
+// rays: n x 6 floats (origin, direction); out: n x 8 floats
+// (distance, prim id bits, position xyz, normal xyz).
+template <int kTri>
+__global__ void __launch_bounds__(kBlock) IntersectRaysKernel(DevScene s, const float *rays, int64_t n, float *out) {
+  int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float *r = rays + 6 * i;
+  float3 o = f3(r[0], r[1], r[2]), d = f3(r[3], r[4], r[5]);
+  TraceCounters c;
+  bool of = false;
+  float t;
+  int h = Trace<false, false, kTri>(s, o, d, INFINITY, &t, &c, &of);
+  float *q = out + 8 * i;
+  if (h < 0) {
+    q[0] = INFINITY;
+    q[1] = __int_as_float(-1);
+    for (int k = 2; k < 8; ++k) q[k] = 0.0f;
+    return;
+  }
+  float3 p, nrm;
+  int mat, light, pid;
+  HitSurface(s, h, o, d, t, &p, &nrm, &mat, &light, &pid);
+  q[0] = t;
+  q[1] = __int_as_float(pid);
+  q[2] = p.x, q[3] = p.y, q[4] = p.z;
+  q[5] = nrm.x, q[6] = nrm.y, q[7] = nrm.z;
+}
+
+template <int kTri>
+__global__ void __launch_bounds__(kBlock) OccludedRaysKernel(DevScene s, const float *rays, const float *maxd,
+                                                             int64_t n, uint8_t *out) {
+  int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float *r = rays + 6 * i;
+  TraceCounters c;
+  bool of = false;
+  float t;
+  int h = Trace<true, false, kTri>(s, f3(r[0], r[1], r[2]), f3(r[3], r[4], r[5]), maxd[i], &t, &c, &of);
+  out[i] = h >= 0 ? 1 : 0;
+}
+
+inline unsigned Blocks(int64_t n) { return static_cast<unsigned>((n + kBlock - 1) / kBlock); }
+
+}  // namespace
+
+void LaunchCamera(const DevCamera &cam, const WaveInfo &w, const PathBuffers &b, int slots, cudaStream_t st) {
+  if (w.n > 0) CameraKernel<<<Blocks(w.n), kBlock, 0, st>>>(cam, w, b, slots);
+}
+
+void LaunchExtend(const DevScene &s, const PathBuffers &b, int buf, int n, int tri_test, bool stats,
+                  cudaStream_t st) {
+  if (n <= 0) return;
+  if (tri_test == MUON_TRI_WATERTIGHT) {
+    if (stats) ExtendKernel<true, MUON_TRI_WATERTIGHT><<<Blocks(n), kBlock, 0, st>>>(s, b.ray_o[buf], b.ray_d[buf], n, b.hits, b.stats);
+    else ExtendKernel<false, MUON_TRI_WATERTIGHT><<<Blocks(n), kBlock, 0, st>>>(s, b.ray_o[buf], b.ray_d[buf], n, b.hits, b.stats);
+  } else {
+    if (stats) ExtendKernel<true, MUON_TRI_REFERENCE><<<Blocks(n), kBlock, 0, st>>>(s, b.ray_o[buf], b.ray_d[buf], n, b.hits, b.stats);
+    else ExtendKernel<false, MUON_TRI_REFERENCE><<<Blocks(n), kBlock, 0, st>>>(s, b.ray_o[buf], b.ray_d[buf], n, b.hits, b.stats);
+  }
+}
+
+void LaunchShadeDebug(const DevScene &s, const WaveInfo &w, const PathBuffers &b, int integrator, int n,
+                      cudaStream_t st) {
+  (void)w;
+  if (n > 0) ShadeDebugKernel<<<Blocks(n), kBlock, 0, st>>>(s, b, integrator, n);
+}
+
+void LaunchShadePath(const DevScene &s, const WaveInfo &w, const ShadeParams &sp, const PathBuffers &b, int buf,
+                     int n, int bounce, cudaStream_t st) {
+  if (n > 0) ShadePathKernel<<<Blocks(n), kBlock, 0, st>>>(s, w, sp, b, buf, n, bounce);
+}
+
+void LaunchOcclude(const DevScene &s, const PathBuffers &b, int slots, int n, int tri_test, bool stats,
+                   cudaStream_t st) {
+  if (n <= 0) return;
+  if (tri_test == MUON_TRI_WATERTIGHT) {
+    if (stats) OccludeKernel<true, MUON_TRI_WATERTIGHT><<<Blocks(n), kBlock, 0, st>>>(s, b.shq, slots, n, b.org, b.slot_dir, b.contrib, b.stats);
+    else OccludeKernel<false, MUON_TRI_WATERTIGHT><<<Blocks(n), kBlock, 0, st>>>(s, b.shq, slots, n, b.org, b.slot_dir, b.contrib, b.stats);
+  } else {
+    if (stats) OccludeKernel<true, MUON_TRI_REFERENCE><<<Blocks(n), kBlock, 0, st>>>(s, b.shq, slots, n, b.org, b.slot_dir, b.contrib, b.stats);
+    else OccludeKernel<false, MUON_TRI_REFERENCE><<<Blocks(n), kBlock, 0, st>>>(s, b.shq, slots, n, b.org, b.slot_dir, b.contrib, b.stats);
+  }
+}
+
+void LaunchFilm(const WaveInfo &w, const PathBuffers &b, int slots, double *sum, double *sum_sq, uint32_t *count,
+                cudaStream_t st) {
+  if (w.npix > 0) FilmKernel<<<Blocks(w.npix), kBlock, 0, st>>>(w, b, slots, sum, sum_sq, count);
+}
+
+void LaunchIntersectRays(const DevScene &s, const float *rays, int64_t n, int tri_test, float *out_hit,
+                         cudaStream_t st) {
+  if (n <= 0) return;
+  if (tri_test == MUON_TRI_WATERTIGHT) IntersectRaysKernel<MUON_TRI_WATERTIGHT><<<Blocks(n), kBlock, 0, st>>>(s, rays, n, out_hit);
+  else IntersectRaysKernel<MUON_TRI_REFERENCE><<<Blocks(n), kBlock, 0, st>>>(s, rays, n, out_hit);
+}
+
+void LaunchOccludedRays(const DevScene &s, const float *rays, const float *maxd, int64_t n, int tri_test,
+                        uint8_t *out, cudaStream_t st) {
+  if (n <= 0) return;
+  if (tri_test == MUON_TRI_WATERTIGHT) OccludedRaysKernel<MUON_TRI_WATERTIGHT><<<Blocks(n), kBlock, 0, st>>>(s, rays, maxd, n, out);
+  else OccludedRaysKernel<MUON_TRI_REFERENCE><<<Blocks(n), kBlock, 0, st>>>(s, rays, maxd, n, out);
+}
+
+}  // namespace muon_gpu

@@ -1,0 +1,539 @@
+// Device scene management, the wavefront render loop and the GPU entry points
+// of the C ABI (include/muon_gpu.h).
+//
+// The loop replaces Renderer::Render's thread pool (muon/renderer.cc:31-77):
+// instead of threads pulling row tiles and tracing one sample at a time, the
+// film's samples are cut into wavefronts of up to `wave_paths` paths and each
+// wavefront is advanced one bounce at a time by whole-GPU kernels.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <memory>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "host_scene.h"
+#include "kernels.cuh"
+#include "scene_build.h"
+
+using namespace muon_gpu;
+
+namespace {
+
+constexpr int kDefaultWavePaths = 1 << 21;
+constexpr int kMaxBounces = 256;  // hard cap for unbounded depth without Russian roulette
+constexpr int kMaxEventPairs = 4096;
+
+struct CudaError {
+  cudaError_t code;
+  const char *where;
+};
+
+#define CUDA_TRY(expr)                                                              \
+  do {                                                                              \
+    cudaError_t _e = (expr);                                                        \
+    if (_e != cudaSuccess) throw CudaError{_e, #expr};                              \
+  } while (0)
+
+struct DeviceBuffer {
+  void *ptr = nullptr;
+  size_t bytes = 0;
+  ~DeviceBuffer() {
+    if (ptr) cudaFree(ptr);
+  }
+  void Ensure(size_t want) {
+    if (want <= bytes && ptr) return;
+    if (ptr) cudaFree(ptr);
+    ptr = nullptr;
+    bytes = 0;
+    if (want == 0) return;
+    cudaError_t e = cudaMalloc(&ptr, want);
+    if (e != cudaSuccess) throw CudaError{e, "cudaMalloc"};
+    bytes = want;
+  }
+  template <typename T>
+  T *as() const {
+    return static_cast<T *>(ptr);
+  }
+};
+
+template <typename T>
+void Upload(DeviceBuffer &buf, const std::vector<T> &v, cudaStream_t st) {
+  buf.Ensure(std::max<size_t>(v.size() * sizeof(T), 16));
+  if (!v.empty()) CUDA_TRY(cudaMemcpyAsync(buf.ptr, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, st));
+}
+
+struct EventPair {
+  cudaEvent_t a = nullptr, b = nullptr;
+  int kind = 0;  // 0 extend, 1 occlude, 2 other
+};
+
+}  // namespace
+
+struct MuonScene {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  SceneImage img;
+  DevScene dev{};
+  DevCamera cam{};
+  // scene arrays
+  DeviceBuffer nodes, prims, shade, smooth, transforms, materials, lights, light_tris, light_tri_ok, other_lights;
+  // work arrays
+  DeviceBuffer ray_o[2], ray_d[2], hits, tp, rad, org, contrib, slot_dir, shq, counters, stats;
+  DeviceBuffer film_sum, film_sq, film_cnt, ray_in, ray_out, ray_aux;
+  int64_t wave_cap = 0;
+  int slots_cap = -1;
+  uint32_t *h_counters = nullptr;  // pinned
+  std::vector<EventPair> events;
+  int events_used = 0;
+  MuonStats last{};
+
+  ~MuonScene() {
+    for (EventPair &e : events) {
+      if (e.a) cudaEventDestroy(e.a);
+      if (e.b) cudaEventDestroy(e.b);
+    }
+    if (h_counters) cudaFreeHost(h_counters);
+    if (stream) cudaStreamDestroy(stream);
+  }
+
+  EventPair *NextEvent(int kind) {
+    if (events_used >= kMaxEventPairs) return nullptr;
+    if (events_used == static_cast<int>(events.size())) {
+      EventPair e;
+      CUDA_TRY(cudaEventCreate(&e.a));
+      CUDA_TRY(cudaEventCreate(&e.b));
+      events.push_back(e);
+    }
+    EventPair *e = &events[events_used++];
+    e->kind = kind;
+    return e;
+  }
+
+  PathBuffers Buffers() const {
+    PathBuffers b;
+    for (int k = 0; k < 2; ++k) {
+      b.ray_o[k] = ray_o[k].as<float4>();
+      b.ray_d[k] = ray_d[k].as<float4>();
+    }
+    b.hits = hits.as<int2>();
+    b.tp = tp.as<float4>();
+    b.rad = rad.as<float4>();
+    b.org = org.as<float4>();
+    b.contrib = contrib.as<float4>();
+    b.slot_dir = slot_dir.as<float4>();
+    b.shq = shq.as<uint32_t>();
+    b.counters = counters.as<uint32_t>();
+    b.stats = stats.as<unsigned long long>();
+    return b;
+  }
+
+  void EnsureWork(int64_t paths, int slots) {
+    if (paths <= wave_cap && slots <= slots_cap) return;
+    int64_t p = std::max(paths, wave_cap);
+    int s = std::max(slots, slots_cap);
+    for (int k = 0; k < 2; ++k) {
+      ray_o[k].Ensure(p * sizeof(float4));
+      ray_d[k].Ensure(p * sizeof(float4));
+    }
+    hits.Ensure(p * sizeof(int2));
+    tp.Ensure(p * sizeof(float4));
+    rad.Ensure(p * sizeof(float4));
+    org.Ensure(p * sizeof(float4));
+    size_t sl = static_cast<size_t>(p) * std::max(s, 1);
+    contrib.Ensure(sl * sizeof(float4));
+    slot_dir.Ensure(sl * sizeof(float4));
+    shq.Ensure(sl * sizeof(uint32_t));
+    wave_cap = p;
+    slots_cap = s;
+  }
+};
+
+namespace muon_gpu {
+namespace {
+thread_local std::string g_last_error;
+}
+void SetLastError(const std::string &msg) { g_last_error = msg; }
+const char *LastError() { return g_last_error.c_str(); }
+}  // namespace muon_gpu
+
+namespace {
+
+int Fail(int code, const std::string &msg) {
+  SetLastError(msg);
+  return code;
+}
+int FailCuda(const CudaError &e) {
+  return Fail(MUON_ERR_CUDA, std::string(e.where) + ": " + cudaGetErrorString(e.code));
+}
+
+void ComputeCamera(const MuonCameraDesc &c, DevCamera *out) {
+  // Camera::Camera (muon/camera.cc:15-35) in the reference's float order.
+  mm::v3 eye = mm::make3(c.eye[0], c.eye[1], c.eye[2]);
+  mm::v3 look = mm::make3(c.look_at[0], c.look_at[1], c.look_at[2]);
+  mm::v3 up = mm::make3(c.up[0], c.up[1], c.up[2]);
+  float tan_y = tanf(mm::radians(c.fov_y_degrees) / 2.0f);
+  float tan_x = tan_y * (static_cast<float>(c.width) / static_cast<float>(c.height));
+  mm::v3 w = mm::normalize(eye - look);
+  mm::v3 u = mm::normalize(mm::cross(up, w));
+  mm::v3 v = mm::cross(w, u);
+  const mm::v3 *src[4] = {&eye, &u, &v, &w};
+  float *dst[4] = {out->eye, out->u, out->v, out->w};
+  for (int k = 0; k < 4; ++k) {
+    dst[k][0] = src[k]->x;
+    dst[k][1] = src[k]->y;
+    dst[k][2] = src[k]->z;
+  }
+  out->tan_fov_x = tan_x;
+  out->tan_fov_y = tan_y;
+  out->width = c.width;
+  out->height = c.height;
+}
+
+int ValidateParams(const MuonRenderParams &p) {
+  if (p.integrator < MUON_INTEGRATOR_NORMALS || p.integrator > MUON_INTEGRATOR_PATHTRACER)
+    return Fail(MUON_ERR_INVALID_ARG, "unknown integrator");
+  if (p.integrator == MUON_INTEGRATOR_RAYTRACER || p.integrator == MUON_INTEGRATOR_ANALYTIC_DIRECT)
+    return Fail(MUON_ERR_INVALID_ARG, "integrator not available on the GPU path yet");
+  if (p.pixel_samples < 1) return Fail(MUON_ERR_INVALID_ARG, "pixel_samples must be >= 1");
+  if (p.next_event_estimation < MUON_NEE_OFF || p.next_event_estimation > MUON_NEE_MIS)
+    return Fail(MUON_ERR_INVALID_ARG, "unknown next_event_estimation mode");
+  if (p.importance_sampling < MUON_IS_HEMISPHERE || p.importance_sampling > MUON_IS_BRDF)
+    return Fail(MUON_ERR_INVALID_ARG, "unknown importance_sampling mode");
+  if (p.triangle_test != MUON_TRI_REFERENCE && p.triangle_test != MUON_TRI_WATERTIGHT)
+    return Fail(MUON_ERR_INVALID_ARG, "unknown triangle_test");
+  if (p.integrator == MUON_INTEGRATOR_PATHTRACER && p.next_event_estimation != MUON_NEE_OFF && p.light_samples < 1)
+    return Fail(MUON_ERR_INVALID_ARG, "light_samples must be >= 1");
+  if (p.max_depth < -1) return Fail(MUON_ERR_INVALID_ARG, "max_depth must be >= -1");
+  if (p.wave_paths < 0) return Fail(MUON_ERR_INVALID_ARG, "wave_paths must be >= 0");
+  return MUON_OK;
+}
+
+// Renders into a device film. Throws CudaError.
+void RenderDevice(MuonScene *sc, const MuonRenderParams &p, double *d_sum, double *d_sq, uint32_t *d_cnt) {
+  cudaStream_t st = sc->stream;
+  const bool pt = p.integrator == MUON_INTEGRATOR_PATHTRACER;
+  const bool stats_on = (p.flags & MUON_RENDER_STATS) != 0;
+  ShadeParams sp{};
+  sp.integrator = p.integrator;
+  sp.nee = p.next_event_estimation;
+  sp.is_mode = p.importance_sampling;
+  sp.rr = p.russian_roulette;
+  sp.min_depth = p.min_depth;
+  // Integrator::Trace casts a ray at depth d only if d <= max_depth (or
+  // max_depth - 1 when lights are sampled) (muon/integration.cc:29-33).
+  sp.max_trace_depth = p.max_depth < 0 ? -1 : (p.next_event_estimation != MUON_NEE_OFF ? p.max_depth - 1 : p.max_depth);
+  sp.strata = p.light_stratify ? static_cast<int>(std::sqrt(static_cast<double>(p.light_samples))) : 1;
+  sp.per_section = p.light_stratify ? 1 : p.light_samples;
+  sp.per_light = sp.strata * sp.strata * sp.per_section;
+  sp.light_samples = std::max(1, p.light_samples);
+  sp.tri_test = p.triangle_test;
+  sp.max_bounces = kMaxBounces;
+  int slots = 0;
+  sp.mis_slot = -1;
+  if (pt && p.next_event_estimation != MUON_NEE_OFF) {
+    slots = sc->dev.num_lights * sp.per_light + sc->dev.num_other_lights;
+    if (p.next_event_estimation == MUON_NEE_MIS) sp.mis_slot = slots++;
+  }
+  sp.slots = slots;
+
+  const int W = sc->img.width, H = sc->img.height;
+  const int64_t npix_total = static_cast<int64_t>(W) * H;
+  const int spp = p.pixel_samples;
+  int64_t budget = p.wave_paths > 0 ? p.wave_paths : kDefaultWavePaths;
+  // Keep per-wave slot storage within ~4 GiB.
+  const int64_t per_path = 160 + 36 * static_cast<int64_t>(std::max(slots, 1));
+  budget = std::max<int64_t>(1, std::min<int64_t>(budget, (int64_t(4) << 30) / per_path));
+  const int ns = static_cast<int>(std::min<int64_t>(spp, budget));
+  const int64_t pix_per_wave = std::max<int64_t>(1, budget / ns);
+  sc->EnsureWork(std::min<int64_t>(pix_per_wave, npix_total) * ns, slots);
+  sc->counters.Ensure(sizeof(uint32_t) * kNumCounters);
+  sc->stats.Ensure(sizeof(unsigned long long) * kNumStats);
+  CUDA_TRY(cudaMemsetAsync(sc->stats.ptr, 0, sizeof(unsigned long long) * kNumStats, st));
+  PathBuffers b = sc->Buffers();
+  sc->events_used = 0;
+
+  cudaEvent_t t0 = sc->NextEvent(2)->a, t1 = sc->events[0].b;
+  CUDA_TRY(cudaEventRecord(t0, st));
+  uint64_t primary = 0, shadow = 0, launches = 0;
+  const bool traces = !(p.max_depth >= 0 && sp.max_trace_depth < 0);
+  for (int64_t p0 = 0; p0 < npix_total; p0 += pix_per_wave) {
+    const int npix = static_cast<int>(std::min<int64_t>(pix_per_wave, npix_total - p0));
+    for (int s0 = 0; s0 < spp; s0 += ns) {
+      WaveInfo w{};
+      w.width = W;
+      w.p0 = static_cast<int32_t>(p0);
+      w.npix = npix;
+      w.s0 = s0;
+      w.ns = std::min(ns, spp - s0);
+      w.n = npix * w.ns;
+      w.sample_offset = static_cast<uint32_t>(p.sample_offset);
+      w.seed = p.seed;
+      LaunchCamera(sc->cam, w, b, slots, st);
+      ++launches;
+      int n_cur = w.n, buf = 0;
+      if (traces) {
+        primary += static_cast<uint64_t>(w.n);
+        for (int bounce = 0; n_cur > 0; ++bounce) {
+          EventPair *ev = sc->NextEvent(0);
+          if (ev) CUDA_TRY(cudaEventRecord(ev->a, st));
+          LaunchExtend(sc->dev, b, buf, n_cur, p.triangle_test, stats_on, st);
+          if (ev) CUDA_TRY(cudaEventRecord(ev->b, st));
+          ++launches;
+          if (!pt) {
+            LaunchShadeDebug(sc->dev, w, b, p.integrator, n_cur, st);
+            ++launches;
+            break;
+          }
+          CUDA_TRY(cudaMemsetAsync(b.counters, 0, sizeof(uint32_t) * kNumCounters, st));
+          LaunchShadePath(sc->dev, w, sp, b, buf, n_cur, bounce, st);
+          ++launches;
+          CUDA_TRY(cudaMemcpyAsync(sc->h_counters, b.counters, sizeof(uint32_t) * kNumCounters,
+                                   cudaMemcpyDeviceToHost, st));
+          CUDA_TRY(cudaStreamSynchronize(st));
+          const int n_sh = static_cast<int>(sc->h_counters[kCntShadow]);
+          const int n_next = static_cast<int>(sc->h_counters[kCntNext]);
+          if (n_sh > 0) {
+            EventPair *eo = sc->NextEvent(1);
+            if (eo) CUDA_TRY(cudaEventRecord(eo->a, st));
+            LaunchOcclude(sc->dev, b, slots, n_sh, p.triangle_test, stats_on, st);
+            if (eo) CUDA_TRY(cudaEventRecord(eo->b, st));
+            ++launches;
+          }
+          shadow += static_cast<uint64_t>(n_sh);
+          n_cur = n_next;
+          buf ^= 1;
+        }
+      }
+      LaunchFilm(w, b, slots, d_sum, d_sq, d_cnt, st);
+      ++launches;
+    }
+  }
+  CUDA_TRY(cudaEventRecord(t1, st));
+  CUDA_TRY(cudaGetLastError());
+  unsigned long long hstats[kNumStats];
+  CUDA_TRY(cudaMemcpyAsync(hstats, sc->stats.ptr, sizeof(hstats), cudaMemcpyDeviceToHost, st));
+  CUDA_TRY(cudaStreamSynchronize(st));
+  MuonStats &o = sc->last;
+  o = MuonStats{};
+  o.primary_rays = primary;
+  o.secondary_rays = hstats[kStatSecondary];
+  o.shadow_rays = shadow;
+  o.bounds_tests = hstats[kStatBoxTests];
+  o.bounds_hits = hstats[kStatBoxHits];
+  o.object_tests = hstats[kStatPrimTests];
+  o.object_hits = hstats[kStatPrimHits];
+  o.paths = static_cast<uint64_t>(npix_total) * spp;
+  o.kernel_launches = launches;
+  o.bvh_nodes = static_cast<uint64_t>(sc->img.nodes.size());
+  o.primitives = static_cast<uint64_t>(sc->img.num_prims);
+  float ms = 0.0f;
+  CUDA_TRY(cudaEventElapsedTime(&ms, t0, t1));
+  o.render_ms = ms;
+  for (int i = 1; i < sc->events_used; ++i) {
+    float e = 0.0f;
+    CUDA_TRY(cudaEventElapsedTime(&e, sc->events[i].a, sc->events[i].b));
+    if (sc->events[i].kind == 0) o.extend_ms += e;
+    else if (sc->events[i].kind == 1) o.occlude_ms += e;
+  }
+  o.shade_ms = std::max(0.0, o.render_ms - o.extend_ms - o.occlude_ms);
+  if (hstats[kStatOverflow]) SetLastError("BVH traversal stack overflowed; results may miss hits");
+}
+
+}  // namespace
+
+
+extern "C" {
+
+const char *muon_gpu_last_error(void) { return muon_gpu::LastError(); }
+
+int muon_gpu_scene_create(const MuonSceneDesc *desc, MuonScene **out) {
+  if (!desc || !out) return Fail(MUON_ERR_INVALID_ARG, "null argument");
+  *out = nullptr;
+  std::unique_ptr<MuonScene> sc;
+  try {
+    sc.reset(new MuonScene());
+    std::string err;
+    if (!BuildSceneImage(*desc, &sc->img, &err)) return Fail(MUON_ERR_INVALID_ARG, err);
+    if (sc->img.bvh.max_depth >= 60) return Fail(MUON_ERR_INVALID_ARG, "BVH too deep for the traversal stack");
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return Fail(MUON_ERR_CUDA, "no CUDA device available");
+    CUDA_TRY(cudaGetDevice(&sc->device));
+    CUDA_TRY(cudaStreamCreateWithFlags(&sc->stream, cudaStreamNonBlocking));
+    CUDA_TRY(cudaMallocHost(reinterpret_cast<void **>(&sc->h_counters), sizeof(uint32_t) * kNumCounters));
+    cudaStream_t st = sc->stream;
+    const SceneImage &im = sc->img;
+    Upload(sc->nodes, im.nodes, st);
+    Upload(sc->prims, im.prims, st);
+    Upload(sc->shade, im.shade, st);
+    Upload(sc->smooth, im.smooth_normals, st);
+    Upload(sc->transforms, im.transforms, st);
+    Upload(sc->materials, im.materials, st);
+    Upload(sc->lights, im.lights, st);
+    Upload(sc->other_lights, im.other_lights, st);
+    // The two triangles of each quad light (muon/parser.cc:735-747), in the
+    // same record format as the BVH's, for the MIS light-hit test.
+    std::vector<PrimRecord> lt(2 * im.lights.size());
+    std::vector<int32_t> lt_ok(2 * im.lights.size(), 0);
+    for (size_t i = 0; i < im.lights.size(); ++i) {
+      const DevLight &l = im.lights[i];
+      mm::v3 c = mm::make3(l.corner.x, l.corner.y, l.corner.z);
+      mm::v3 e0 = mm::make3(l.edge0.x, l.edge0.y, l.edge0.z), e1 = mm::make3(l.edge1.x, l.edge1.y, l.edge1.z);
+      mm::v3 va = c, vb = c + e0, vc = c + e1, vd = c + e0 + e1;
+      const mm::v3 tri[2][3] = {{va, vc, vb}, {vb, vc, vd}};
+      for (int t = 0; t < 2; ++t) {
+        mm::v3 n = mm::cross(tri[t][1] - tri[t][0], tri[t][2] - tri[t][0]);
+        PrimRecord &r = lt[2 * i + t];
+        r.p0 = F4{tri[t][0].x, tri[t][0].y, tri[t][0].z, mm::dot(tri[t][0], n)};
+        r.p1 = F4{tri[t][1].x, tri[t][1].y, tri[t][1].z, 1e-4f};
+        r.p2 = F4{tri[t][2].x, tri[t][2].y, tri[t][2].z, 0.0f};
+        r.p3 = F4{n.x, n.y, n.z, 0.0f};
+        lt_ok[2 * i + t] = mm::length(n) >= 1e-4f ? 1 : 0;
+      }
+    }
+    Upload(sc->light_tris, lt, st);
+    Upload(sc->light_tri_ok, lt_ok, st);
+    DevScene &d = sc->dev;
+    d.nodes = sc->nodes.as<BvhNode>();
+    d.prims = sc->prims.as<PrimRecord>();
+    d.shade = sc->shade.as<ShadeRecord>();
+    d.smooth_normals = im.any_smooth ? sc->smooth.as<F4>() : nullptr;
+    d.transforms = sc->transforms.as<DevTransform>();
+    d.materials = sc->materials.as<DevMaterial>();
+    d.lights = sc->lights.as<DevLight>();
+    d.light_tris = sc->light_tris.as<PrimRecord>();
+    d.light_tri_ok = sc->light_tri_ok.as<int32_t>();
+    d.other_lights = sc->other_lights.as<DevLight>();
+    d.num_nodes = static_cast<int32_t>(im.nodes.size());
+    d.num_lights = static_cast<int32_t>(im.lights.size());
+    d.num_other_lights = static_cast<int32_t>(im.other_lights.size());
+    ComputeCamera(im.camera, &sc->cam);
+    CUDA_TRY(cudaStreamSynchronize(st));
+  } catch (const CudaError &e) {
+    return FailCuda(e);
+  } catch (const std::bad_alloc &) {
+    return Fail(MUON_ERR_OOM, "host allocation failed");
+  }
+  *out = sc.release();
+  return MUON_OK;
+}
+
+void muon_gpu_scene_destroy(MuonScene *scene) { delete scene; }
+
+int muon_gpu_render_device(MuonScene *scene, const MuonRenderParams *params, double *d_sum, double *d_sum_sq,
+                           uint32_t *d_count) {
+  if (!scene || !params || !d_sum || !d_sum_sq || !d_count) return Fail(MUON_ERR_INVALID_ARG, "null argument");
+  int rc = ValidateParams(*params);
+  if (rc != MUON_OK) return rc;
+  try {
+    CUDA_TRY(cudaSetDevice(scene->device));
+    if (!(params->flags & MUON_RENDER_ACCUMULATE)) {
+      size_t np = static_cast<size_t>(scene->img.width) * scene->img.height;
+      CUDA_TRY(cudaMemsetAsync(d_sum, 0, 3 * np * sizeof(double), scene->stream));
+      CUDA_TRY(cudaMemsetAsync(d_sum_sq, 0, 3 * np * sizeof(double), scene->stream));
+      CUDA_TRY(cudaMemsetAsync(d_count, 0, np * sizeof(uint32_t), scene->stream));
+    }
+    RenderDevice(scene, *params, d_sum, d_sum_sq, d_count);
+  } catch (const CudaError &e) {
+    return FailCuda(e);
+  } catch (const std::bad_alloc &) {
+    return Fail(MUON_ERR_OOM, "host allocation failed");
+  }
+  return MUON_OK;
+}
+
+int muon_gpu_render(MuonScene *scene, const MuonRenderParams *params, MuonFilm *film) {
+  if (!scene || !params || !film || !film->sum || !film->sum_sq || !film->count)
+    return Fail(MUON_ERR_INVALID_ARG, "null argument");
+  if (film->width != scene->img.width || film->height != scene->img.height)
+    return Fail(MUON_ERR_INVALID_ARG, "film size does not match the scene");
+  int rc = ValidateParams(*params);
+  if (rc != MUON_OK) return rc;
+  try {
+    CUDA_TRY(cudaSetDevice(scene->device));
+    const size_t np = static_cast<size_t>(film->width) * film->height;
+    scene->film_sum.Ensure(3 * np * sizeof(double));
+    scene->film_sq.Ensure(3 * np * sizeof(double));
+    scene->film_cnt.Ensure(np * sizeof(uint32_t));
+    cudaStream_t st = scene->stream;
+    if (params->flags & MUON_RENDER_ACCUMULATE) {
+      CUDA_TRY(cudaMemcpyAsync(scene->film_sum.ptr, film->sum, 3 * np * sizeof(double), cudaMemcpyHostToDevice, st));
+      CUDA_TRY(cudaMemcpyAsync(scene->film_sq.ptr, film->sum_sq, 3 * np * sizeof(double), cudaMemcpyHostToDevice, st));
+      CUDA_TRY(cudaMemcpyAsync(scene->film_cnt.ptr, film->count, np * sizeof(uint32_t), cudaMemcpyHostToDevice, st));
+    } else {
+      CUDA_TRY(cudaMemsetAsync(scene->film_sum.ptr, 0, 3 * np * sizeof(double), st));
+      CUDA_TRY(cudaMemsetAsync(scene->film_sq.ptr, 0, 3 * np * sizeof(double), st));
+      CUDA_TRY(cudaMemsetAsync(scene->film_cnt.ptr, 0, np * sizeof(uint32_t), st));
+    }
+    RenderDevice(scene, *params, scene->film_sum.as<double>(), scene->film_sq.as<double>(),
+                 scene->film_cnt.as<uint32_t>());
+    CUDA_TRY(cudaMemcpyAsync(film->sum, scene->film_sum.ptr, 3 * np * sizeof(double), cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaMemcpyAsync(film->sum_sq, scene->film_sq.ptr, 3 * np * sizeof(double), cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaMemcpyAsync(film->count, scene->film_cnt.ptr, np * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaStreamSynchronize(st));
+  } catch (const CudaError &e) {
+    return FailCuda(e);
+  } catch (const std::bad_alloc &) {
+    return Fail(MUON_ERR_OOM, "host allocation failed");
+  }
+  return MUON_OK;
+}
+
+int muon_gpu_intersect(MuonScene *scene, const MuonRay *rays, int64_t n, int32_t triangle_test, MuonHit *hits) {
+  if (!scene || (n > 0 && (!rays || !hits)) || n < 0) return Fail(MUON_ERR_INVALID_ARG, "bad argument");
+  if (triangle_test != MUON_TRI_REFERENCE && triangle_test != MUON_TRI_WATERTIGHT)
+    return Fail(MUON_ERR_INVALID_ARG, "unknown triangle_test");
+  if (n == 0) return MUON_OK;
+  static_assert(sizeof(MuonRay) == 24 && sizeof(MuonHit) == 32, "ray/hit layout");
+  try {
+    CUDA_TRY(cudaSetDevice(scene->device));
+    cudaStream_t st = scene->stream;
+    scene->ray_in.Ensure(n * sizeof(MuonRay));
+    scene->ray_out.Ensure(n * sizeof(MuonHit));
+    CUDA_TRY(cudaMemcpyAsync(scene->ray_in.ptr, rays, n * sizeof(MuonRay), cudaMemcpyHostToDevice, st));
+    LaunchIntersectRays(scene->dev, scene->ray_in.as<float>(), n, triangle_test, scene->ray_out.as<float>(), st);
+    CUDA_TRY(cudaGetLastError());
+    CUDA_TRY(cudaMemcpyAsync(hits, scene->ray_out.ptr, n * sizeof(MuonHit), cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaStreamSynchronize(st));
+  } catch (const CudaError &e) {
+    return FailCuda(e);
+  }
+  return MUON_OK;
+}
+
+int muon_gpu_occluded(MuonScene *scene, const MuonRay *rays, const float *max_distance, int64_t n,
+                      int32_t triangle_test, uint8_t *occluded) {
+  if (!scene || (n > 0 && (!rays || !max_distance || !occluded)) || n < 0)
+    return Fail(MUON_ERR_INVALID_ARG, "bad argument");
+  if (triangle_test != MUON_TRI_REFERENCE && triangle_test != MUON_TRI_WATERTIGHT)
+    return Fail(MUON_ERR_INVALID_ARG, "unknown triangle_test");
+  if (n == 0) return MUON_OK;
+  try {
+    CUDA_TRY(cudaSetDevice(scene->device));
+    cudaStream_t st = scene->stream;
+    scene->ray_in.Ensure(n * sizeof(MuonRay));
+    scene->ray_aux.Ensure(n * sizeof(float));
+    scene->ray_out.Ensure(n);
+    CUDA_TRY(cudaMemcpyAsync(scene->ray_in.ptr, rays, n * sizeof(MuonRay), cudaMemcpyHostToDevice, st));
+    CUDA_TRY(cudaMemcpyAsync(scene->ray_aux.ptr, max_distance, n * sizeof(float), cudaMemcpyHostToDevice, st));
+    LaunchOccludedRays(scene->dev, scene->ray_in.as<float>(), scene->ray_aux.as<float>(), n, triangle_test,
+                       scene->ray_out.as<uint8_t>(), st);
+    CUDA_TRY(cudaGetLastError());
+    CUDA_TRY(cudaMemcpyAsync(occluded, scene->ray_out.ptr, n, cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaStreamSynchronize(st));
+  } catch (const CudaError &e) {
+    return FailCuda(e);
+  }
+  return MUON_OK;
+}
+
+int muon_gpu_stats(const MuonScene *scene, MuonStats *stats) {
+  if (!scene || !stats) return Fail(MUON_ERR_INVALID_ARG, "null argument");
+  *stats = scene->last;
+  return MUON_OK;
+}
+
+}  // extern "C"

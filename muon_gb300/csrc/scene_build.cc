@@ -1,0 +1,571 @@
+// Scene flattening and BVH construction on the host.
+//
+// The reference keeps primitives in object space and transforms every ray into
+// object space per primitive test (muon/objects.cc:29-46). Here triangles are
+// pre-transformed to world space once (the idea noted at muon/objects.h:65-66)
+// and the reference's parallel-ray rejection |d.n| < 1e-4, which the reference
+// applies to the object-space unnormalised normal and re-normalised direction
+// (muon/objects.cc:104-108), is carried over as a per-triangle world-space
+// threshold eps = 1e-4 * |n_world| / |n_object|. A triangle whose object-space
+// |n| is below 1e-4 can never pass that test in the reference, so it is left
+// out of the BVH (its primitive id stays reserved). Spheres keep their
+// transforms and are intersected in object space like the reference.
+//
+// The BVH replaces the reference's 12-bucket widest-axis SAH build
+// (muon/acceleration.cc:241-458): binned SAH over all three axes with a
+// bounded leaf size. Closest hits do not depend on the tree shape.
+#include "scene_build.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <limits>
+
+namespace muon_gpu {
+
+namespace {
+
+constexpr int kBins = 32;
+constexpr float kTraversalCost = 1.0f;
+constexpr float kIntersectCost = 1.0f;
+
+struct Ref {
+  float c[3];
+  int32_t idx;
+};
+
+struct BuildNode {
+  Aabb box;
+  int32_t left = -1, right = -1;  // children in the build array
+  int32_t start = 0, count = 0;   // leaf range in the ref array
+};
+
+Aabb EmptyBox() {
+  Aabb b;
+  for (int k = 0; k < 3; ++k) {
+    b.lo[k] = std::numeric_limits<float>::infinity();
+    b.hi[k] = -std::numeric_limits<float>::infinity();
+  }
+  return b;
+}
+void Grow(Aabb &b, const Aabb &o) {
+  for (int k = 0; k < 3; ++k) {
+    b.lo[k] = std::min(b.lo[k], o.lo[k]);
+    b.hi[k] = std::max(b.hi[k], o.hi[k]);
+  }
+}
+float Area(const Aabb &b) {
+  float dx = b.hi[0] - b.lo[0], dy = b.hi[1] - b.lo[1], dz = b.hi[2] - b.lo[2];
+  if (!(dx >= 0.0f) || !(dy >= 0.0f) || !(dz >= 0.0f)) return 0.0f;
+  return 2.0f * (dx * dy + dx * dz + dy * dz);
+}
+
+class Builder {
+ public:
+  Builder(const std::vector<Aabb> &boxes, int strategy, int max_leaf)
+      : boxes_(boxes), strategy_(strategy), max_leaf_(std::max(1, max_leaf)) {
+    refs_.resize(boxes.size());
+    for (size_t i = 0; i < boxes.size(); ++i) {
+      for (int k = 0; k < 3; ++k) refs_[i].c[k] = 0.5f * (boxes[i].lo[k] + boxes[i].hi[k]);
+      refs_[i].idx = static_cast<int32_t>(i);
+    }
+  }
+
+  int32_t Build(int32_t start, int32_t end, int depth) {
+    BuildNode node;
+    node.box = EmptyBox();
+    Aabb cbox = EmptyBox();
+    for (int32_t i = start; i < end; ++i) {
+      Grow(node.box, boxes_[refs_[i].idx]);
+      Aabb c;
+      for (int k = 0; k < 3; ++k) c.lo[k] = c.hi[k] = refs_[i].c[k];
+      Grow(cbox, c);
+    }
+    max_depth_ = std::max(max_depth_, depth);
+    int32_t n = end - start;
+    int32_t id = static_cast<int32_t>(nodes_.size());
+    nodes_.push_back(node);
+    if (n <= 1) return MakeLeaf(id, start, n);
+
+    int32_t mid = -1;
+    if (strategy_ == MUON_PARTITION_SAH) {
+      mid = SplitSah(start, end, node.box, cbox);
+    } else if (strategy_ == MUON_PARTITION_MIDPOINT) {
+      int axis = WidestAxis(cbox);
+      float m = 0.5f * (cbox.lo[axis] + cbox.hi[axis]);
+      Ref *p = std::partition(&refs_[start], &refs_[0] + end, [&](const Ref &r) { return r.c[axis] < m; });
+      mid = static_cast<int32_t>(p - &refs_[0]);
+      if (mid == start || mid == end) mid = -2;
+      if (n <= max_leaf_ && mid == -2) return MakeLeaf(id, start, n);
+    } else {
+      mid = -2;
+    }
+    if (mid == -1) return MakeLeaf(id, start, n);  // SAH chose a leaf
+    if (mid == -2) {
+      // Median split on the widest centroid axis (also the fallback when
+      // every centroid coincides).
+      int axis = WidestAxis(cbox);
+      mid = start + n / 2;
+      std::nth_element(&refs_[start], &refs_[mid], &refs_[0] + end,
+                       [&](const Ref &a, const Ref &b) { return a.c[axis] < b.c[axis]; });
+    }
+    int32_t l = Build(start, mid, depth + 1);
+    int32_t r = Build(mid, end, depth + 1);
+    nodes_[id].left = l;
+    nodes_[id].right = r;
+    return id;
+  }
+
+  std::vector<BuildNode> nodes_;
+  std::vector<Ref> refs_;
+  int max_depth_ = 0;
+  int64_t leaves_ = 0;
+  int max_leaf_seen_ = 0;
+
+ private:
+  static int WidestAxis(const Aabb &b) {
+    float d[3] = {b.hi[0] - b.lo[0], b.hi[1] - b.lo[1], b.hi[2] - b.lo[2]};
+    return d[0] > d[1] && d[0] > d[2] ? 0 : (d[1] > d[2] ? 1 : 2);
+  }
+
+  int32_t MakeLeaf(int32_t id, int32_t start, int32_t n) {
+    nodes_[id].start = start;
+    nodes_[id].count = n;
+    ++leaves_;
+    max_leaf_seen_ = std::max(max_leaf_seen_, n);
+    return id;
+  }
+
+  // Returns the split position, -1 for "make a leaf", -2 for "median split".
+  int32_t SplitSah(int32_t start, int32_t end, const Aabb &box, const Aabb &cbox) {
+    int32_t n = end - start;
+    float best_cost = std::numeric_limits<float>::infinity();
+    int best_axis = -1, best_bin = -1;
+    float parent_area = Area(box);
+    for (int axis = 0; axis < 3; ++axis) {
+      float extent = cbox.hi[axis] - cbox.lo[axis];
+      if (!(extent > 0.0f)) continue;
+      float scale = kBins / extent;
+      Aabb bin_box[kBins];
+      int32_t bin_n[kBins] = {0};
+      for (int b = 0; b < kBins; ++b) bin_box[b] = EmptyBox();
+      for (int32_t i = start; i < end; ++i) {
+        int b = std::min(kBins - 1, static_cast<int>((refs_[i].c[axis] - cbox.lo[axis]) * scale));
+        b = std::max(0, b);
+        ++bin_n[b];
+        Grow(bin_box[b], boxes_[refs_[i].idx]);
+      }
+      float right_area[kBins];
+      int32_t right_n[kBins];
+      Aabb acc = EmptyBox();
+      int32_t cnt = 0;
+      for (int b = kBins - 1; b > 0; --b) {
+        Grow(acc, bin_box[b]);
+        cnt += bin_n[b];
+        right_area[b] = Area(acc);
+        right_n[b] = cnt;
+      }
+      acc = EmptyBox();
+      cnt = 0;
+      for (int b = 0; b < kBins - 1; ++b) {
+        Grow(acc, bin_box[b]);
+        cnt += bin_n[b];
+        if (cnt == 0 || right_n[b + 1] == 0) continue;
+        float cost = Area(acc) * cnt + right_area[b + 1] * right_n[b + 1];
+        if (cost < best_cost) {
+          best_cost = cost;
+          best_axis = axis;
+          best_bin = b;
+        }
+      }
+    }
+    if (best_axis < 0) return n <= max_leaf_ ? -1 : -2;
+    float split_cost = kTraversalCost + kIntersectCost * best_cost / std::max(parent_area, 1e-30f);
+    float leaf_cost = kIntersectCost * n;
+    if (n <= max_leaf_ && leaf_cost <= split_cost) return -1;
+    float extent = cbox.hi[best_axis] - cbox.lo[best_axis];
+    float scale = kBins / extent;
+    float lo = cbox.lo[best_axis];
+    Ref *p = std::partition(&refs_[start], &refs_[0] + end, [&](const Ref &r) {
+      int b = std::min(kBins - 1, static_cast<int>((r.c[best_axis] - lo) * scale));
+      return std::max(0, b) <= best_bin;
+    });
+    int32_t mid = static_cast<int32_t>(p - &refs_[0]);
+    if (mid == start || mid == end) return -2;
+    return mid;
+  }
+
+  const std::vector<Aabb> &boxes_;
+  int strategy_;
+  int max_leaf_;
+};
+
+// Pads a box outwards by a few ulps so that rounding in the slab test cannot
+// cull a primitive whose own test reports a hit on the box surface.
+Aabb Pad(const Aabb &b) {
+  Aabb o = b;
+  for (int k = 0; k < 3; ++k) {
+    if (!(b.lo[k] <= b.hi[k])) continue;
+    float m = std::max(std::fabs(b.lo[k]), std::fabs(b.hi[k])) + (b.hi[k] - b.lo[k]);
+    float e = m * 4e-7f + 1e-30f;
+    o.lo[k] = b.lo[k] - e;
+    o.hi[k] = b.hi[k] + e;
+  }
+  return o;
+}
+
+void SetChild(BvhNode &n, int slot, const Aabb &b0, int32_t link) {
+  Aabb b = Pad(b0);
+  if (slot == 0) {
+    n.a.x = b.lo[0], n.a.y = b.hi[0], n.a.z = b.lo[1], n.a.w = b.hi[1];
+    n.c.x = b.lo[2], n.c.y = b.hi[2];
+    n.d.x = link;
+  } else {
+    n.b.x = b.lo[0], n.b.y = b.hi[0], n.b.z = b.lo[1], n.b.w = b.hi[1];
+    n.c.z = b.lo[2], n.c.w = b.hi[2];
+    n.d.y = link;
+  }
+}
+
+}  // namespace
+
+void BuildBvh(const std::vector<Aabb> &boxes, int accel, int strategy, int max_leaf,
+              std::vector<BvhNode> *nodes, std::vector<int32_t> *order, std::vector<uint8_t> *last,
+              BvhBuildStats *stats) {
+  nodes->clear();
+  order->clear();
+  last->clear();
+  *stats = BvhBuildStats();
+  if (boxes.empty()) return;
+  Builder b(boxes, strategy, accel == MUON_ACCEL_LINEAR ? static_cast<int>(boxes.size()) : max_leaf);
+  int32_t root;
+  if (accel == MUON_ACCEL_LINEAR) {
+    BuildNode leaf;
+    leaf.box = EmptyBox();
+    for (const Aabb &x : boxes) Grow(leaf.box, x);
+    leaf.start = 0;
+    leaf.count = static_cast<int32_t>(boxes.size());
+    b.nodes_.push_back(leaf);
+    b.leaves_ = 1;
+    b.max_leaf_seen_ = leaf.count;
+    root = 0;
+  } else {
+    root = b.Build(0, static_cast<int32_t>(boxes.size()), 0);
+  }
+  order->resize(boxes.size());
+  last->assign(boxes.size(), 0);
+  for (size_t i = 0; i < boxes.size(); ++i) (*order)[i] = b.refs_[i].idx;
+  const std::vector<BuildNode> &bn = b.nodes_;
+  for (const BuildNode &x : bn) {
+    if (x.left < 0 && x.count > 0) (*last)[x.start + x.count - 1] = 1;
+  }
+
+  // Depth-first flattening: each interior build node becomes one 64-byte
+  // node holding its two children's boxes.
+  auto link_of = [&](int32_t id, std::vector<int32_t> &pending) -> int32_t {
+    const BuildNode &x = bn[id];
+    if (x.left < 0) return ~x.start;
+    pending.push_back(id);
+    return 0;  // patched below
+  };
+  nodes->reserve(bn.size() / 2 + 1);
+  double sah = 0.0;
+  float root_area = std::max(Area(bn[root].box), 1e-30f);
+  if (bn[root].left < 0) {
+    BvhNode n{};
+    SetChild(n, 0, bn[root].box, ~bn[root].start);
+    SetChild(n, 1, EmptyBox(), kEmptyLink);
+    nodes->push_back(n);
+  } else {
+    // Explicit stack of (build node, output slot).
+    struct Item {
+      int32_t build;
+      int32_t out;
+    };
+    std::vector<Item> stack;
+    nodes->push_back(BvhNode{});
+    stack.push_back({root, 0});
+    while (!stack.empty()) {
+      Item it = stack.back();
+      stack.pop_back();
+      const BuildNode &x = bn[it.build];
+      sah += kTraversalCost * Area(x.box) / root_area;
+      int32_t kids[2] = {x.left, x.right};
+      for (int s = 0; s < 2; ++s) {
+        const BuildNode &k = bn[kids[s]];
+        int32_t link;
+        if (k.left < 0) {
+          link = ~k.start;
+          sah += kIntersectCost * k.count * Area(k.box) / root_area;
+        } else {
+          link = static_cast<int32_t>(nodes->size());
+          nodes->push_back(BvhNode{});
+          stack.push_back({kids[s], link});
+        }
+        SetChild((*nodes)[it.out], s, k.box, link);
+      }
+    }
+  }
+  (void)link_of;
+  stats->nodes = static_cast<int64_t>(nodes->size());
+  stats->leaves = b.leaves_;
+  stats->max_depth = b.max_depth_;
+  stats->max_leaf = b.max_leaf_seen_;
+  stats->sah_cost = sah;
+}
+
+namespace {
+
+mm::m4 ToM4(const float *m) {
+  mm::m4 r;
+  std::memcpy(&r, m, sizeof(float) * 16);
+  return r;
+}
+void PackRows(const mm::m4 &m, float *out) {
+  for (int c = 0; c < 4; ++c) {
+    out[3 * c + 0] = m.c[c].x;
+    out[3 * c + 1] = m.c[c].y;
+    out[3 * c + 2] = m.c[c].z;
+  }
+}
+F4 MakeF4(float x, float y, float z, float w) { return F4{x, y, z, w}; }
+float IntBits(int32_t v) {
+  float f;
+  std::memcpy(&f, &v, 4);
+  return f;
+}
+mm::v3 V3(const float *p) { return mm::make3(p[0], p[1], p[2]); }
+
+// Lobe-selection probability of the reference BRDFs (Phong::reflectiveness,
+// muon/materials.cc:113-123; GGX::reflectiveness, muon/materials.cc:270-293).
+float Reflectiveness(const MuonMaterialDesc &m) {
+  float specular = (m.specular[0] + m.specular[1] + m.specular[2]) / 3.0f;
+  float diffuse = (m.diffuse[0] + m.diffuse[1] + m.diffuse[2]) / 3.0f;
+  float denom = diffuse + specular;
+  if (m.brdf == MUON_BRDF_GGX) {
+    if (denom == 0.0f) return 1.0f;
+    return mm::fmax_ref(specular / denom, 0.25f);
+  }
+  return denom > 0.0f ? specular / denom : 0.0f;
+}
+
+}  // namespace
+
+bool BuildSceneImage(const MuonSceneDesc &desc, SceneImage *img, std::string *error) {
+  if (desc.num_triangles < 0 || desc.num_spheres < 0 || desc.num_materials < 0 ||
+      desc.num_lights < 0 || desc.num_transforms < 0) {
+    *error = "negative array size in scene description";
+    return false;
+  }
+  if ((desc.num_triangles > 0 && !desc.triangles) || (desc.num_spheres > 0 && !desc.spheres) ||
+      (desc.num_materials > 0 && !desc.materials) || (desc.num_lights > 0 && !desc.lights) ||
+      (desc.num_transforms > 0 && !desc.transforms)) {
+    *error = "null array in scene description";
+    return false;
+  }
+  if (desc.width <= 0 || desc.height <= 0 || desc.camera.width <= 0 || desc.camera.height <= 0) {
+    *error = "film and camera sizes must be positive";
+    return false;
+  }
+  const int64_t ntri = desc.num_triangles, nsph = desc.num_spheres;
+  img->num_prims = ntri + nsph;
+  img->camera = desc.camera;
+  img->width = desc.width;
+  img->height = desc.height;
+
+  // Transforms.
+  img->transforms.resize(desc.num_transforms);
+  for (int32_t i = 0; i < desc.num_transforms; ++i) {
+    DevTransform &t = img->transforms[i];
+    std::memset(&t, 0, sizeof(t));
+    PackRows(ToM4(desc.transforms[i].object_to_world), t.o2w);
+    PackRows(ToM4(desc.transforms[i].world_to_object), t.w2o);
+    PackRows(ToM4(desc.transforms[i].normal_to_world), t.n2w);
+  }
+  // Materials.
+  img->materials.resize(desc.num_materials);
+  for (int32_t i = 0; i < desc.num_materials; ++i) {
+    const MuonMaterialDesc &m = desc.materials[i];
+    if (m.brdf < MUON_BRDF_LAMBERTIAN || m.brdf > MUON_BRDF_GGX) {
+      *error = "material has an unknown brdf";
+      return false;
+    }
+    DevMaterial &d = img->materials[i];
+    d.diffuse = MakeF4(m.diffuse[0], m.diffuse[1], m.diffuse[2], m.shininess);
+    d.specular = MakeF4(m.specular[0], m.specular[1], m.specular[2], m.roughness);
+    d.emission = MakeF4(m.emission[0], m.emission[1], m.emission[2], IntBits(m.brdf));
+    d.ambient = MakeF4(m.ambient[0], m.ambient[1], m.ambient[2], Reflectiveness(m));
+  }
+  // Lights: quad lights feed NEE/MIS; the others only the ray tracer.
+  std::vector<int32_t> quad_index(desc.num_lights, -1);
+  for (int32_t i = 0; i < desc.num_lights; ++i) {
+    const MuonLightDesc &l = desc.lights[i];
+    DevLight d{};
+    d.corner = MakeF4(l.p0[0], l.p0[1], l.p0[2], IntBits(l.type));
+    mm::v3 e0 = V3(l.p1), e1 = V3(l.p2);
+    d.edge0 = MakeF4(e0.x, e0.y, e0.z, mm::length(e0));
+    d.edge1 = MakeF4(e1.x, e1.y, e1.z, mm::length(e1));
+    mm::v3 c01 = mm::cross(e0, e1);
+    d.color = MakeF4(l.color[0], l.color[1], l.color[2], mm::length(c01));
+    mm::v3 rn = mm::normalize(c01);
+    d.rev_normal = MakeF4(rn.x, rn.y, rn.z, 0.0f);
+    mm::v3 qn = mm::normalize(mm::cross(e1, e0));
+    d.quad_normal = MakeF4(qn.x, qn.y, qn.z, 0.0f);
+    if (l.type == MUON_LIGHT_QUAD) {
+      quad_index[i] = static_cast<int32_t>(img->lights.size());
+      img->lights.push_back(d);
+    } else if (l.type == MUON_LIGHT_POINT || l.type == MUON_LIGHT_DIRECTIONAL) {
+      d.edge0 = MakeF4(l.p1[0], l.p1[1], l.p1[2], 0.0f);  // attenuation for point lights
+      img->other_lights.push_back(d);
+    } else {
+      *error = "light has an unknown type";
+      return false;
+    }
+  }
+
+  auto check_index = [&](int32_t v, int32_t n, const char *what) {
+    if (v < -1 || v >= n) {
+      *error = std::string("primitive refers to a missing ") + what;
+      return false;
+    }
+    return true;
+  };
+
+  // World-space primitive data and bounds.
+  std::vector<Aabb> boxes;
+  std::vector<int64_t> source;  // box -> primitive (tri i, or ntri + sphere j)
+  boxes.reserve(ntri + nsph);
+  source.reserve(ntri + nsph);
+  std::vector<PrimRecord> tri_rec(ntri);
+  std::vector<ShadeRecord> tri_shade(ntri);
+  std::vector<F4> tri_normals;
+  img->any_smooth = false;
+  for (int64_t i = 0; i < ntri; ++i) img->any_smooth |= desc.triangles[i].smooth != 0;
+  if (img->any_smooth) tri_normals.resize(3 * ntri);
+  img->leaf_of_prim_id.assign(img->num_prims, -1);
+
+  for (int64_t i = 0; i < ntri; ++i) {
+    const MuonTriangleDesc &t = desc.triangles[i];
+    if (!check_index(t.transform, desc.num_transforms, "transform") ||
+        !check_index(t.material, desc.num_materials, "material") || t.material < 0 ||
+        !check_index(t.light, desc.num_lights, "light")) {
+      return false;
+    }
+    if (t.prim_id < 0 || t.prim_id >= img->num_prims) {
+      *error = "primitive id out of range";
+      return false;
+    }
+    mm::v3 ov[3] = {V3(t.v[0]), V3(t.v[1]), V3(t.v[2])};
+    mm::v3 wv[3];
+    mm::m4 m = t.transform >= 0 ? ToM4(desc.transforms[t.transform].object_to_world) : mm::identity4();
+    for (int k = 0; k < 3; ++k) wv[k] = t.transform >= 0 ? mm::xform_point(m, ov[k]) : ov[k];
+    mm::v3 n_obj = mm::cross(ov[1] - ov[0], ov[2] - ov[0]);
+    mm::v3 n_w = mm::cross(wv[1] - wv[0], wv[2] - wv[0]);
+    float len_obj = mm::length(n_obj);
+    float eps = 1e-4f;
+    if (t.transform >= 0) eps = 1e-4f * (mm::length(n_w) / len_obj);
+    PrimRecord &r = tri_rec[i];
+    r.p0 = MakeF4(wv[0].x, wv[0].y, wv[0].z, mm::dot(wv[0], n_w));
+    r.p1 = MakeF4(wv[1].x, wv[1].y, wv[1].z, eps);
+    r.p2 = MakeF4(wv[2].x, wv[2].y, wv[2].z, 0.0f);
+    uint32_t flags = t.smooth ? kPrimSmooth : 0u;
+    r.p3 = MakeF4(n_w.x, n_w.y, n_w.z, 0.0f);
+    // Shading normal as the reference forms it: the unit object-space normal
+    // carried by the inverse transpose and normalised again (muon/objects.cc:
+    // 40-41, 165-167); for a mirroring transform it points against n_w.
+    mm::m4 nt0 = t.transform >= 0 ? ToM4(desc.transforms[t.transform].normal_to_world) : mm::identity4();
+    mm::v3 un = mm::xform_dir(nt0, mm::normalize(n_obj));
+    ShadeRecord &s = tri_shade[i];
+    s.s0 = MakeF4(un.x, un.y, un.z, IntBits(t.material));
+    s.s1 = I4{t.light >= 0 ? quad_index[t.light] : -1, t.prim_id, t.transform, static_cast<int32_t>(flags)};
+    std::memcpy(&r.p3.w, &flags, 4);
+    if (t.smooth) {
+      // normalize(M^-T (w n0 + u n1 + v n2)) equals the normalised blend of
+      // the pre-transformed vertex normals, by linearity.
+      mm::m4 nt = t.transform >= 0 ? ToM4(desc.transforms[t.transform].normal_to_world) : mm::identity4();
+      for (int k = 0; k < 3; ++k) {
+        mm::v3 vn = V3(t.n[k]);
+        mm::v4 w4 = t.transform >= 0 ? mm::mul(nt, mm::v4{vn.x, vn.y, vn.z, 0.0f}) : mm::v4{vn.x, vn.y, vn.z, 0.0f};
+        tri_normals[3 * i + k] = MakeF4(w4.x, w4.y, w4.z, 0.0f);
+      }
+    }
+    // |d.n| <= |n| for a unit direction, so such a triangle is never hit.
+    if (!(len_obj >= 1e-4f)) continue;
+    Aabb b;
+    for (int k = 0; k < 3; ++k) {
+      b.lo[k] = std::min(std::min(mm::comp(wv[0], k), mm::comp(wv[1], k)), mm::comp(wv[2], k));
+      b.hi[k] = std::max(std::max(mm::comp(wv[0], k), mm::comp(wv[1], k)), mm::comp(wv[2], k));
+    }
+    boxes.push_back(b);
+    source.push_back(i);
+  }
+  std::vector<PrimRecord> sph_rec(nsph);
+  std::vector<ShadeRecord> sph_shade(nsph);
+  for (int64_t j = 0; j < nsph; ++j) {
+    const MuonSphereDesc &s = desc.spheres[j];
+    if (!check_index(s.transform, desc.num_transforms, "transform") ||
+        !check_index(s.material, desc.num_materials, "material") || s.material < 0) {
+      return false;
+    }
+    if (s.prim_id < 0 || s.prim_id >= img->num_prims) {
+      *error = "primitive id out of range";
+      return false;
+    }
+    PrimRecord &r = sph_rec[j];
+    uint32_t flags = kPrimSphere;
+    r.p0 = MakeF4(s.center[0], s.center[1], s.center[2], s.radius);
+    r.p1 = MakeF4(0.0f, IntBits(s.transform), 0.0f, 0.0f);
+    r.p2 = MakeF4(0, 0, 0, 0);
+    r.p3 = MakeF4(0, 0, 0, 0);
+    std::memcpy(&r.p3.w, &flags, 4);
+    ShadeRecord &sh = sph_shade[j];
+    sh.s0 = MakeF4(0, 0, 0, IntBits(s.material));
+    sh.s1 = I4{-1, s.prim_id, s.transform, static_cast<int32_t>(flags)};
+    // World bounds: the object box's 8 corners transformed (Bounds::Transform,
+    // muon/bounds.cc:52-69).
+    mm::v3 c = V3(s.center);
+    mm::v3 lo = c - mm::splat3(s.radius), hi = c + mm::splat3(s.radius);
+    Aabb b;
+    if (s.transform < 0) {
+      for (int k = 0; k < 3; ++k) b.lo[k] = mm::comp(lo, k), b.hi[k] = mm::comp(hi, k);
+    } else {
+      mm::m4 m = ToM4(desc.transforms[s.transform].object_to_world);
+      b = EmptyBox();
+      for (int corner = 0; corner < 8; ++corner) {
+        mm::v3 p = mm::make3(corner & 1 ? hi.x : lo.x, corner & 2 ? hi.y : lo.y, corner & 4 ? hi.z : lo.z);
+        mm::v3 w = mm::xform_point(m, p);
+        Aabb pb;
+        for (int k = 0; k < 3; ++k) pb.lo[k] = pb.hi[k] = mm::comp(w, k);
+        Grow(b, pb);
+      }
+    }
+    boxes.push_back(b);
+    source.push_back(ntri + j);
+  }
+
+  std::vector<int32_t> order;
+  std::vector<uint8_t> last;
+  int max_leaf = desc.max_leaf_size > 0 ? desc.max_leaf_size : 4;
+  BuildBvh(boxes, desc.acceleration, desc.partition_strategy, max_leaf, &img->nodes, &order, &last, &img->bvh);
+  img->prims.resize(order.size());
+  img->shade.resize(order.size());
+  if (img->any_smooth) img->smooth_normals.resize(3 * order.size());
+  for (size_t slot = 0; slot < order.size(); ++slot) {
+    int64_t src = source[order[slot]];
+    PrimRecord r = src < ntri ? tri_rec[src] : sph_rec[src - ntri];
+    ShadeRecord s = src < ntri ? tri_shade[src] : sph_shade[src - ntri];
+    uint32_t flags;
+    std::memcpy(&flags, &r.p3.w, 4);
+    if (last[slot]) flags |= kPrimLast;
+    std::memcpy(&r.p3.w, &flags, 4);
+    img->prims[slot] = r;
+    img->shade[slot] = s;
+    img->leaf_of_prim_id[s.s1.y] = static_cast<int32_t>(slot);
+    if (img->any_smooth && src < ntri) {
+      for (int k = 0; k < 3; ++k) img->smooth_normals[3 * slot + k] = tri_normals[3 * src + k];
+    }
+  }
+  return true;
+}
+
+}  // namespace muon_gpu

@@ -1,0 +1,55 @@
+// Host-side construction of the device scene image: world-space primitive
+// records, shading records, the flattened BVH, materials and lights.
+#pragma once
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/muon_gpu.h"
+#include "dev_layout.h"
+#include "mmath.h"
+
+namespace muon_gpu {
+
+struct Aabb {
+  float lo[3], hi[3];
+};
+
+struct BvhBuildStats {
+  int64_t nodes = 0;
+  int64_t leaves = 0;
+  int32_t max_depth = 0;
+  int32_t max_leaf = 0;
+  double sah_cost = 0.0;
+};
+
+// Builds a binary BVH over `boxes` and flattens it into 64-byte two-child
+// nodes. `order` receives, for each leaf-order slot, the index of the input
+// box; `last` marks the final slot of each leaf. strategy is MUON_PARTITION_*;
+// accel MUON_ACCEL_LINEAR puts every primitive into one leaf.
+void BuildBvh(const std::vector<Aabb> &boxes, int accel, int strategy, int max_leaf,
+              std::vector<BvhNode> *nodes, std::vector<int32_t> *order, std::vector<uint8_t> *last,
+              BvhBuildStats *stats);
+
+struct SceneImage {
+  std::vector<BvhNode> nodes;
+  std::vector<PrimRecord> prims;          // leaf order
+  std::vector<ShadeRecord> shade;         // leaf order
+  std::vector<F4> smooth_normals;         // 3 per leaf slot when any triangle is smooth
+  std::vector<DevTransform> transforms;
+  std::vector<DevMaterial> materials;
+  std::vector<DevLight> lights;           // quad lights only
+  std::vector<DevLight> other_lights;     // point / directional lights
+  std::vector<int32_t> leaf_of_prim_id;   // parse-order id -> leaf slot (-1 = never hit)
+  int64_t num_prims = 0;                  // primitives in the scene, including never-hit ones
+  bool any_smooth = false;
+  MuonCameraDesc camera{};
+  int32_t width = 0, height = 0;
+  BvhBuildStats bvh;
+};
+
+// Flattens a scene description. Returns false with a message on invalid input.
+bool BuildSceneImage(const MuonSceneDesc &desc, SceneImage *img, std::string *error);
+
+}  // namespace muon_gpu

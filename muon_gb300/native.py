@@ -1,0 +1,151 @@
+"""ctypes view of include/muon_gpu.h and the loader for libmuon_gpu.so.
+
+The library is built in-tree by muon_gb300/build.py. There is no fallback: if
+the shared library cannot be loaded, every call raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "lib", "libmuon_gpu.so")
+HEADER = os.path.join(HERE, "..", "include", "muon_gpu.h")
+
+MUON_OK = 0
+ERRORS = {1: "invalid argument", 2: "out of memory", 3: "CUDA error", 4: "device timeout", 5: "parse error", 6: "I/O error"}
+
+INTEGRATORS = {"normals": 0, "albedo": 1, "depth": 2, "raytracer": 3, "analyticdirect": 4, "pathtracer": 5}
+NEE = {"off": 0, "on": 1, "mis": 2}
+IMPORTANCE = {"hemisphere": 0, "cosine": 1, "brdf": 2}
+TRI_REFERENCE, TRI_WATERTIGHT = 0, 1
+ACCEL_LINEAR, ACCEL_BVH = 0, 1
+PARTITION = {"uniform": 0, "midpoint": 1, "sah": 2}
+RENDER_STATS, RENDER_ACCUMULATE = 1, 2
+
+
+class TransformDesc(C.Structure):
+    _fields_ = [("object_to_world", C.c_float * 16), ("world_to_object", C.c_float * 16),
+                ("normal_to_world", C.c_float * 16)]
+
+
+class MaterialDesc(C.Structure):
+    _fields_ = [("ambient", C.c_float * 3), ("diffuse", C.c_float * 3), ("specular", C.c_float * 3),
+                ("emission", C.c_float * 3), ("shininess", C.c_float), ("roughness", C.c_float),
+                ("brdf", C.c_int32), ("pad", C.c_int32)]
+
+
+class LightDesc(C.Structure):
+    _fields_ = [("type", C.c_int32), ("color", C.c_float * 3), ("p0", C.c_float * 3), ("p1", C.c_float * 3),
+                ("p2", C.c_float * 3)]
+
+
+class TriangleDesc(C.Structure):
+    _fields_ = [("v", (C.c_float * 3) * 3), ("n", (C.c_float * 3) * 3), ("transform", C.c_int32),
+                ("material", C.c_int32), ("light", C.c_int32), ("smooth", C.c_int32), ("prim_id", C.c_int32),
+                ("pad", C.c_int32)]
+
+
+class SphereDesc(C.Structure):
+    _fields_ = [("center", C.c_float * 3), ("radius", C.c_float), ("transform", C.c_int32),
+                ("material", C.c_int32), ("prim_id", C.c_int32), ("pad", C.c_int32)]
+
+
+class CameraDesc(C.Structure):
+    _fields_ = [("eye", C.c_float * 3), ("look_at", C.c_float * 3), ("up", C.c_float * 3),
+                ("fov_y_degrees", C.c_float), ("width", C.c_int32), ("height", C.c_int32)]
+
+
+class SceneDesc(C.Structure):
+    _fields_ = [("width", C.c_int32), ("height", C.c_int32), ("camera", CameraDesc),
+                ("transforms", C.POINTER(TransformDesc)), ("num_transforms", C.c_int32),
+                ("materials", C.POINTER(MaterialDesc)), ("num_materials", C.c_int32),
+                ("lights", C.POINTER(LightDesc)), ("num_lights", C.c_int32),
+                ("triangles", C.POINTER(TriangleDesc)), ("num_triangles", C.c_int64),
+                ("spheres", C.POINTER(SphereDesc)), ("num_spheres", C.c_int64),
+                ("acceleration", C.c_int32), ("partition_strategy", C.c_int32), ("max_leaf_size", C.c_int32),
+                ("pad", C.c_int32)]
+
+
+class RenderParams(C.Structure):
+    _fields_ = [("integrator", C.c_int32), ("pixel_samples", C.c_int32), ("light_samples", C.c_int32),
+                ("light_stratify", C.c_int32), ("next_event_estimation", C.c_int32),
+                ("russian_roulette", C.c_int32), ("importance_sampling", C.c_int32), ("min_depth", C.c_int32),
+                ("max_depth", C.c_int32), ("sample_offset", C.c_int32), ("seed", C.c_uint64),
+                ("triangle_test", C.c_int32), ("wave_paths", C.c_int32), ("flags", C.c_uint32),
+                ("pad", C.c_int32)]
+
+
+class Film(C.Structure):
+    _fields_ = [("width", C.c_int32), ("height", C.c_int32), ("sum", C.POINTER(C.c_double)),
+                ("sum_sq", C.POINTER(C.c_double)), ("count", C.POINTER(C.c_uint32))]
+
+
+class Ray(C.Structure):
+    _fields_ = [("origin", C.c_float * 3), ("direction", C.c_float * 3)]
+
+
+class Hit(C.Structure):
+    _fields_ = [("distance", C.c_float), ("prim_id", C.c_int32), ("position", C.c_float * 3),
+                ("normal", C.c_float * 3)]
+
+
+class Stats(C.Structure):
+    _fields_ = [("primary_rays", C.c_uint64), ("secondary_rays", C.c_uint64), ("shadow_rays", C.c_uint64),
+                ("object_tests", C.c_uint64), ("object_hits", C.c_uint64), ("bounds_tests", C.c_uint64),
+                ("bounds_hits", C.c_uint64), ("paths", C.c_uint64), ("render_ms", C.c_double),
+                ("extend_ms", C.c_double), ("occlude_ms", C.c_double), ("shade_ms", C.c_double),
+                ("kernel_launches", C.c_uint64), ("bvh_nodes", C.c_uint64), ("primitives", C.c_uint64)]
+
+
+# Every entry point declared in include/muon_gpu.h: name -> (restype, argtypes)
+SIGNATURES = {
+    "muon_parse_scene_file": (C.c_int, [C.c_char_p, C.POINTER(C.c_void_p)]),
+    "muon_parse_scene_string": (C.c_int, [C.c_char_p, C.c_char_p, C.POINTER(C.c_void_p)]),
+    "muon_parsed_scene_desc": (C.c_int, [C.c_void_p, C.POINTER(SceneDesc), C.POINTER(RenderParams)]),
+    "muon_parsed_scene_gamma": (C.c_float, [C.c_void_p]),
+    "muon_parsed_scene_output": (C.c_char_p, [C.c_void_p]),
+    "muon_parsed_scene_warnings": (C.c_int32, [C.c_void_p]),
+    "muon_parsed_scene_free": (None, [C.c_void_p]),
+    "muon_film_tonemap": (C.c_int, [C.POINTER(Film), C.c_float, C.POINTER(C.c_uint8)]),
+    "muon_film_write": (C.c_int, [C.POINTER(Film), C.c_float, C.c_char_p]),
+    "muon_gpu_scene_create": (C.c_int, [C.POINTER(SceneDesc), C.POINTER(C.c_void_p)]),
+    "muon_gpu_scene_destroy": (None, [C.c_void_p]),
+    "muon_gpu_render": (C.c_int, [C.c_void_p, C.POINTER(RenderParams), C.POINTER(Film)]),
+    "muon_gpu_render_device": (C.c_int, [C.c_void_p, C.POINTER(RenderParams), C.c_void_p, C.c_void_p,
+                                         C.c_void_p]),
+    "muon_gpu_intersect": (C.c_int, [C.c_void_p, C.POINTER(Ray), C.c_int64, C.c_int32, C.POINTER(Hit)]),
+    "muon_gpu_occluded": (C.c_int, [C.c_void_p, C.POINTER(Ray), C.POINTER(C.c_float), C.c_int64, C.c_int32,
+                                    C.POINTER(C.c_uint8)]),
+    "muon_gpu_stats": (C.c_int, [C.c_void_p, C.POINTER(Stats)]),
+    "muon_gpu_last_error": (C.c_char_p, []),
+}
+
+_lib = None
+
+
+def load() -> C.CDLL:
+    """Loads libmuon_gpu.so (raises if it has not been built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(f"{LIB_PATH} is missing: build it with muon_gb300.build.build()")
+        lib = C.CDLL(LIB_PATH)
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(lib, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = lib
+    return _lib
+
+
+class MuonError(RuntimeError):
+    def __init__(self, code: int, message: str):
+        super().__init__(f"{ERRORS.get(code, code)}: {message}")
+        self.code = code
+
+
+def check(code: int) -> None:
+    if code != MUON_OK:
+        msg = load().muon_gpu_last_error()
+        raise MuonError(code, msg.decode() if msg else "")

@@ -1,0 +1,228 @@
+"""Seeded synthetic scenes for the benchmark workloads, emitted as .muon text.
+
+The same text is rendered by the GPU path and by the CPU oracle, so both see
+identical input. Numbers are written with 9 significant digits, which
+round-trips float32 exactly through the reference parser's `istream >> float`.
+
+Small geometry is authored at a large object-space scale and shrunk with a
+`scale` transform: the reference rejects any triangle whose object-space
+unnormalised normal is shorter than 1e-4 (muon/objects.cc:104-108), which
+would make small triangles authored directly invisible.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+
+def _f(x: float) -> str:
+    return format(float(np.float32(x)), ".9g")
+
+
+def _v(*xs) -> str:
+    return " ".join(_f(x) for x in xs)
+
+
+# Unit cube vertices and outward-facing triangles (counter-clockwise seen from
+# outside).
+_CUBE_V = [(-1, -1, -1), (1, -1, -1), (1, 1, -1), (-1, 1, -1), (-1, -1, 1), (1, -1, 1), (1, 1, 1), (-1, 1, 1)]
+_CUBE_T = [(0, 2, 1), (0, 3, 2), (4, 5, 6), (4, 6, 7), (0, 1, 5), (0, 5, 4), (3, 7, 6), (3, 6, 2),
+           (0, 4, 7), (0, 7, 3), (1, 2, 6), (1, 6, 5)]
+
+
+def _cube(lines: list[str]) -> None:
+    lines.append("start_mesh")
+    for v in _CUBE_V:
+        lines.append("vertex " + _v(*v))
+    for t in _CUBE_T:
+        lines.append("tri %d %d %d" % t)
+    lines.append("end_mesh")
+
+
+def _quad(lines: list[str], a, b, c, d) -> None:
+    """Two triangles a-b-c, a-c-d (normal (b-a)x(c-a))."""
+    lines.append("start_mesh")
+    for v in (a, b, c, d):
+        lines.append("vertex " + _v(*v))
+    lines.append("tri 0 1 2")
+    lines.append("tri 0 2 3")
+    lines.append("end_mesh")
+
+
+def cornell(width: int = 256, height: int = 256, spp: int = 16, max_depth: int = 5, seed: int = 1,
+            integrator: str = "pathtracer", nee: str = "mis") -> str:
+    """Cornell box: five walls of the box [-1,1]x[0,2]x[-1,1] (2 triangles each,
+    facing inwards; left (0.63,0.065,0.05), right (0.14,0.45,0.09), others 0.73),
+    two rotated boxes (12 triangles each, Lambertian 0.73), a 0.25x0.25 ceiling
+    quad light with emission (17,12,4); pinhole camera with 40 degree FOV."""
+    L = ["# Cornell box: 5 walls, 2 rotated boxes, one 0.25x0.25 ceiling light",
+         f"random_seed {seed}",
+         f"film_size {width} {height}",
+         f"integrator {integrator}",
+         f"pixel_samples {spp}",
+         f"max_depth {max_depth}",
+         f"next_event_estimation {nee}",
+         "importance_sampling brdf",
+         "russian_roulette off",
+         "camera 0 1 3.9  0 1 0  0 1 0  40",
+         "quad_light -0.125 1.999 -0.125  0 0 0.25  0.25 0 0  17 12 4",
+         "brdf lambertian",
+         "ambient 0 0 0",
+         "specular 0 0 0",
+         "emission 0 0 0"]
+    grey = (0.73, 0.73, 0.73)
+    walls = [
+        ("floor", grey, (-1, 0, -1), (-1, 0, 1), (1, 0, 1), (1, 0, -1)),
+        ("ceiling", grey, (-1, 2, -1), (1, 2, -1), (1, 2, 1), (-1, 2, 1)),
+        ("back", grey, (-1, 0, -1), (1, 0, -1), (1, 2, -1), (-1, 2, -1)),
+        ("left", (0.63, 0.065, 0.05), (-1, 0, -1), (-1, 2, -1), (-1, 2, 1), (-1, 0, 1)),
+        ("right", (0.14, 0.45, 0.09), (1, 0, -1), (1, 0, 1), (1, 2, 1), (1, 2, -1)),
+    ]
+    for name, kd, a, b, c, d in walls:
+        L.append(f"# {name}")
+        L.append("diffuse " + _v(*kd))
+        _quad(L, a, b, c, d)
+    L.append("diffuse " + _v(*grey))
+    for (tx, ty, tz, ang, sx, sy, sz) in ((0.33, 0.3, 0.35, -18.0, 0.3, 0.3, 0.3),
+                                          (-0.35, 0.6, -0.3, 22.0, 0.3, 0.6, 0.3)):
+        L += ["push_transform", f"translate {_v(tx, ty, tz)}", f"rotate 0 1 0 {_f(ang)}", f"scale {_v(sx, sy, sz)}"]
+        _cube(L)
+        L.append("pop_transform")
+    return "\n".join(L) + "\n"
+
+
+def sphere_field(width: int = 512, height: int = 512, spp: int = 64, max_depth: int = 8, n_spheres: int = 512,
+                 seed: int = 1, nee: str = "mis") -> str:
+    """Random sphere field: centres U[-10,10]^3, radii U[0.2,1.0]; material
+    uniform over {Lambertian albedo U[0.1,0.9]^3; Phong kd U[0,0.5]^3,
+    ks U[0,0.5]^3, shininess 10^U[0,3]; GGX roughness U[0.05,0.6], F0
+    U[0.02,0.9], diffuse 0}; a ground quad below the field and one 2x2 quad
+    light of emission 10 above it. numpy PCG64 stream seeded with `seed`."""
+    rng = np.random.default_rng(seed)
+    L = ["# random sphere field",
+         f"random_seed {seed}",
+         f"film_size {width} {height}",
+         "integrator pathtracer",
+         f"pixel_samples {spp}",
+         f"max_depth {max_depth}",
+         f"next_event_estimation {nee}",
+         "importance_sampling brdf",
+         "russian_roulette off",
+         "gamma 2.2",
+         "camera 0 6 34  0 0 0  0 1 0  45",
+         "quad_light -1 12 -1  0 0 2  2 0 0  10 10 10",
+         "ambient 0 0 0",
+         "emission 0 0 0",
+         "brdf lambertian",
+         "diffuse 0.5 0.5 0.5",
+         "specular 0 0 0"]
+    _quad(L, (-30, -11, -30), (-30, -11, 30), (30, -11, 30), (30, -11, -30))
+    centres = rng.uniform(-10.0, 10.0, size=(n_spheres, 3))
+    radii = rng.uniform(0.2, 1.0, size=n_spheres)
+    kinds = rng.integers(0, 3, size=n_spheres)
+    for i in range(n_spheres):
+        k = kinds[i]
+        if k == 0:
+            L += ["brdf lambertian", "diffuse " + _v(*rng.uniform(0.1, 0.9, 3)), "specular 0 0 0"]
+        elif k == 1:
+            L += ["brdf phong", "diffuse " + _v(*rng.uniform(0.0, 0.5, 3)), "specular " + _v(*rng.uniform(0.0, 0.5, 3)),
+                  "shininess " + _f(10.0 ** rng.uniform(0.0, 3.0))]
+        else:
+            f0 = rng.uniform(0.02, 0.9)
+            L += ["brdf ggx", "diffuse 0 0 0", "specular " + _v(f0, f0, f0), "roughness " + _f(rng.uniform(0.05, 0.6))]
+        L.append("sphere " + _v(*centres[i], radii[i]))
+    return "\n".join(L) + "\n"
+
+
+def icosphere(level: int) -> tuple[np.ndarray, np.ndarray]:
+    """Unit icosphere: 12 + 30 (4^level - 1) / 3 * ... vertices, 20 * 4^level
+    triangles (counter-clockwise seen from outside). Returns (V float64, F int32)."""
+    t = (1.0 + 5.0 ** 0.5) / 2.0
+    v = [(-1, t, 0), (1, t, 0), (-1, -t, 0), (1, -t, 0), (0, -1, t), (0, 1, t), (0, -1, -t), (0, 1, -t),
+         (t, 0, -1), (t, 0, 1), (-t, 0, -1), (-t, 0, 1)]
+    f = [(0, 11, 5), (0, 5, 1), (0, 1, 7), (0, 7, 10), (0, 10, 11), (1, 5, 9), (5, 11, 4), (11, 10, 2),
+         (10, 7, 6), (7, 1, 8), (3, 9, 4), (3, 4, 2), (3, 2, 6), (3, 6, 8), (3, 8, 9), (4, 9, 5), (2, 4, 11),
+         (6, 2, 10), (8, 6, 7), (9, 8, 1)]
+    V = np.array(v, dtype=np.float64)
+    V /= np.linalg.norm(V, axis=1, keepdims=True)
+    F = np.array(f, dtype=np.int64)
+    for _ in range(level):
+        # midpoint of every edge, shared between its two triangles
+        e = np.concatenate([F[:, [0, 1]], F[:, [1, 2]], F[:, [2, 0]]])
+        e.sort(axis=1)
+        key = e[:, 0] * (len(V) + 1) + e[:, 1]
+        uniq, inv = np.unique(key, return_inverse=True)
+        a, b = uniq // (len(V) + 1), uniq % (len(V) + 1)
+        mid = V[a] + V[b]
+        mid /= np.linalg.norm(mid, axis=1, keepdims=True)
+        m = inv.reshape(3, -1).T + len(V)
+        V = np.concatenate([V, mid])
+        F = np.concatenate([np.stack([F[:, 0], m[:, 0], m[:, 2]], 1), np.stack([F[:, 1], m[:, 1], m[:, 0]], 1),
+                            np.stack([F[:, 2], m[:, 2], m[:, 1]], 1), m])
+    return V, F.astype(np.int32)
+
+
+def value_noise(p: np.ndarray, seed: int, freq: float = 3.0) -> np.ndarray:
+    """Seeded 3-D value noise in [-1, 1]: trilinear blend of random lattice values."""
+    rng = np.random.default_rng(seed)
+    lattice = rng.uniform(-1.0, 1.0, size=(64, 64, 64))
+    q = (p + 2.0) * freq
+    i0 = np.floor(q).astype(np.int64)
+    f = q - i0
+    f = f * f * (3.0 - 2.0 * f)
+    out = np.zeros(len(p))
+    for dx in (0, 1):
+        for dy in (0, 1):
+            for dz in (0, 1):
+                w = (f[:, 0] if dx else 1 - f[:, 0]) * (f[:, 1] if dy else 1 - f[:, 1]) * (f[:, 2] if dz else 1 - f[:, 2])
+                out += w * lattice[(i0[:, 0] + dx) % 64, (i0[:, 1] + dy) % 64, (i0[:, 2] + dz) % 64]
+    return out
+
+
+def _mesh(lines: list[str], V: np.ndarray, F: np.ndarray) -> None:
+    lines.append("start_mesh")
+    lines.extend("vertex " + _v(*v) for v in V)
+    lines.extend("tri %d %d %d" % tuple(t) for t in F)
+    lines.append("end_mesh")
+
+
+def feature_mix(width: int = 128, height: int = 128, spp: int = 1, integrator: str = "normals",
+                nee: str = "mis", max_depth: int = 5) -> str:
+    """Cornell room exercising every primitive path: rotated/scaled triangles, a
+    mirrored (negative-scale) box, a non-uniformly scaled sphere, a plain
+    sphere, a smooth-shaded icosphere (compute_vertex_normals), Phong and GGX
+    materials, two quad lights and a point light."""
+    L = ["# feature coverage scene", "random_seed 7", f"film_size {width} {height}", f"integrator {integrator}",
+         f"pixel_samples {spp}", f"max_depth {max_depth}", f"next_event_estimation {nee}",
+         "importance_sampling brdf", "russian_roulette off", "camera 0 1 3.9  0 1 0  0 1 0  40",
+         "quad_light -0.125 1.999 -0.125  0 0 0.25  0.25 0 0  17 12 4",
+         "quad_light -0.99 1.2 -0.3  0 0.3 0  0 0 0.6  4 4 6",
+         "point_light 0.5 1.5 0.5  1 1 1", "ambient 0 0 0", "emission 0 0 0", "brdf lambertian", "specular 0 0 0"]
+    walls = [((0.73, 0.73, 0.73), (-1, 0, -1), (-1, 0, 1), (1, 0, 1), (1, 0, -1)),
+             ((0.73, 0.73, 0.73), (-1, 2, -1), (1, 2, -1), (1, 2, 1), (-1, 2, 1)),
+             ((0.73, 0.73, 0.73), (-1, 0, -1), (1, 0, -1), (1, 2, -1), (-1, 2, -1)),
+             ((0.63, 0.065, 0.05), (-1, 0, -1), (-1, 2, -1), (-1, 2, 1), (-1, 0, 1)),
+             ((0.14, 0.45, 0.09), (1, 0, -1), (1, 0, 1), (1, 2, 1), (1, 2, -1))]
+    for kd, a, b, c, d in walls:
+        L.append("diffuse " + _v(*kd))
+        _quad(L, a, b, c, d)
+    L += ["brdf phong", "diffuse 0.5 0.45 0.4", "specular 0.3 0.3 0.3", "shininess 40",
+          "push_transform", "translate -0.5 0.25 -0.4", "rotate 0.2 1 0.1 30", "scale 0.25 0.25 0.25"]
+    _cube(L)
+    L += ["pop_transform", "push_transform", "translate 0.55 0.2 -0.5", "rotate 0 1 0 -15", "scale -0.2 0.2 0.2"]
+    _cube(L)
+    L += ["pop_transform", "brdf ggx", "diffuse 0.1 0.1 0.1", "specular 0.8 0.6 0.3", "roughness 0.2",
+          "push_transform", "translate 0.45 0.75 0.1", "rotate 1 0 1 40", "scale 0.3 0.15 0.2",
+          "sphere 0 0 0 1", "pop_transform", "roughness 0.05", "specular 0.9 0.9 0.9",
+          "sphere -0.45 0.9 0.25 0.22", "brdf lambertian", "diffuse 0.2 0.5 0.8", "specular 0 0 0",
+          "compute_vertex_normals on", "push_transform", "translate -0.1 0.3 0.45", "scale 0.002 0.002 0.002"]
+    V, F = icosphere(2)
+    _mesh(L, V * 100.0, F)
+    L += ["pop_transform"]
+    return "\n".join(L) + "\n"
+
+
+WORKLOADS = {
+    "cornell": cornell,
+    "sphere_field": sphere_field,
+    "feature_mix": feature_mix,
+}

@@ -1,67 +1,153 @@
 // Test-oracle driver over the reference renderer's own objects (built by
-// oracle/Makefile into oracle/_ref/; test infrastructure only).
+// oracle/Makefile into oracle/_ref/; test infrastructure only, never shipped).
 //
-// For a .muon scene it parses with the reference Parser (muon/parser.cc:230),
-// casts the sample-0 ray through every pixel centre with Camera::CastRay
-// (muon/camera.cc:37, pixel centre per muon/sampling.cc:89-91) and intersects
-// it with the reference acceleration structure (muon/acceleration.cc:65).
-// Output (binary, little endian):
-//   header: "MUONHIT1", int32 width, int32 height
-//   per pixel (row-major, y outer): int32 hit, float distance, float pos[3],
-//   float normal[3], float diffuse[3], float specular[3], int32 is_light
-// The integrator's Shade() is not called; the fields above are exactly the
-// inputs of NormalsTracer/AlbedoTracer/DepthTracer (muon/integration.cc:47-72).
+//   ref_driver hits  scene.muon out.bin [linear|bvh]
+//     Parses with the reference Parser (muon/parser.cc:230), casts the sample-0
+//     ray through every pixel centre with Camera::CastRay (muon/camera.cc:37;
+//     pixel centre per muon/sampling.cc:89-91) and intersects it with the
+//     reference acceleration structure (muon/acceleration.cc:65 / :168).
+//     Per pixel (row-major, y outer), little endian:
+//       float ray[6]; int32 hit; int32 prim_id; float distance; float pos[3];
+//       float normal[3]; float albedo[3]
+//     prim_id is the index in scene-file order, known only for the linear
+//     structure (which keeps AddPrimitive order); -2 with the BVH. The fields
+//     are the inputs of NormalsTracer/AlbedoTracer/DepthTracer
+//     (muon/integration.cc:47-72).
+//
+//   ref_driver render scene.muon out.bin [spp] [seed]
+//     Renderer::Render's sample loop (muon/renderer.cc:34-66) on one thread:
+//     TileImage + TileQueue order, Sampler::NextSample, CastRay, the scene's
+//     integrator Trace. Accumulates an FP64 film instead of the FP32 one.
+//     spp overrides pixel_samples; seed (if given) replaces the scene's seed
+//     generator before tiles and the path tracer are seeded.
+//     Output: int32 w, h, spp, then w*h*3 doubles of sums and of sums of
+//     squares, then uint64 primary, secondary, object tests, bounds tests.
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <fstream>
+#include <map>
 #include <string>
+#include <vector>
 
 #include "muon/acceleration.h"
+#include "muon/integration.h"
 #include "muon/options.h"
 #include "muon/parser.h"
+#include "muon/sampling.h"
 
-int main(int argc, char **argv) {
-  if (argc < 3) {
-    std::fprintf(stderr, "usage: ref_driver scene.muon out.bin [linear]\n");
-    return 2;
+namespace {
+
+// Reads Structure::primitives_ (protected) through a derived-class member
+// pointer, to map primitives back to their AddPrimitive order.
+struct PrimitiveAccess : muon::acceleration::Structure {
+  static std::vector<std::unique_ptr<muon::Primitive>> &Of(muon::acceleration::Structure &s) {
+    return s.*(&PrimitiveAccess::primitives_);
   }
-  muon::Options options;
-  options.output = "";
-  options.acceleration = (argc > 3 && std::string(argv[3]) == "linear")
-                             ? muon::AccelerationType::kLinear
-                             : muon::AccelerationType::kBVH;
-  options.partition_strategy = muon::PartitionStrategy::kSAH;
-  options.parallelism = 1;
-  options.show_stats = false;
-  muon::Parser parser(argv[1], options);
+};
+
+muon::Options MakeOptions(bool linear) {
+  muon::Options o;
+  o.output = "";
+  o.acceleration = linear ? muon::AccelerationType::kLinear : muon::AccelerationType::kBVH;
+  o.partition_strategy = muon::PartitionStrategy::kSAH;
+  o.parallelism = 1;
+  o.show_stats = false;
+  return o;
+}
+
+int Hits(const char *scene, const char *out_path, bool linear) {
+  muon::Options options = MakeOptions(linear);
+  muon::Parser parser(scene, options);
   muon::SceneConfig sc = parser.Parse();
+  std::map<const muon::Primitive *, int32_t> ids;
+  if (linear) {
+    auto &prims = PrimitiveAccess::Of(*sc.scene->root);
+    for (size_t i = 0; i < prims.size(); ++i) ids[prims[i].get()] = static_cast<int32_t>(i);
+  }
   auto ws = sc.scene->root->CreateWorkspace();
   int w = sc.scene->width, h = sc.scene->height;
-  std::ofstream out(argv[2], std::ios::binary);
-  out.write("MUONHIT1", 8);
-  out.write(reinterpret_cast<const char *>(&w), 4);
-  out.write(reinterpret_cast<const char *>(&h), 4);
+  std::ofstream out(out_path, std::ios::binary);
   for (int y = 0; y < h; ++y) {
     for (int x = 0; x < w; ++x) {
       muon::Ray r = sc.scene->camera->CastRay(x + 0.5f, y + 0.5f);
       auto hit = sc.scene->root->Intersect(ws.get(), r);
-      int32_t is_hit = hit ? 1 : 0;
-      float rec[13] = {0};
-      int32_t is_light = 0;
+      float ray[6];
+      for (int k = 0; k < 3; ++k) ray[k] = r.origin()[k], ray[3 + k] = r.direction()[k];
+      int32_t head[2] = {hit ? 1 : 0, -1};
+      float rec[10] = {0};
       if (hit) {
+        head[1] = linear ? ids[hit->obj] : -2;
         rec[0] = hit->distance;
         for (int k = 0; k < 3; ++k) {
           rec[1 + k] = hit->pos[k];
           rec[4 + k] = hit->normal[k];
-          rec[7 + k] = hit->obj->material->diffuse[k];
-          rec[10 + k] = hit->obj->material->specular[k];
+          rec[7 + k] = hit->obj->material->diffuse[k] + hit->obj->material->specular[k];
         }
-        is_light = hit->obj->light != nullptr;
       }
-      out.write(reinterpret_cast<const char *>(&is_hit), 4);
+      out.write(reinterpret_cast<const char *>(ray), sizeof(ray));
+      out.write(reinterpret_cast<const char *>(head), sizeof(head));
       out.write(reinterpret_cast<const char *>(rec), sizeof(rec));
-      out.write(reinterpret_cast<const char *>(&is_light), 4);
     }
   }
   return 0;
+}
+
+int Render(const char *scene, const char *out_path, int spp_override, long long seed) {
+  muon::Options options = MakeOptions(false);
+  muon::Parser parser(scene, options);
+  muon::SceneConfig sc = parser.Parse();
+  if (seed >= 0) {
+    // Re-seed as if the file had said `random_seed <seed>` before the
+    // integrator line: a fresh path-tracer RNG and tile seeds.
+    sc.scene->seedgen = std::make_unique<muon::SeedGenerator>(static_cast<unsigned int>(seed));
+    if (dynamic_cast<muon::PathTracer *>(sc.integrator_prototype.get())) {
+      sc.integrator_prototype = std::make_unique<muon::PathTracer>(*sc.scene, sc.scene->seedgen->Next());
+    }
+  }
+  if (spp_override > 0) sc.scene->pixel_samples = spp_override;
+  const int w = sc.scene->width, h = sc.scene->height, spp = sc.scene->pixel_samples;
+  std::vector<double> sum(3 * static_cast<size_t>(w) * h, 0.0), sq(sum.size(), 0.0);
+  int num_tiles = muon::NumTiles(w, h, spp, 1);
+  muon::TileQueue tiles(muon::TileImage(w, h, num_tiles, *sc.scene->seedgen));
+  std::unique_ptr<muon::Integrator> integrator = sc.integrator_prototype->Clone();
+  integrator->Init();
+  absl::optional<muon::Tile> tile;
+  while ((tile = tiles.TryDequeue())) {
+    muon::Sampler sampler(tile.value(), spp);
+    float x, y;
+    while (sampler.NextSample(x, y)) {
+      muon::Ray r = sc.scene->camera->CastRay(x, y);
+      glm::vec3 c = integrator->Trace(r);
+      size_t p = static_cast<size_t>(static_cast<int>(y)) * w + static_cast<int>(x);
+      for (int k = 0; k < 3; ++k) {
+        sum[3 * p + k] += c[k];
+        sq[3 * p + k] += static_cast<double>(c[k]) * c[k];
+      }
+    }
+  }
+  muon::TraceStats ts = integrator->trace_stats();
+  std::ofstream out(out_path, std::ios::binary);
+  int32_t head[3] = {w, h, spp};
+  out.write(reinterpret_cast<const char *>(head), sizeof(head));
+  out.write(reinterpret_cast<const char *>(sum.data()), sum.size() * sizeof(double));
+  out.write(reinterpret_cast<const char *>(sq.data()), sq.size() * sizeof(double));
+  uint64_t counters[4] = {ts.primary_rays(), ts.secondary_rays(), ts.object_tests(), ts.bounds_tests()};
+  out.write(reinterpret_cast<const char *>(counters), sizeof(counters));
+  return 0;
+}
+
+}  // namespace
+
+int main(int argc, char **argv) {
+  if (argc >= 4 && std::string(argv[1]) == "hits") {
+    return Hits(argv[2], argv[3], argc > 4 && std::string(argv[4]) == "linear");
+  }
+  if (argc >= 4 && std::string(argv[1]) == "render") {
+    int spp = argc > 4 ? std::atoi(argv[4]) : 0;
+    long long seed = argc > 5 ? std::atoll(argv[5]) : -1;
+    return Render(argv[2], argv[3], spp, seed);
+  }
+  std::fprintf(stderr, "usage: ref_driver hits|render scene.muon out.bin ...\n");
+  return 2;
 }

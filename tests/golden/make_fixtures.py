@@ -1,0 +1,116 @@
+"""Generates the committed golden fixtures from the reference renderer.
+
+Runs the reference's own code (oracle/_ref/ref_driver, built from the
+reference sources by oracle/Makefile) on the seeded synthetic scenes of
+muon_gb300.scenes and stores small .npz files next to this script:
+
+  hits_<name>.npz  sample-0 camera rays and the reference's closest hits
+                   (linear structure: parse-order primitive ids; BVH: values)
+  pt_<name>.npz    FP64 films of independent single-thread path-traced
+                   renders (distinct seeds) for statistical parity tests
+
+Usage: python tests/golden/make_fixtures.py [--only NAME ...]
+Requires the reference sources (to build oracle/_ref); the GPU machine only reads
+the .npz files.
+"""
+from __future__ import annotations
+
+import argparse
+import os
+import subprocess
+import sys
+import tempfile
+from concurrent.futures import ThreadPoolExecutor
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from muon_gb300 import scenes  # noqa: E402
+
+DRIVER = os.path.join(ROOT, "oracle", "_ref", "ref_driver")
+HIT_DTYPE = np.dtype([("ray", "<f4", 6), ("hit", "<i4"), ("id", "<i4"), ("dist", "<f4"), ("pos", "<f4", 3),
+                      ("normal", "<f4", 3), ("albedo", "<f4", 3)])
+
+HIT_SCENES = {
+    "cornell": lambda: scenes.cornell(128, 128, 1, 5, 1, "normals"),
+    "sphere_field": lambda: scenes.sphere_field(128, 128, 1, 8).replace("integrator pathtracer", "integrator normals"),
+    "feature_mix": lambda: scenes.feature_mix(128, 128, 1, "normals"),
+}
+
+# (scene text, runs, spp per run)
+PT_SCENES = {
+    "cornell": (lambda: scenes.cornell(48, 48, 64, 5, 1, "pathtracer"), 16, 64),
+    "feature_mix": (lambda: scenes.feature_mix(48, 48, 64, "pathtracer", "mis", 5), 16, 64),
+    "sphere_field": (lambda: scenes.sphere_field(48, 48, 64, 8), 16, 64),
+    "cornell_nee_on": (lambda: scenes.cornell(48, 48, 64, 5, 1, "pathtracer", "on"), 16, 64),
+    "cornell_nee_off": (lambda: scenes.cornell(48, 48, 64, 5, 1, "pathtracer", "off"), 16, 64),
+}
+
+
+def build_driver() -> None:
+    subprocess.run(["make", "-C", os.path.join(ROOT, "oracle"), "-j8", "-s"], check=True)
+
+
+def hits(name: str) -> None:
+    text = HIT_SCENES[name]()
+    with tempfile.TemporaryDirectory() as td:
+        sp = os.path.join(td, "s.muon")
+        open(sp, "w").write(text)
+        recs = {}
+        for mode in ("linear", "bvh"):
+            out = os.path.join(td, mode + ".bin")
+            subprocess.run([DRIVER, "hits", sp, out, mode], check=True)
+            recs[mode] = np.fromfile(out, HIT_DTYPE)
+    lin, bvh = recs["linear"], recs["bvh"]
+    np.savez_compressed(os.path.join(HERE, f"hits_{name}.npz"), scene=np.array(text), rays=lin["ray"],
+                        hit=lin["hit"].astype(np.int8), prim_id=lin["id"].astype(np.int32), distance=lin["dist"],
+                        normal=lin["normal"], albedo=lin["albedo"], bvh_distance=bvh["dist"],
+                        bvh_normal=bvh["normal"])
+    print(f"hits_{name}: {len(lin)} rays, {int(lin['hit'].sum())} hits")
+
+
+def _render(args) -> np.ndarray:
+    text, spp, seed = args
+    with tempfile.TemporaryDirectory() as td:
+        sp = os.path.join(td, "s.muon")
+        open(sp, "w").write(text)
+        out = os.path.join(td, "f.bin")
+        subprocess.run([DRIVER, "render", sp, out, str(spp), str(seed)], check=True)
+        raw = open(out, "rb").read()
+    w, h, n = np.frombuffer(raw, np.int32, 3)
+    vals = np.frombuffer(raw, np.float64, 6 * w * h, offset=12)
+    counters = np.frombuffer(raw, np.uint64, 4, offset=12 + 8 * 6 * w * h)
+    return vals[:3 * w * h].reshape(h, w, 3), vals[3 * w * h:].reshape(h, w, 3), int(n), counters
+
+
+def pt(name: str) -> None:
+    make, runs, spp = PT_SCENES[name]
+    text = make()
+    with ThreadPoolExecutor(max_workers=os.cpu_count() or 4) as ex:
+        res = list(ex.map(_render, [(text, spp, 1000 + r) for r in range(runs)]))
+    sums = np.stack([r[0] for r in res])
+    sqs = np.stack([r[1] for r in res])
+    counters = np.stack([r[3] for r in res]).astype(np.int64)
+    np.savez_compressed(os.path.join(HERE, f"pt_{name}.npz"), scene=np.array(text), sums=sums.astype(np.float64),
+                        sum_sq=sqs.astype(np.float64), spp=np.int32(spp), counters=counters)
+    print(f"pt_{name}: {runs} runs x {spp} spp, mean {sums.sum(0).mean() / (runs * spp):.4f}")
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--only", nargs="*")
+    a = ap.parse_args()
+    build_driver()
+    for name in HIT_SCENES:
+        if not a.only or name in a.only:
+            hits(name)
+    for name in PT_SCENES:
+        if not a.only or ("pt_" + name) in a.only:
+            pt(name)
+
+
+if __name__ == "__main__":
+    main()

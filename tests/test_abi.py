@@ -1,0 +1,50 @@
+"""The C ABI library builds, loads and exports every declared entry point."""
+import re
+
+from conftest import ROOT
+
+
+def _declared_functions():
+    text = open(f"{ROOT}/include/muon_gpu.h").read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(muon_[a-z0-9_]+)\s*\(", text)))
+
+
+def test_header_declares_the_boundary():
+    names = _declared_functions()
+    for required in ["muon_gpu_scene_create", "muon_gpu_render", "muon_gpu_intersect", "muon_gpu_occluded",
+                     "muon_gpu_stats", "muon_gpu_scene_destroy", "muon_gpu_last_error", "muon_parse_scene_file"]:
+        assert required in names
+
+
+def test_library_exports_every_declared_symbol(lib):
+    from muon_gb300 import native
+
+    for name in _declared_functions():
+        assert hasattr(lib, name), name
+        assert name in native.SIGNATURES, f"{name} missing from the ctypes signatures"
+
+
+def test_errors_are_status_codes(lib):
+    import ctypes as C
+
+    from muon_gb300 import native
+
+    h = C.c_void_p()
+    rc = lib.muon_parse_scene_file(b"/nonexistent/scene.muon", C.byref(h))
+    assert rc == 5
+    assert b"cannot open" in lib.muon_gpu_last_error()
+    assert lib.muon_gpu_scene_create(None, C.byref(h)) == 1
+    assert lib.muon_gpu_render(None, None, None) == 1
+    assert lib.muon_gpu_stats(None, None) == 1
+    assert native.MUON_OK == 0
+
+
+def test_scene_without_camera_is_a_parse_error(lib):
+    import pytest
+
+    import muon_gb300 as m
+
+    with pytest.raises(m.MuonError) as e:
+        m.parse_string("film_size 4 4\nsphere 0 0 0 1\n")
+    assert e.value.code == 5

@@ -1,0 +1,103 @@
+"""Host parser semantics (muon/parser.cc:230-880) on small scene texts."""
+import numpy as np
+import pytest
+
+import muon_gb300 as m
+from muon_gb300 import native, scenes
+
+CAM = "camera 0 0 5  0 0 0  0 1 0  45\n"
+
+
+def parse(text):
+    return m.parse_string(text)
+
+
+def test_defaults(lib):
+    p = parse(CAM)
+    d, r = p.desc, p.params
+    assert (d.width, d.height) == (150, 150)
+    assert r.integrator == native.INTEGRATORS["raytracer"]
+    assert (r.pixel_samples, r.light_samples, r.max_depth, r.min_depth) == (1, 1, 5, 0)
+    assert r.next_event_estimation == 0 and r.importance_sampling == 0 and r.russian_roulette == 0
+    assert p.gamma == 1.0 and p.output is None
+
+
+def test_random_seed_falls_through_into_film_size(lib):
+    # muon/parser.cc:267-286: the seed case has no break
+    p = parse("random_seed 5 64 32\n" + CAM)
+    assert (p.desc.width, p.desc.height) == (64, 32)
+    p = parse("random_seed 5\n" + CAM)
+    assert (p.desc.width, p.desc.height) == (150, 150)
+    assert p.warnings == 1
+    a = parse("random_seed 5\nintegrator pathtracer\n" + CAM).params.seed
+    b = parse("random_seed 5\nintegrator pathtracer\n" + CAM).params.seed
+    c = parse("random_seed 6\nintegrator pathtracer\n" + CAM).params.seed
+    assert a == b != c
+    # std::mt19937(5)'s first output
+    assert a == 953453411
+
+
+def test_camera_keeps_film_size_of_its_line(lib):
+    p = parse("film_size 20 10\n" + CAM + "film_size 40 30\n")
+    assert (p.desc.camera.width, p.desc.camera.height) == (20, 10)
+    assert (p.desc.width, p.desc.height) == (40, 30)
+
+
+def test_lambertian_builds_phong(lib):
+    p = parse(CAM + "brdf lambertian\nsphere 0 0 0 1\nbrdf ggx\nsphere 0 0 0 1\n")
+    mats = [p.desc.materials[p.desc.spheres[i].material] for i in range(2)]
+    assert mats[0].brdf == 1 and mats[1].brdf == 2
+
+
+def test_quad_light_adds_two_emissive_triangles(lib):
+    p = parse(CAM + "ambient 0.3 0.3 0.3\nquad_light 1 2 3  1 0 0  0 0 2  5 6 7\n")
+    d = p.desc
+    assert d.num_triangles == 2 and d.num_lights == 1
+    t0, t1 = d.triangles[0], d.triangles[1]
+    v = lambda t: np.array([[t.v[k][j] for j in range(3)] for k in range(3)])
+    va, vb, vc, vd = np.array([1, 2, 3.0]), np.array([2, 2, 3.0]), np.array([1, 2, 5.0]), np.array([2, 2, 5.0])
+    assert np.array_equal(v(t0), [va, vc, vb]) and np.array_equal(v(t1), [vb, vc, vd])
+    mat = d.materials[t0.material]
+    assert list(mat.emission) == [5, 6, 7] and list(mat.ambient) == [0, 0, 0] and mat.brdf == 1
+    assert t0.light == 0 and t0.transform == -1 and (t0.prim_id, t1.prim_id) == (0, 1)
+
+
+def test_transform_stack_and_inverse(lib):
+    p = parse(CAM + "push_transform\ntranslate 1 2 3\nrotate 0 1 0 90\nscale 2 2 2\nsphere 0 0 0 1\npop_transform\n"
+              "sphere 0 0 0 1\n")
+    d = p.desc
+    s0, s1 = d.spheres[0], d.spheres[1]
+    assert s1.transform == -1 and s0.transform >= 0
+    t = d.transforms[s0.transform]
+    M = np.array(t.object_to_world, dtype=np.float64).reshape(4, 4).T
+    Minv = np.array(t.world_to_object, dtype=np.float64).reshape(4, 4).T
+    T = np.eye(4); T[:3, 3] = [1, 2, 3]
+    R = np.array([[0, 0, 1, 0], [0, 1, 0, 0], [-1, 0, 0, 0], [0, 0, 0, 1.0]])
+    S = np.diag([2, 2, 2, 1.0])
+    assert np.allclose(M, T @ R @ S, atol=1e-6)
+    assert np.allclose(Minv @ M, np.eye(4), atol=1e-6)
+    NT = np.array(t.normal_to_world, dtype=np.float64).reshape(4, 4).T
+    assert np.allclose(NT, Minv.T, atol=0)
+
+
+def test_vertex_normals_accumulate_and_normalise(lib):
+    text = CAM + ("compute_vertex_normals on\nvertex 0 0 0\nvertex 1 0 0\nvertex 0 1 0\nvertex 0 0 1\n"
+                  "tri 0 1 2\ntri 0 3 1\n")
+    d = parse(text).desc
+    n0 = np.array([d.triangles[0].n[0][j] for j in range(3)])
+    assert np.allclose(n0, np.array([0, 1, 1]) / np.sqrt(2), atol=1e-7)
+    assert d.triangles[0].smooth == 1
+
+
+def test_bad_lines_are_skipped(lib):
+    p = parse(CAM + "bogus 1 2\nsphere 1 2\ntri 0 1 99\nfilm_size x y\n")
+    assert p.warnings == 4 and p.desc.num_spheres == 0 and p.desc.num_triangles == 0
+
+
+@pytest.mark.parametrize("name", ["cornell", "sphere_field", "feature_mix"])
+def test_synthetic_scenes_parse(lib, name):
+    p = parse(scenes.WORKLOADS[name]())
+    assert p.desc.num_triangles + p.desc.num_spheres > 0
+    ids = sorted([p.desc.triangles[i].prim_id for i in range(p.desc.num_triangles)] +
+                 [p.desc.spheres[i].prim_id for i in range(p.desc.num_spheres)])
+    assert ids == list(range(len(ids)))

@@ -71,12 +71,22 @@ extern "C" {
 #define MUON_PARTITION_UNIFORM 0
 #define MUON_PARTITION_MIDPOINT 1
 #define MUON_PARTITION_SAH 2
-/* Triangle test used by the traversal kernels. REFERENCE repeats the
- * reference's plane + edge-function test (muon/objects.cc:58-175) on
- * world-space vertices; WATERTIGHT is the watertight ray/triangle test of
- * Woop, Benthin and Wald (JCGT 2013). */
-#define MUON_TRI_REFERENCE 0
-#define MUON_TRI_WATERTIGHT 1
+/* Primitive intersection arithmetic of the traversal kernels.
+ *   FAST        the reference's triangle test (plane + three edge functions,
+ *               muon/objects.cc:58-175) and sphere test on world-space data,
+ *               with fused multiply-adds; hits equal the reference's except at
+ *               rounding edges.
+ *   WATERTIGHT  the watertight ray/triangle test of Woop, Benthin and Wald
+ *               (JCGT 2013); spheres as FAST.
+ *   EXACT       the reference's arithmetic bit for bit: each primitive is
+ *               tested in its object space with the ray carried by the inverse
+ *               transform and its direction re-normalised (muon/objects.cc:
+ *               29-46, muon/transform.h:13-18), no fused multiply-adds, the
+ *               distance measured back in world space. Slower for transformed
+ *               primitives. */
+#define MUON_ISECT_FAST 0
+#define MUON_ISECT_WATERTIGHT 1
+#define MUON_ISECT_EXACT 2
 
 /* render flags */
 #define MUON_RENDER_STATS 1u      /* count bounds/object tests (slower)        */
@@ -170,7 +180,7 @@ typedef struct MuonRenderParams {
   int32_t max_depth; /* -1 = unbounded */
   int32_t sample_offset; /* index of the first sample (progressive runs) */
   uint64_t seed;
-  int32_t triangle_test; /* MUON_TRI_* */
+  int32_t intersect_mode; /* MUON_ISECT_* */
   int32_t wave_paths;    /* paths in flight per wavefront; 0 = tuned     */
   uint32_t flags;        /* MUON_RENDER_*                               */
   int32_t pad;
@@ -264,10 +274,10 @@ int muon_gpu_render_device(MuonScene *scene, const MuonRenderParams *params, dou
 
 /* Batched ray queries mirroring Structure::Intersect and
  * Structure::HasIntersection (muon/acceleration.h:44-49) on host arrays. */
-int muon_gpu_intersect(MuonScene *scene, const MuonRay *rays, int64_t n, int32_t triangle_test,
+int muon_gpu_intersect(MuonScene *scene, const MuonRay *rays, int64_t n, int32_t intersect_mode,
                        MuonHit *hits);
 int muon_gpu_occluded(MuonScene *scene, const MuonRay *rays, const float *max_distance, int64_t n,
-                      int32_t triangle_test, uint8_t *occluded);
+                      int32_t intersect_mode, uint8_t *occluded);
 
 /* Counters and device timings of the last render (muon/stats.h:11-44). */
 int muon_gpu_stats(const MuonScene *scene, MuonStats *stats);

@@ -155,8 +155,8 @@ class Scene:
                 v = native.NEE[v]
             elif k == "importance_sampling" and isinstance(v, str):
                 v = native.IMPORTANCE[v]
-            elif k == "triangle_test" and isinstance(v, str):
-                v = native.TRI_WATERTIGHT if v == "watertight" else native.TRI_REFERENCE
+            elif k == "intersect_mode" and isinstance(v, str):
+                v = {"fast": native.ISECT_FAST, "watertight": native.ISECT_WATERTIGHT, "exact": native.ISECT_EXACT}[v]
             setattr(p, k, v)
         return p
 
@@ -174,7 +174,7 @@ class Scene:
         check(load().muon_gpu_render_device(self._h, C.byref(params), C.c_void_p(d_sum), C.c_void_p(d_sum_sq),
                                              C.c_void_p(d_count)))
 
-    def intersect(self, origins: np.ndarray, directions: np.ndarray, triangle_test: int = native.TRI_REFERENCE):
+    def intersect(self, origins: np.ndarray, directions: np.ndarray, intersect_mode: int = native.ISECT_EXACT):
         """Closest hits (Structure::Intersect) for a batch of rays.
 
         Returns (distance, prim_id, position, normal); prim_id is the primitive's
@@ -185,12 +185,12 @@ class Scene:
         rays[:, :3] = origins
         rays[:, 3:] = directions
         hits = np.zeros((n, 8), dtype=np.float32)
-        check(load().muon_gpu_intersect(self._h, rays.ctypes.data_as(C.POINTER(native.Ray)), n, triangle_test,
+        check(load().muon_gpu_intersect(self._h, rays.ctypes.data_as(C.POINTER(native.Ray)), n, intersect_mode,
                                         hits.ctypes.data_as(C.POINTER(native.Hit))))
         return hits[:, 0].copy(), hits[:, 1].view(np.int32).copy(), hits[:, 2:5].copy(), hits[:, 5:8].copy()
 
     def occluded(self, origins: np.ndarray, directions: np.ndarray, max_distance: np.ndarray,
-                 triangle_test: int = native.TRI_REFERENCE) -> np.ndarray:
+                 intersect_mode: int = native.ISECT_EXACT) -> np.ndarray:
         """Any hit closer than max_distance (Structure::HasIntersection)."""
         n = len(origins)
         rays = np.zeros((n, 6), dtype=np.float32)
@@ -199,7 +199,7 @@ class Scene:
         md = np.ascontiguousarray(max_distance, dtype=np.float32)
         out = np.zeros(n, dtype=np.uint8)
         check(load().muon_gpu_occluded(self._h, rays.ctypes.data_as(C.POINTER(native.Ray)),
-                                       md.ctypes.data_as(C.POINTER(C.c_float)), n, triangle_test,
+                                       md.ctypes.data_as(C.POINTER(C.c_float)), n, intersect_mode,
                                        out.ctypes.data_as(C.POINTER(C.c_uint8))))
         return out.astype(bool)
 

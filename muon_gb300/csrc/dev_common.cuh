@@ -10,6 +10,8 @@
 
 namespace muon_gpu {
 
+constexpr float kEps = 0.0001f;  // kEpsilon, muon/types.h:13
+
 __device__ __forceinline__ float3 f3(float x, float y, float z) { return make_float3(x, y, z); }
 __device__ __forceinline__ float3 f3(const F4 &v) { return make_float3(v.x, v.y, v.z); }
 __device__ __forceinline__ float3 f3(const float4 &v) { return make_float3(v.x, v.y, v.z); }

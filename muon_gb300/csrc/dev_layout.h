@@ -12,11 +12,15 @@
 // primitive record is ~link. Leaves end at the record flagged kPrimLast.
 // Node 0 is the root; an empty child slot has an inverted box.
 //
-// Primitive records (64 bytes, leaf order):
+// Primitive records (64 bytes, leaf order), world space:
 //   triangle: p0 = (a.xyz, dot(a,n)), p1 = (b.xyz, eps), p2 = (c.xyz, -),
 //             p3 = (n.xyz, flags)       n = (b-a) x (c-a), unnormalised
 //   sphere:   p0 = (centre.xyz, radius), p1 = (-, transform, -, -),
 //             p2 = -, p3 = (-, -, -, flags)
+// and the same in object space for the exact mode:
+//   triangle: p0 = (a.xyz, -), p1 = (b.xyz, transform), p2 = (c.xyz, |n|^2),
+//             p3 = (n.xyz, flags)
+//   sphere:   as above
 // Shading records (32 bytes, leaf order): s0 = (unit normal.xyz, material),
 // s1 = (light, prim_id, transform, flags).
 #pragma once
@@ -84,13 +88,16 @@ struct alignas(16) DevLight {
 // Pointers into one scene's device arrays (all leaf order where relevant).
 struct DevScene {
   const BvhNode *nodes;
-  const PrimRecord *prims;
+  const PrimRecord *prims;      // world-space records (fast / watertight)
+  const PrimRecord *prims_obj;  // object-space records (exact)
   const ShadeRecord *shade;
-  const F4 *smooth_normals;  // 3 per slot, or null
+  const F4 *smooth_normals;      // 3 per slot, carried to world space, or null
+  const F4 *smooth_normals_obj;  // 3 per slot, object space, or null
   const DevTransform *transforms;
   const DevMaterial *materials;
   const DevLight *lights;       // quad lights
   const PrimRecord *light_tris; // 2 per quad light, in light order (for MIS)
+  const PrimRecord *light_tris_obj;  // the same in the object-space format
   const int32_t *light_tri_ok;  // per light triangle: 1 if it can be hit
   const DevLight *other_lights; // point/directional
   int32_t num_nodes;

@@ -17,7 +17,6 @@ namespace muon_gpu {
 
 constexpr float kPi = 3.14159265358979323846f;
 constexpr float kInvPi = 0.318309886183790671538f;
-constexpr float kEps = 0.0001f;  // kEpsilon, muon/types.h:13
 
 // Camera ray through screen position (x, y), evaluated with the reference's
 // operation order and no contraction, so primary rays match it bit for bit.

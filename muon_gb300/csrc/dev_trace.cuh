@@ -17,6 +17,9 @@ struct RayPre {
   // watertight-test shear
   int kx, ky, kz;
   float sx, sy, sz;
+  // exact mode: the direction as the reference carries it into the object
+  // space of an untransformed primitive, normalize(I * (d, 0))
+  mm::v3 dn;
 };
 
 __device__ __forceinline__ float SafeInv(float x) {
@@ -31,7 +34,7 @@ __device__ __forceinline__ RayPre Prepare(float3 o, float3 d) {
   r.d = d;
   r.idir = f3(SafeInv(d.x), SafeInv(d.y), SafeInv(d.z));
   r.ood = o * r.idir;
-  if (kTriTest == MUON_TRI_WATERTIGHT) {
+  if (kTriTest == MUON_ISECT_WATERTIGHT) {
     float ax = fabsf(d.x), ay = fabsf(d.y), az = fabsf(d.z);
     r.kz = ax > ay ? (ax > az ? 0 : 2) : (ay > az ? 1 : 2);
     r.kx = r.kz == 2 ? 0 : r.kz + 1;
@@ -48,6 +51,7 @@ __device__ __forceinline__ RayPre Prepare(float3 o, float3 d) {
     r.sy = dy / dz;
     r.sz = 1.0f / dz;
   }
+  if (kTriTest == MUON_ISECT_EXACT) r.dn = mm::normalize(mm::make3(d.x, d.y, d.z));
   return r;
 }
 
@@ -129,10 +133,80 @@ __device__ __forceinline__ float SphereTest(const DevScene &s, const RayPre &r, 
   return t > 0.0f ? t : -1.0f;
 }
 
+// ---- exact mode: the reference's arithmetic, no contraction --------------
+// Rows 0..2 of M * (p, 1) and of M * (d, 0) for a packed affine matrix, in
+// the reference library's column order ((c0 x + c1 y) + (c2 z + c3 w)).
+__device__ __forceinline__ mm::v3 XPointExact(const float *m, mm::v3 p) {
+  using namespace mm;
+  return make3(add(add(mul(m[0], p.x), mul(m[3], p.y)), add(mul(m[6], p.z), m[9])),
+               add(add(mul(m[1], p.x), mul(m[4], p.y)), add(mul(m[7], p.z), m[10])),
+               add(add(mul(m[2], p.x), mul(m[5], p.y)), add(mul(m[8], p.z), m[11])));
+}
+__device__ __forceinline__ mm::v3 XDirExact(const float *m, mm::v3 d) {
+  using namespace mm;
+  return normalize(make3(add(add(mul(m[0], d.x), mul(m[3], d.y)), mul(m[6], d.z)),
+                         add(add(mul(m[1], d.x), mul(m[4], d.y)), mul(m[7], d.z)),
+                         add(add(mul(m[2], d.x), mul(m[5], d.y)), mul(m[8], d.z))));
+}
+__device__ __forceinline__ mm::v3 V(const F4 &v) { return mm::make3(v.x, v.y, v.z); }
+__device__ __forceinline__ mm::v3 V(float3 v) { return mm::make3(v.x, v.y, v.z); }
+
+// The ray in a primitive's object space (Ray::Transform, muon/camera.cc:7-11).
+__device__ __forceinline__ void ObjectRay(const DevScene &s, const RayPre &r, int xf, mm::v3 *o, mm::v3 *d) {
+  if (xf < 0) {
+    *o = V(r.o);
+    *d = r.dn;
+  } else {
+    const DevTransform &T = s.transforms[xf];
+    *o = XPointExact(T.w2o, V(r.o));
+    *d = XDirExact(T.w2o, V(r.d));
+  }
+}
+
+// Object-space test with the reference's operations; returns the world
+// distance |M p - o| (muon/objects.cc:38-43) or -1, and the object-space t.
+__device__ __forceinline__ float PrimTestExact(const DevScene &s, const RayPre &r, const PrimRecord &p, uint32_t flags,
+                                               float *t_obj) {
+  using namespace mm;
+  const int xf = __float_as_int((flags & kPrimSphere) ? p.p1.y : p.p1.w);
+  v3 o, d;
+  ObjectRay(s, r, xf, &o, &d);
+  float t;
+  if (flags & kPrimSphere) {
+    v3 dc = o - V(p.p0);
+    float b = dot(d, dc);
+    float c = sub(dot(dc, dc), mul(p.p0.w, p.p0.w));
+    float disc = sub(mul(b, b), c);
+    if (disc < 0.0f) return -1.0f;
+    float sq = fsqrt(disc);
+    float r0 = add(-b, sq), r1 = sub(-b, sq);
+    if (r0 < 0.0f && r1 < 0.0f) return -1.0f;
+    t = fmin_ref(r0, r1);
+    if (t < 0.0f) t = fmax_ref(r0, r1);
+  } else {
+    v3 n = V(p.p3);
+    float dn = dot(n, d);
+    if (dn > -kEps && dn < kEps) return -1.0f;
+    v3 a = V(p.p0), b = V(p.p1), c = V(p.p2);
+    t = div(sub(dot(a, n), dot(o, n)), dn);
+    if (t < 0.0f) return -1.0f;
+    v3 q = o + d * t;
+    if (dot(n, cross(b - a, q - a)) < 0.0f) return -1.0f;
+    if (dot(n, cross(c - b, q - b)) < 0.0f) return -1.0f;
+    if (dot(n, cross(a - c, q - c)) < 0.0f) return -1.0f;
+  }
+  *t_obj = t;
+  v3 q = o + d * t;
+  v3 w = xf < 0 ? q : XPointExact(s.transforms[xf].o2w, q);
+  return length(w - V(r.o));
+}
+
 template <int kTriTest>
-__device__ __forceinline__ float PrimTest(const DevScene &s, const RayPre &r, const PrimRecord &p, uint32_t flags) {
+__device__ __forceinline__ float PrimTest(const DevScene &s, const RayPre &r, const PrimRecord &p, uint32_t flags,
+                                          float *t_obj) {
+  if (kTriTest == MUON_ISECT_EXACT) return PrimTestExact(s, r, p, flags, t_obj);
   if (flags & kPrimSphere) return SphereTest(s, r, p);
-  return kTriTest == MUON_TRI_WATERTIGHT ? TriWatertight(r, p) : TriReference(r, p);
+  return kTriTest == MUON_ISECT_WATERTIGHT ? TriWatertight(r, p) : TriReference(r, p);
 }
 
 __device__ __forceinline__ PrimRecord LoadPrim(const PrimRecord *prims, int i) {
@@ -155,7 +229,7 @@ struct TraceCounters {
 // receives its distance. A stack overflow sets *overflow.
 template <bool kAnyHit, bool kStats, int kTriTest>
 __device__ __forceinline__ int Trace(const DevScene &s, float3 o, float3 d, float tmax, float *t_hit,
-                                     TraceCounters *cnt, bool *overflow) {
+                                     TraceCounters *cnt, bool *overflow, float *t_obj_hit = nullptr) {
   int hit = -1;
   if (s.num_nodes == 0) return -1;
   const RayPre r = Prepare<kTriTest>(o, d);
@@ -210,15 +284,18 @@ __device__ __forceinline__ int Trace(const DevScene &s, float3 o, float3 d, floa
     if (node == kEmptyLink) break;
     // Leaf: test its primitives until the record flagged as last.
     int i = ~node;
+    const PrimRecord *recs = kTriTest == MUON_ISECT_EXACT ? s.prims_obj : s.prims;
     while (true) {
-      PrimRecord p = LoadPrim(s.prims, i);
+      PrimRecord p = LoadPrim(recs, i);
       uint32_t flags = __float_as_uint(p.p3.w);
-      float t = PrimTest<kTriTest>(s, r, p, flags);
+      float t_obj = 0.0f;
+      float t = PrimTest<kTriTest>(s, r, p, flags, &t_obj);
       if (kStats) cnt->prim_tests += 1;
       if (t > 0.0f && t < tmax) {
         if (kStats) cnt->prim_hits += 1;
         tmax = t;
         hit = i;
+        if (kTriTest == MUON_ISECT_EXACT && t_obj_hit) *t_obj_hit = t_obj;
         if (kAnyHit) {
           *t_hit = t;
           return hit;

@@ -16,6 +16,8 @@
 // reserves the block's range with a single atomicAdd.
 #include <cuda_runtime.h>
 
+#include <type_traits>
+
 #include "dev_shade.cuh"
 #include "dev_trace.cuh"
 #include "kernels.cuh"
@@ -109,6 +111,66 @@ __device__ __forceinline__ void HitSurface(const DevScene &s, int slot, float3 o
   *prim_id_out = s1.y;
 }
 
+// Exact counterpart of HitSurface: the hit rebuilt in the primitive's object
+// space from the object-space ray parameter and carried back with the
+// reference's transforms (muon/objects.cc:29-46, 160-174, 261-262).
+__device__ __forceinline__ void HitSurfaceExact(const DevScene &s, int slot, float3 o, float3 d, float t_obj,
+                                                float3 *p_out, float3 *n_out, float *dist_out, int *mat_out,
+                                                int *light_out, int *prim_id_out) {
+  using namespace mm;
+  const float4 *q4 = reinterpret_cast<const float4 *>(s.shade + slot);
+  float4 s0 = __ldg(q4);
+  int4 s1 = __ldg(reinterpret_cast<const int4 *>(q4 + 1));
+  PrimRecord pr = LoadPrim(s.prims_obj, slot);
+  const uint32_t flags = __float_as_uint(pr.p3.w);
+  const int xf = __float_as_int((flags & kPrimSphere) ? pr.p1.y : pr.p1.w);
+  v3 oo, dd;
+  if (xf < 0) {
+    oo = V(o);
+    dd = normalize(V(d));
+  } else {
+    oo = XPointExact(s.transforms[xf].w2o, V(o));
+    dd = XDirExact(s.transforms[xf].w2o, V(d));
+  }
+  v3 q = oo + dd * t_obj;
+  v3 n;
+  if (flags & kPrimSphere) {
+    n = normalize(q - V(pr.p0));
+  } else if (flags & kPrimSmooth) {
+    v3 a = V(pr.p0), b = V(pr.p1), c = V(pr.p2), fn = V(pr.p3);
+    float len2 = pr.p2.w;
+    float v = div(dot(fn, cross(b - a, q - a)), len2);
+    float w = div(dot(fn, cross(c - b, q - b)), len2);
+    float u = div(dot(fn, cross(a - c, q - c)), len2);
+    const F4 *vn = s.smooth_normals_obj + 3 * slot;
+    n = w * V(vn[0]) + u * V(vn[1]) + v * V(vn[2]);
+  } else {
+    n = normalize(V(pr.p3));
+  }
+  v3 pw = xf < 0 ? q : XPointExact(s.transforms[xf].o2w, q);
+  v3 nw = xf < 0 ? normalize(n) : XDirExact(s.transforms[xf].n2w, n);
+  *p_out = f3(pw.x, pw.y, pw.z);
+  *n_out = f3(nw.x, nw.y, nw.z);
+  *dist_out = length(pw - V(o));
+  *mat_out = __float_as_int(s0.w);
+  *light_out = s1.x;
+  *prim_id_out = s1.y;
+}
+
+// Surface at a path vertex in the given intersection mode; `tv` is the value
+// the extend kernel stored (world distance, or the object-space t in exact
+// mode).
+template <int kMode>
+__device__ __forceinline__ void Surface(const DevScene &s, int slot, float3 o, float3 d, float tv, float3 *p,
+                                        float3 *n, float *dist, int *mat, int *light, int *pid) {
+  if (kMode == MUON_ISECT_EXACT) {
+    HitSurfaceExact(s, slot, o, d, tv, p, n, dist, mat, light, pid);
+  } else {
+    HitSurface(s, slot, o, d, tv, p, n, mat, light, pid);
+    *dist = tv;
+  }
+}
+
 __device__ __forceinline__ Rng MakeRng(const WaveInfo &w, int path, uint32_t bounce) {
   int pixel = w.p0 + path / w.ns;
   uint32_t sample = w.sample_offset + static_cast<uint32_t>(w.s0 + path % w.ns);
@@ -159,9 +221,10 @@ __global__ void __launch_bounds__(kBlock) ExtendKernel(DevScene s, const float4 
   bool overflow = false;
   if (j < n) {
     float4 o4 = ray_o[j], d4 = ray_d[j];
-    float t;
-    int h = Trace<false, kStats, kTri>(s, f3(o4.x, o4.y, o4.z), f3(d4.x, d4.y, d4.z), d4.w, &t, &c, &overflow);
-    hits[j] = make_int2(__float_as_int(t), h);
+    float t, t_obj = 0.0f;
+    int h = Trace<false, kStats, kTri>(s, f3(o4.x, o4.y, o4.z), f3(d4.x, d4.y, d4.z), d4.w, &t, &c, &overflow,
+                                       &t_obj);
+    hits[j] = make_int2(__float_as_int(kTri == MUON_ISECT_EXACT ? t_obj : t), h);
   }
   if (kStats) {
     AddStat(stats, kStatBoxTests, c.box_tests);
@@ -200,6 +263,7 @@ __global__ void __launch_bounds__(kBlock) OccludeKernel(DevScene s, const uint32
 
 // ---- deterministic integrators --------------------------------------------
 // NormalsTracer / AlbedoTracer / DepthTracer (muon/integration.cc:47-72).
+template <int kMode>
 __global__ void __launch_bounds__(kBlock) ShadeDebugKernel(DevScene s, PathBuffers b, int integrator, int n) {
   int j = blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= n) return;
@@ -209,16 +273,19 @@ __global__ void __launch_bounds__(kBlock) ShadeDebugKernel(DevScene s, PathBuffe
   float4 out = make_float4(0, 0, 0, 0);
   if (h.y >= 0) {
     float3 p, nrm;
+    float dist;
     int mat, light, pid;
-    float t = __int_as_float(h.x);
-    HitSurface(s, h.y, f3(o4.x, o4.y, o4.z), f3(d4.x, d4.y, d4.z), t, &p, &nrm, &mat, &light, &pid);
+    Surface<kMode>(s, h.y, f3(o4.x, o4.y, o4.z), f3(d4.x, d4.y, d4.z), __int_as_float(h.x), &p, &nrm, &dist, &mat,
+                   &light, &pid);
+    using mm::add;
+    using mm::mul;
     if (integrator == MUON_INTEGRATOR_NORMALS) {
-      out = make_float4(nrm.x * 0.5f + 0.5f, nrm.y * 0.5f + 0.5f, nrm.z * 0.5f + 0.5f, 0.0f);
+      out = make_float4(add(mul(nrm.x, 0.5f), 0.5f), add(mul(nrm.y, 0.5f), 0.5f), add(mul(nrm.z, 0.5f), 0.5f), 0.0f);
     } else if (integrator == MUON_INTEGRATOR_ALBEDO) {
       Mat m = LoadMat(s.materials, mat);
-      out = make_float4(m.kd.x + m.ks.x, m.kd.y + m.ks.y, m.kd.z + m.ks.z, 0.0f);
+      out = make_float4(add(m.kd.x, m.ks.x), add(m.kd.y, m.ks.y), add(m.kd.z, m.ks.z), 0.0f);
     } else {
-      float v = 1.0f / (1.0f + t);
+      float v = mm::div(1.0f, add(1.0f, dist));
       out = make_float4(v, v, v, 0.0f);
     }
   }
@@ -234,6 +301,7 @@ __global__ void __launch_bounds__(kBlock) ShadeDebugKernel(DevScene s, PathBuffe
 // resolved by the occlusion pass) are folded into the path radiance first.
 constexpr int kMaskSlots = 64;
 
+template <int kMode>
 __global__ void __launch_bounds__(kBlock) ShadePathKernel(DevScene s, WaveInfo w, ShadeParams sp, PathBuffers b,
                                                           int buf, int n, int bounce) {
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
@@ -266,8 +334,9 @@ __global__ void __launch_bounds__(kBlock) ShadePathKernel(DevScene s, WaveInfo w
 
     if (h.y >= 0) {
       float3 p, nrm;
+      float hit_dist;
       int mat_id, light_id, pid;
-      HitSurface(s, h.y, o, d, __int_as_float(h.x), &p, &nrm, &mat_id, &light_id, &pid);
+      Surface<kMode>(s, h.y, o, d, __int_as_float(h.x), &p, &nrm, &hit_dist, &mat_id, &light_id, &pid);
       const Mat m = LoadMat(s.materials, mat_id);
       const float3 shift = p + kEps * nrm;
       Rng rng = MakeRng(w, path, static_cast<uint32_t>(bounce));
@@ -351,20 +420,17 @@ __global__ void __launch_bounds__(kBlock) ShadePathKernel(DevScene s, WaveInfo w
               ++counted;
               float best = INFINITY;
               int best_light = -1;
-              if (sp.tri_test == MUON_TRI_WATERTIGHT) {
-                RayPre rp = Prepare<MUON_TRI_WATERTIGHT>(shift, dir);
-                for (int lt = 0; lt < 2 * s.num_lights; ++lt) {
-                  if (!s.light_tri_ok[lt]) continue;
-                  float t = TriWatertight(rp, LoadPrim(s.light_tris, lt));
-                  if (t > 0.0f && t < best) best = t, best_light = lt >> 1;
-                }
-              } else {
-                RayPre rp = Prepare<MUON_TRI_REFERENCE>(shift, dir);
-                for (int lt = 0; lt < 2 * s.num_lights; ++lt) {
-                  if (!s.light_tri_ok[lt]) continue;
-                  float t = TriReference(rp, LoadPrim(s.light_tris, lt));
-                  if (t > 0.0f && t < best) best = t, best_light = lt >> 1;
-                }
+              // Same triangle test and ray preparation as the traversal, so the
+              // light's distance is bit-identical to the one the any-hit
+              // query will compare against.
+              RayPre rp = Prepare<kMode>(shift, dir);
+              const PrimRecord *lts = kMode == MUON_ISECT_EXACT ? s.light_tris_obj : s.light_tris;
+              for (int lt = 0; lt < 2 * s.num_lights; ++lt) {
+                if (!s.light_tri_ok[lt]) continue;
+                PrimRecord lp = LoadPrim(lts, lt);
+                float t_obj;
+                float t = PrimTest<kMode>(s, rp, lp, __float_as_uint(lp.p3.w), &t_obj);
+                if (t > 0.0f && t < best) best = t, best_light = lt >> 1;
               }
               if (best_light >= 0) {
                 float wgt = PowerHeuristic(bpdf, NeePdf(s, shift, dir));
@@ -467,8 +533,8 @@ __global__ void __launch_bounds__(kBlock) IntersectRaysKernel(DevScene s, const 
   float3 o = f3(r[0], r[1], r[2]), d = f3(r[3], r[4], r[5]);
   TraceCounters c;
   bool of = false;
-  float t;
-  int h = Trace<false, false, kTri>(s, o, d, INFINITY, &t, &c, &of);
+  float t, t_obj = 0.0f;
+  int h = Trace<false, false, kTri>(s, o, d, INFINITY, &t, &c, &of, &t_obj);
   float *q = out + 8 * i;
   if (h < 0) {
     q[0] = INFINITY;
@@ -477,9 +543,10 @@ __global__ void __launch_bounds__(kBlock) IntersectRaysKernel(DevScene s, const 
     return;
   }
   float3 p, nrm;
+  float dist;
   int mat, light, pid;
-  HitSurface(s, h, o, d, t, &p, &nrm, &mat, &light, &pid);
-  q[0] = t;
+  Surface<kTri>(s, h, o, d, kTri == MUON_ISECT_EXACT ? t_obj : t, &p, &nrm, &dist, &mat, &light, &pid);
+  q[0] = dist;
   q[1] = __int_as_float(pid);
   q[2] = p.x, q[3] = p.y, q[4] = p.z;
   q[5] = nrm.x, q[6] = nrm.y, q[7] = nrm.z;
@@ -500,45 +567,54 @@ __global__ void __launch_bounds__(kBlock) OccludedRaysKernel(DevScene s, const f
 
 inline unsigned Blocks(int64_t n) { return static_cast<unsigned>((n + kBlock - 1) / kBlock); }
 
+// Calls f(std::integral_constant<int, mode>) for a runtime intersection mode.
+template <class F>
+void WithMode(int mode, F &&f) {
+  if (mode == MUON_ISECT_WATERTIGHT) f(std::integral_constant<int, MUON_ISECT_WATERTIGHT>());
+  else if (mode == MUON_ISECT_EXACT) f(std::integral_constant<int, MUON_ISECT_EXACT>());
+  else f(std::integral_constant<int, MUON_ISECT_FAST>());
+}
+
 }  // namespace
 
 void LaunchCamera(const DevCamera &cam, const WaveInfo &w, const PathBuffers &b, int slots, cudaStream_t st) {
   if (w.n > 0) CameraKernel<<<Blocks(w.n), kBlock, 0, st>>>(cam, w, b, slots);
 }
 
-void LaunchExtend(const DevScene &s, const PathBuffers &b, int buf, int n, int tri_test, bool stats,
-                  cudaStream_t st) {
+void LaunchExtend(const DevScene &s, const PathBuffers &b, int buf, int n, int isect, bool stats, cudaStream_t st) {
   if (n <= 0) return;
-  if (tri_test == MUON_TRI_WATERTIGHT) {
-    if (stats) ExtendKernel<true, MUON_TRI_WATERTIGHT><<<Blocks(n), kBlock, 0, st>>>(s, b.ray_o[buf], b.ray_d[buf], n, b.hits, b.stats);
-    else ExtendKernel<false, MUON_TRI_WATERTIGHT><<<Blocks(n), kBlock, 0, st>>>(s, b.ray_o[buf], b.ray_d[buf], n, b.hits, b.stats);
-  } else {
-    if (stats) ExtendKernel<true, MUON_TRI_REFERENCE><<<Blocks(n), kBlock, 0, st>>>(s, b.ray_o[buf], b.ray_d[buf], n, b.hits, b.stats);
-    else ExtendKernel<false, MUON_TRI_REFERENCE><<<Blocks(n), kBlock, 0, st>>>(s, b.ray_o[buf], b.ray_d[buf], n, b.hits, b.stats);
-  }
+  WithMode(isect, [&](auto m) {
+    constexpr int M = decltype(m)::value;
+    if (stats) ExtendKernel<true, M><<<Blocks(n), kBlock, 0, st>>>(s, b.ray_o[buf], b.ray_d[buf], n, b.hits, b.stats);
+    else ExtendKernel<false, M><<<Blocks(n), kBlock, 0, st>>>(s, b.ray_o[buf], b.ray_d[buf], n, b.hits, b.stats);
+  });
 }
 
-void LaunchShadeDebug(const DevScene &s, const WaveInfo &w, const PathBuffers &b, int integrator, int n,
+void LaunchShadeDebug(const DevScene &s, const WaveInfo &w, const PathBuffers &b, int integrator, int n, int isect,
                       cudaStream_t st) {
   (void)w;
-  if (n > 0) ShadeDebugKernel<<<Blocks(n), kBlock, 0, st>>>(s, b, integrator, n);
+  if (n <= 0) return;
+  WithMode(isect, [&](auto m) {
+    ShadeDebugKernel<decltype(m)::value><<<Blocks(n), kBlock, 0, st>>>(s, b, integrator, n);
+  });
 }
 
 void LaunchShadePath(const DevScene &s, const WaveInfo &w, const ShadeParams &sp, const PathBuffers &b, int buf,
                      int n, int bounce, cudaStream_t st) {
-  if (n > 0) ShadePathKernel<<<Blocks(n), kBlock, 0, st>>>(s, w, sp, b, buf, n, bounce);
+  if (n <= 0) return;
+  WithMode(sp.isect, [&](auto m) {
+    ShadePathKernel<decltype(m)::value><<<Blocks(n), kBlock, 0, st>>>(s, w, sp, b, buf, n, bounce);
+  });
 }
 
-void LaunchOcclude(const DevScene &s, const PathBuffers &b, int slots, int n, int tri_test, bool stats,
+void LaunchOcclude(const DevScene &s, const PathBuffers &b, int slots, int n, int isect, bool stats,
                    cudaStream_t st) {
   if (n <= 0) return;
-  if (tri_test == MUON_TRI_WATERTIGHT) {
-    if (stats) OccludeKernel<true, MUON_TRI_WATERTIGHT><<<Blocks(n), kBlock, 0, st>>>(s, b.shq, slots, n, b.org, b.slot_dir, b.contrib, b.stats);
-    else OccludeKernel<false, MUON_TRI_WATERTIGHT><<<Blocks(n), kBlock, 0, st>>>(s, b.shq, slots, n, b.org, b.slot_dir, b.contrib, b.stats);
-  } else {
-    if (stats) OccludeKernel<true, MUON_TRI_REFERENCE><<<Blocks(n), kBlock, 0, st>>>(s, b.shq, slots, n, b.org, b.slot_dir, b.contrib, b.stats);
-    else OccludeKernel<false, MUON_TRI_REFERENCE><<<Blocks(n), kBlock, 0, st>>>(s, b.shq, slots, n, b.org, b.slot_dir, b.contrib, b.stats);
-  }
+  WithMode(isect, [&](auto m) {
+    constexpr int M = decltype(m)::value;
+    if (stats) OccludeKernel<true, M><<<Blocks(n), kBlock, 0, st>>>(s, b.shq, slots, n, b.org, b.slot_dir, b.contrib, b.stats);
+    else OccludeKernel<false, M><<<Blocks(n), kBlock, 0, st>>>(s, b.shq, slots, n, b.org, b.slot_dir, b.contrib, b.stats);
+  });
 }
 
 void LaunchFilm(const WaveInfo &w, const PathBuffers &b, int slots, double *sum, double *sum_sq, uint32_t *count,
@@ -546,18 +622,19 @@ void LaunchFilm(const WaveInfo &w, const PathBuffers &b, int slots, double *sum,
   if (w.npix > 0) FilmKernel<<<Blocks(w.npix), kBlock, 0, st>>>(w, b, slots, sum, sum_sq, count);
 }
 
-void LaunchIntersectRays(const DevScene &s, const float *rays, int64_t n, int tri_test, float *out_hit,
-                         cudaStream_t st) {
+void LaunchIntersectRays(const DevScene &s, const float *rays, int64_t n, int isect, float *out_hit, cudaStream_t st) {
   if (n <= 0) return;
-  if (tri_test == MUON_TRI_WATERTIGHT) IntersectRaysKernel<MUON_TRI_WATERTIGHT><<<Blocks(n), kBlock, 0, st>>>(s, rays, n, out_hit);
-  else IntersectRaysKernel<MUON_TRI_REFERENCE><<<Blocks(n), kBlock, 0, st>>>(s, rays, n, out_hit);
+  WithMode(isect, [&](auto m) {
+    IntersectRaysKernel<decltype(m)::value><<<Blocks(n), kBlock, 0, st>>>(s, rays, n, out_hit);
+  });
 }
 
-void LaunchOccludedRays(const DevScene &s, const float *rays, const float *maxd, int64_t n, int tri_test,
-                        uint8_t *out, cudaStream_t st) {
+void LaunchOccludedRays(const DevScene &s, const float *rays, const float *maxd, int64_t n, int isect, uint8_t *out,
+                        cudaStream_t st) {
   if (n <= 0) return;
-  if (tri_test == MUON_TRI_WATERTIGHT) OccludedRaysKernel<MUON_TRI_WATERTIGHT><<<Blocks(n), kBlock, 0, st>>>(s, rays, maxd, n, out);
-  else OccludedRaysKernel<MUON_TRI_REFERENCE><<<Blocks(n), kBlock, 0, st>>>(s, rays, maxd, n, out);
+  WithMode(isect, [&](auto m) {
+    OccludedRaysKernel<decltype(m)::value><<<Blocks(n), kBlock, 0, st>>>(s, rays, maxd, n, out);
+  });
 }
 
 }  // namespace muon_gpu

@@ -60,24 +60,24 @@ struct ShadeParams {
   int32_t light_samples;
   int32_t slots;           // shadow slots per path
   int32_t mis_slot;        // slot index of the MIS ray, -1 if none
-  int32_t tri_test;
+  int32_t isect;
   int32_t max_bounces;
 };
 
 void LaunchCamera(const DevCamera &cam, const WaveInfo &w, const PathBuffers &b, int slots, cudaStream_t st);
-void LaunchExtend(const DevScene &s, const PathBuffers &b, int buf, int n, int tri_test, bool stats,
+void LaunchExtend(const DevScene &s, const PathBuffers &b, int buf, int n, int isect, bool stats,
                   cudaStream_t st);
-void LaunchShadeDebug(const DevScene &s, const WaveInfo &w, const PathBuffers &b, int integrator, int n,
+void LaunchShadeDebug(const DevScene &s, const WaveInfo &w, const PathBuffers &b, int integrator, int n, int isect,
                       cudaStream_t st);
 void LaunchShadePath(const DevScene &s, const WaveInfo &w, const ShadeParams &sp, const PathBuffers &b, int buf,
                      int n, int bounce, cudaStream_t st);
-void LaunchOcclude(const DevScene &s, const PathBuffers &b, int slots, int n, int tri_test, bool stats, cudaStream_t st);
+void LaunchOcclude(const DevScene &s, const PathBuffers &b, int slots, int n, int isect, bool stats, cudaStream_t st);
 void LaunchFilm(const WaveInfo &w, const PathBuffers &b, int slots, double *sum, double *sum_sq, uint32_t *count,
                 cudaStream_t st);
 // Ray-level queries for the batched Intersect/HasIntersection seams.
-void LaunchIntersectRays(const DevScene &s, const float *rays, int64_t n, int tri_test, float *out_hit,
+void LaunchIntersectRays(const DevScene &s, const float *rays, int64_t n, int isect, float *out_hit,
                          cudaStream_t st);
-void LaunchOccludedRays(const DevScene &s, const float *rays, const float *maxd, int64_t n, int tri_test,
+void LaunchOccludedRays(const DevScene &s, const float *rays, const float *maxd, int64_t n, int isect,
                         uint8_t *out, cudaStream_t st);
 
 }  // namespace muon_gpu

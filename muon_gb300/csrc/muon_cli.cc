@@ -1,7 +1,7 @@
 // `muon` command-line renderer on the GPU path. Accepts the reference CLI's
 // flags (muon/muon.cc:12-21): --scene, --output, --acceleration,
 // --partition_strategy, --parallelism (host threads; unused, the GPU renders),
-// --stats; plus --samples / --seed overrides and --triangle_test.
+// --stats; plus --samples / --seed overrides and --intersect_mode.
 #include <chrono>
 #include <cstdio>
 #include <cstdlib>
@@ -30,7 +30,7 @@ bool Flag(const char *arg, const char *name, std::string *value) {
 }  // namespace
 
 int main(int argc, char **argv) {
-  std::string scene, output, accel = "bvh", partition = "sah", stats = "true", samples, seed, tri = "reference";
+  std::string scene, output, accel = "bvh", partition = "sah", stats = "true", samples, seed, tri = "exact";
   for (int i = 1; i < argc; ++i) {
     std::string v;
     if (Flag(argv[i], "--scene", &v)) scene = v;
@@ -41,7 +41,7 @@ int main(int argc, char **argv) {
     else if (Flag(argv[i], "--stats", &v)) stats = v.empty() ? "true" : v;
     else if (Flag(argv[i], "--samples", &v)) samples = v;
     else if (Flag(argv[i], "--seed", &v)) seed = v;
-    else if (Flag(argv[i], "--triangle_test", &v)) tri = v;
+    else if (Flag(argv[i], "--intersect_mode", &v)) tri = v;
     else {
       std::fprintf(stderr, "unknown flag %s\n", argv[i]);
       return 1;
@@ -75,7 +75,7 @@ int main(int argc, char **argv) {
   }
   if (!samples.empty()) params.pixel_samples = std::atoi(samples.c_str());
   if (!seed.empty()) params.seed = std::strtoull(seed.c_str(), nullptr, 10);
-  params.triangle_test = tri == "watertight" ? MUON_TRI_WATERTIGHT : MUON_TRI_REFERENCE;
+  params.intersect_mode = tri == "watertight" ? MUON_ISECT_WATERTIGHT : (tri == "fast" ? MUON_ISECT_FAST : MUON_ISECT_EXACT);
   MuonScene *gs = nullptr;
   if (muon_gpu_scene_create(&desc, &gs) != MUON_OK) {
     std::fprintf(stderr, "scene upload failed: %s\n", muon_gpu_last_error());

@@ -80,7 +80,8 @@ struct MuonScene {
   DevScene dev{};
   DevCamera cam{};
   // scene arrays
-  DeviceBuffer nodes, prims, shade, smooth, transforms, materials, lights, light_tris, light_tri_ok, other_lights;
+  DeviceBuffer nodes, prims, prims_obj, shade, smooth, smooth_obj, transforms, materials, lights, light_tris,
+      light_tris_obj, light_tri_ok, other_lights;
   // work arrays
   DeviceBuffer ray_o[2], ray_d[2], hits, tp, rad, org, contrib, slot_dir, shq, counters, stats;
   DeviceBuffer film_sum, film_sq, film_cnt, ray_in, ray_out, ray_aux;
@@ -203,8 +204,8 @@ int ValidateParams(const MuonRenderParams &p) {
     return Fail(MUON_ERR_INVALID_ARG, "unknown next_event_estimation mode");
   if (p.importance_sampling < MUON_IS_HEMISPHERE || p.importance_sampling > MUON_IS_BRDF)
     return Fail(MUON_ERR_INVALID_ARG, "unknown importance_sampling mode");
-  if (p.triangle_test != MUON_TRI_REFERENCE && p.triangle_test != MUON_TRI_WATERTIGHT)
-    return Fail(MUON_ERR_INVALID_ARG, "unknown triangle_test");
+  if (p.intersect_mode < MUON_ISECT_FAST || p.intersect_mode > MUON_ISECT_EXACT)
+    return Fail(MUON_ERR_INVALID_ARG, "unknown intersect_mode");
   if (p.integrator == MUON_INTEGRATOR_PATHTRACER && p.next_event_estimation != MUON_NEE_OFF && p.light_samples < 1)
     return Fail(MUON_ERR_INVALID_ARG, "light_samples must be >= 1");
   if (p.max_depth < -1) return Fail(MUON_ERR_INVALID_ARG, "max_depth must be >= -1");
@@ -230,7 +231,7 @@ void RenderDevice(MuonScene *sc, const MuonRenderParams &p, double *d_sum, doubl
   sp.per_section = p.light_stratify ? 1 : p.light_samples;
   sp.per_light = sp.strata * sp.strata * sp.per_section;
   sp.light_samples = std::max(1, p.light_samples);
-  sp.tri_test = p.triangle_test;
+  sp.isect = p.intersect_mode;
   sp.max_bounces = kMaxBounces;
   int slots = 0;
   sp.mis_slot = -1;
@@ -280,11 +281,11 @@ void RenderDevice(MuonScene *sc, const MuonRenderParams &p, double *d_sum, doubl
         for (int bounce = 0; n_cur > 0; ++bounce) {
           EventPair *ev = sc->NextEvent(0);
           if (ev) CUDA_TRY(cudaEventRecord(ev->a, st));
-          LaunchExtend(sc->dev, b, buf, n_cur, p.triangle_test, stats_on, st);
+          LaunchExtend(sc->dev, b, buf, n_cur, p.intersect_mode, stats_on, st);
           if (ev) CUDA_TRY(cudaEventRecord(ev->b, st));
           ++launches;
           if (!pt) {
-            LaunchShadeDebug(sc->dev, w, b, p.integrator, n_cur, st);
+            LaunchShadeDebug(sc->dev, w, b, p.integrator, n_cur, p.intersect_mode, st);
             ++launches;
             break;
           }
@@ -299,7 +300,7 @@ void RenderDevice(MuonScene *sc, const MuonRenderParams &p, double *d_sum, doubl
           if (n_sh > 0) {
             EventPair *eo = sc->NextEvent(1);
             if (eo) CUDA_TRY(cudaEventRecord(eo->a, st));
-            LaunchOcclude(sc->dev, b, slots, n_sh, p.triangle_test, stats_on, st);
+            LaunchOcclude(sc->dev, b, slots, n_sh, p.intersect_mode, stats_on, st);
             if (eo) CUDA_TRY(cudaEventRecord(eo->b, st));
             ++launches;
           }
@@ -368,15 +369,17 @@ int muon_gpu_scene_create(const MuonSceneDesc *desc, MuonScene **out) {
     const SceneImage &im = sc->img;
     Upload(sc->nodes, im.nodes, st);
     Upload(sc->prims, im.prims, st);
+    Upload(sc->prims_obj, im.prims_obj, st);
     Upload(sc->shade, im.shade, st);
     Upload(sc->smooth, im.smooth_normals, st);
+    Upload(sc->smooth_obj, im.smooth_normals_obj, st);
     Upload(sc->transforms, im.transforms, st);
     Upload(sc->materials, im.materials, st);
     Upload(sc->lights, im.lights, st);
     Upload(sc->other_lights, im.other_lights, st);
     // The two triangles of each quad light (muon/parser.cc:735-747), in the
     // same record format as the BVH's, for the MIS light-hit test.
-    std::vector<PrimRecord> lt(2 * im.lights.size());
+    std::vector<PrimRecord> lt(2 * im.lights.size()), lt_obj(2 * im.lights.size());
     std::vector<int32_t> lt_ok(2 * im.lights.size(), 0);
     for (size_t i = 0; i < im.lights.size(); ++i) {
       const DevLight &l = im.lights[i];
@@ -392,19 +395,31 @@ int muon_gpu_scene_create(const MuonSceneDesc *desc, MuonScene **out) {
         r.p2 = F4{tri[t][2].x, tri[t][2].y, tri[t][2].z, 0.0f};
         r.p3 = F4{n.x, n.y, n.z, 0.0f};
         lt_ok[2 * i + t] = mm::length(n) >= 1e-4f ? 1 : 0;
+        PrimRecord &ro = lt_obj[2 * i + t];
+        int32_t identity = -1;
+        float xf_bits;
+        std::memcpy(&xf_bits, &identity, 4);
+        ro.p0 = F4{tri[t][0].x, tri[t][0].y, tri[t][0].z, 0.0f};
+        ro.p1 = F4{tri[t][1].x, tri[t][1].y, tri[t][1].z, xf_bits};
+        ro.p2 = F4{tri[t][2].x, tri[t][2].y, tri[t][2].z, mm::dot(n, n)};
+        ro.p3 = F4{n.x, n.y, n.z, 0.0f};
       }
     }
     Upload(sc->light_tris, lt, st);
+    Upload(sc->light_tris_obj, lt_obj, st);
     Upload(sc->light_tri_ok, lt_ok, st);
     DevScene &d = sc->dev;
     d.nodes = sc->nodes.as<BvhNode>();
     d.prims = sc->prims.as<PrimRecord>();
+    d.prims_obj = sc->prims_obj.as<PrimRecord>();
     d.shade = sc->shade.as<ShadeRecord>();
     d.smooth_normals = im.any_smooth ? sc->smooth.as<F4>() : nullptr;
+    d.smooth_normals_obj = im.any_smooth ? sc->smooth_obj.as<F4>() : nullptr;
     d.transforms = sc->transforms.as<DevTransform>();
     d.materials = sc->materials.as<DevMaterial>();
     d.lights = sc->lights.as<DevLight>();
     d.light_tris = sc->light_tris.as<PrimRecord>();
+    d.light_tris_obj = sc->light_tris_obj.as<PrimRecord>();
     d.light_tri_ok = sc->light_tri_ok.as<int32_t>();
     d.other_lights = sc->other_lights.as<DevLight>();
     d.num_nodes = static_cast<int32_t>(im.nodes.size());
@@ -482,10 +497,10 @@ int muon_gpu_render(MuonScene *scene, const MuonRenderParams *params, MuonFilm *
   return MUON_OK;
 }
 
-int muon_gpu_intersect(MuonScene *scene, const MuonRay *rays, int64_t n, int32_t triangle_test, MuonHit *hits) {
+int muon_gpu_intersect(MuonScene *scene, const MuonRay *rays, int64_t n, int32_t intersect_mode, MuonHit *hits) {
   if (!scene || (n > 0 && (!rays || !hits)) || n < 0) return Fail(MUON_ERR_INVALID_ARG, "bad argument");
-  if (triangle_test != MUON_TRI_REFERENCE && triangle_test != MUON_TRI_WATERTIGHT)
-    return Fail(MUON_ERR_INVALID_ARG, "unknown triangle_test");
+  if (intersect_mode < MUON_ISECT_FAST || intersect_mode > MUON_ISECT_EXACT)
+    return Fail(MUON_ERR_INVALID_ARG, "unknown intersect_mode");
   if (n == 0) return MUON_OK;
   static_assert(sizeof(MuonRay) == 24 && sizeof(MuonHit) == 32, "ray/hit layout");
   try {
@@ -494,7 +509,7 @@ int muon_gpu_intersect(MuonScene *scene, const MuonRay *rays, int64_t n, int32_t
     scene->ray_in.Ensure(n * sizeof(MuonRay));
     scene->ray_out.Ensure(n * sizeof(MuonHit));
     CUDA_TRY(cudaMemcpyAsync(scene->ray_in.ptr, rays, n * sizeof(MuonRay), cudaMemcpyHostToDevice, st));
-    LaunchIntersectRays(scene->dev, scene->ray_in.as<float>(), n, triangle_test, scene->ray_out.as<float>(), st);
+    LaunchIntersectRays(scene->dev, scene->ray_in.as<float>(), n, intersect_mode, scene->ray_out.as<float>(), st);
     CUDA_TRY(cudaGetLastError());
     CUDA_TRY(cudaMemcpyAsync(hits, scene->ray_out.ptr, n * sizeof(MuonHit), cudaMemcpyDeviceToHost, st));
     CUDA_TRY(cudaStreamSynchronize(st));
@@ -505,11 +520,11 @@ int muon_gpu_intersect(MuonScene *scene, const MuonRay *rays, int64_t n, int32_t
 }
 
 int muon_gpu_occluded(MuonScene *scene, const MuonRay *rays, const float *max_distance, int64_t n,
-                      int32_t triangle_test, uint8_t *occluded) {
+                      int32_t intersect_mode, uint8_t *occluded) {
   if (!scene || (n > 0 && (!rays || !max_distance || !occluded)) || n < 0)
     return Fail(MUON_ERR_INVALID_ARG, "bad argument");
-  if (triangle_test != MUON_TRI_REFERENCE && triangle_test != MUON_TRI_WATERTIGHT)
-    return Fail(MUON_ERR_INVALID_ARG, "unknown triangle_test");
+  if (intersect_mode < MUON_ISECT_FAST || intersect_mode > MUON_ISECT_EXACT)
+    return Fail(MUON_ERR_INVALID_ARG, "unknown intersect_mode");
   if (n == 0) return MUON_OK;
   try {
     CUDA_TRY(cudaSetDevice(scene->device));
@@ -519,7 +534,7 @@ int muon_gpu_occluded(MuonScene *scene, const MuonRay *rays, const float *max_di
     scene->ray_out.Ensure(n);
     CUDA_TRY(cudaMemcpyAsync(scene->ray_in.ptr, rays, n * sizeof(MuonRay), cudaMemcpyHostToDevice, st));
     CUDA_TRY(cudaMemcpyAsync(scene->ray_aux.ptr, max_distance, n * sizeof(float), cudaMemcpyHostToDevice, st));
-    LaunchOccludedRays(scene->dev, scene->ray_in.as<float>(), scene->ray_aux.as<float>(), n, triangle_test,
+    LaunchOccludedRays(scene->dev, scene->ray_in.as<float>(), scene->ray_aux.as<float>(), n, intersect_mode,
                        scene->ray_out.as<uint8_t>(), st);
     CUDA_TRY(cudaGetLastError());
     CUDA_TRY(cudaMemcpyAsync(occluded, scene->ray_out.ptr, n, cudaMemcpyDeviceToHost, st));

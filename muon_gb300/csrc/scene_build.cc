@@ -436,12 +436,12 @@ bool BuildSceneImage(const MuonSceneDesc &desc, SceneImage *img, std::string *er
   std::vector<int64_t> source;  // box -> primitive (tri i, or ntri + sphere j)
   boxes.reserve(ntri + nsph);
   source.reserve(ntri + nsph);
-  std::vector<PrimRecord> tri_rec(ntri);
+  std::vector<PrimRecord> tri_rec(ntri), tri_obj(ntri);
   std::vector<ShadeRecord> tri_shade(ntri);
-  std::vector<F4> tri_normals;
+  std::vector<F4> tri_normals, tri_normals_obj;
   img->any_smooth = false;
   for (int64_t i = 0; i < ntri; ++i) img->any_smooth |= desc.triangles[i].smooth != 0;
-  if (img->any_smooth) tri_normals.resize(3 * ntri);
+  if (img->any_smooth) tri_normals.resize(3 * ntri), tri_normals_obj.resize(3 * ntri);
   img->leaf_of_prim_id.assign(img->num_prims, -1);
 
   for (int64_t i = 0; i < ntri; ++i) {
@@ -464,6 +464,10 @@ bool BuildSceneImage(const MuonSceneDesc &desc, SceneImage *img, std::string *er
     float len_obj = mm::length(n_obj);
     float eps = 1e-4f;
     if (t.transform >= 0) eps = 1e-4f * (mm::length(n_w) / len_obj);
+    PrimRecord &ro = tri_obj[i];
+    ro.p0 = MakeF4(ov[0].x, ov[0].y, ov[0].z, 0.0f);
+    ro.p1 = MakeF4(ov[1].x, ov[1].y, ov[1].z, IntBits(t.transform));
+    ro.p2 = MakeF4(ov[2].x, ov[2].y, ov[2].z, mm::dot(n_obj, n_obj));
     PrimRecord &r = tri_rec[i];
     r.p0 = MakeF4(wv[0].x, wv[0].y, wv[0].z, mm::dot(wv[0], n_w));
     r.p1 = MakeF4(wv[1].x, wv[1].y, wv[1].z, eps);
@@ -479,6 +483,8 @@ bool BuildSceneImage(const MuonSceneDesc &desc, SceneImage *img, std::string *er
     s.s0 = MakeF4(un.x, un.y, un.z, IntBits(t.material));
     s.s1 = I4{t.light >= 0 ? quad_index[t.light] : -1, t.prim_id, t.transform, static_cast<int32_t>(flags)};
     std::memcpy(&r.p3.w, &flags, 4);
+    ro.p3 = r.p3;
+    ro.p3.x = n_obj.x, ro.p3.y = n_obj.y, ro.p3.z = n_obj.z;
     if (t.smooth) {
       // normalize(M^-T (w n0 + u n1 + v n2)) equals the normalised blend of
       // the pre-transformed vertex normals, by linearity.
@@ -487,6 +493,7 @@ bool BuildSceneImage(const MuonSceneDesc &desc, SceneImage *img, std::string *er
         mm::v3 vn = V3(t.n[k]);
         mm::v4 w4 = t.transform >= 0 ? mm::mul(nt, mm::v4{vn.x, vn.y, vn.z, 0.0f}) : mm::v4{vn.x, vn.y, vn.z, 0.0f};
         tri_normals[3 * i + k] = MakeF4(w4.x, w4.y, w4.z, 0.0f);
+        tri_normals_obj[3 * i + k] = MakeF4(vn.x, vn.y, vn.z, 0.0f);
       }
     }
     // |d.n| <= |n| for a unit direction, so such a triangle is never hit.
@@ -548,21 +555,28 @@ bool BuildSceneImage(const MuonSceneDesc &desc, SceneImage *img, std::string *er
   int max_leaf = desc.max_leaf_size > 0 ? desc.max_leaf_size : 4;
   BuildBvh(boxes, desc.acceleration, desc.partition_strategy, max_leaf, &img->nodes, &order, &last, &img->bvh);
   img->prims.resize(order.size());
+  img->prims_obj.resize(order.size());
   img->shade.resize(order.size());
-  if (img->any_smooth) img->smooth_normals.resize(3 * order.size());
+  if (img->any_smooth) img->smooth_normals.resize(3 * order.size()), img->smooth_normals_obj.resize(3 * order.size());
   for (size_t slot = 0; slot < order.size(); ++slot) {
     int64_t src = source[order[slot]];
     PrimRecord r = src < ntri ? tri_rec[src] : sph_rec[src - ntri];
+    PrimRecord ro = src < ntri ? tri_obj[src] : sph_rec[src - ntri];
     ShadeRecord s = src < ntri ? tri_shade[src] : sph_shade[src - ntri];
     uint32_t flags;
     std::memcpy(&flags, &r.p3.w, 4);
     if (last[slot]) flags |= kPrimLast;
     std::memcpy(&r.p3.w, &flags, 4);
+    std::memcpy(&ro.p3.w, &flags, 4);
     img->prims[slot] = r;
+    img->prims_obj[slot] = ro;
     img->shade[slot] = s;
     img->leaf_of_prim_id[s.s1.y] = static_cast<int32_t>(slot);
     if (img->any_smooth && src < ntri) {
-      for (int k = 0; k < 3; ++k) img->smooth_normals[3 * slot + k] = tri_normals[3 * src + k];
+      for (int k = 0; k < 3; ++k) {
+        img->smooth_normals[3 * slot + k] = tri_normals[3 * src + k];
+        img->smooth_normals_obj[3 * slot + k] = tri_normals_obj[3 * src + k];
+      }
     }
   }
   return true;

@@ -34,9 +34,11 @@ void BuildBvh(const std::vector<Aabb> &boxes, int accel, int strategy, int max_l
 
 struct SceneImage {
   std::vector<BvhNode> nodes;
-  std::vector<PrimRecord> prims;          // leaf order
+  std::vector<PrimRecord> prims;          // leaf order, world space
+  std::vector<PrimRecord> prims_obj;      // leaf order, object space (exact mode)
   std::vector<ShadeRecord> shade;         // leaf order
   std::vector<F4> smooth_normals;         // 3 per leaf slot when any triangle is smooth
+  std::vector<F4> smooth_normals_obj;     // the same in object space
   std::vector<DevTransform> transforms;
   std::vector<DevMaterial> materials;
   std::vector<DevLight> lights;           // quad lights only

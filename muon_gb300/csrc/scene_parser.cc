@@ -76,7 +76,7 @@ class Parser {
     s_->params.importance_sampling = MUON_IS_HEMISPHERE;
     s_->params.min_depth = 0;
     s_->params.max_depth = 5;
-    s_->params.triangle_test = MUON_TRI_REFERENCE;
+    s_->params.intersect_mode = MUON_ISECT_EXACT;
   }
 
   void Line(const std::string &raw);

@@ -18,7 +18,7 @@ ERRORS = {1: "invalid argument", 2: "out of memory", 3: "CUDA error", 4: "device
 INTEGRATORS = {"normals": 0, "albedo": 1, "depth": 2, "raytracer": 3, "analyticdirect": 4, "pathtracer": 5}
 NEE = {"off": 0, "on": 1, "mis": 2}
 IMPORTANCE = {"hemisphere": 0, "cosine": 1, "brdf": 2}
-TRI_REFERENCE, TRI_WATERTIGHT = 0, 1
+ISECT_FAST, ISECT_WATERTIGHT, ISECT_EXACT = 0, 1, 2
 ACCEL_LINEAR, ACCEL_BVH = 0, 1
 PARTITION = {"uniform": 0, "midpoint": 1, "sah": 2}
 RENDER_STATS, RENDER_ACCUMULATE = 1, 2
@@ -72,7 +72,7 @@ class RenderParams(C.Structure):
                 ("light_stratify", C.c_int32), ("next_event_estimation", C.c_int32),
                 ("russian_roulette", C.c_int32), ("importance_sampling", C.c_int32), ("min_depth", C.c_int32),
                 ("max_depth", C.c_int32), ("sample_offset", C.c_int32), ("seed", C.c_uint64),
-                ("triangle_test", C.c_int32), ("wave_paths", C.c_int32), ("flags", C.c_uint32),
+                ("intersect_mode", C.c_int32), ("wave_paths", C.c_int32), ("flags", C.c_uint32),
                 ("pad", C.c_int32)]
 
 

@@ -1,88 +1,113 @@
 """Ray-level parity with the reference renderer on the GPU.
 
 The golden fixtures hold the reference's own sample-0 camera rays and closest
-hits (tests/golden/make_fixtures.py). Hit primitive ids must agree on at least
-99.99% of pixels; the remainder may only be rays that graze an edge shared by
-two primitives (both hit within 1e-5 of the same distance). Distances and
-normals agree within 1e-5 relative.
+hits (tests/golden/make_fixtures.py runs the reference build). In the EXACT
+intersection mode the GPU repeats the reference's arithmetic, so wherever it
+reports the same primitive the distance, normal and integrator outputs are
+bit-identical. Primitive ids may differ only where two primitives are hit at
+exactly the same distance (a ray through a shared edge), where the winner
+depends on traversal order: the reference's own BVH and linear structures
+disagree there too. Such pixels must stay below 0.5% and must be exact ties.
+FAST and WATERTIGHT mode agree to the stated tolerances.
 """
 import numpy as np
 import pytest
 
 import muon_gb300 as m
 from conftest import GOLDEN
+from muon_gb300 import native
 
 SCENES = ["cornell", "sphere_field", "feature_mix"]
-REL_TOL = 1e-5
 
 
 def load(name):
     return np.load(f"{GOLDEN}/hits_{name}.npz")
 
 
+def ref_ids(fx):
+    return np.where(fx["hit"] == 1, fx["prim_id"], -1)
+
+
 @pytest.mark.gpu
 @pytest.mark.parametrize("name", SCENES)
-def test_closest_hit_ids_match_reference(lib, name):
+def test_exact_hits_are_bitwise_equal_to_reference(lib, name):
     fx = load(name)
     scene = m.Scene.from_string(str(fx["scene"]))
     rays = fx["rays"]
-    dist, pid, pos, nrm = scene.intersect(rays[:, :3], rays[:, 3:])
-    ref_id = np.where(fx["hit"] == 1, fx["prim_id"], -1)
-    agree = pid == ref_id
-    frac = agree.mean()
-    bad = np.nonzero(~agree)[0]
-    # a disagreement is acceptable only at an edge: both sides hit, same distance
-    edge = (pid[bad] >= 0) & (ref_id[bad] >= 0) & (np.abs(dist[bad] - fx["distance"][bad]) <= 1e-5 * fx["distance"][bad])
-    print(f"{name}: id agreement {frac:.6f}, {len(bad)} differing, {int(edge.sum())} at shared edges")
-    assert frac >= 0.9999 or bool(edge.all())
-    assert (~agree).sum() <= max(2, int(0.0001 * len(pid))) + int(edge.sum())
-    both = agree & (ref_id >= 0)
+    dist, pid, pos, nrm = scene.intersect(rays[:, :3], rays[:, 3:], native.ISECT_EXACT)
+    rid = ref_ids(fx)
+    agree = pid == rid
+    tie = ~agree & (pid >= 0) & (rid >= 0) & (dist == fx["distance"])
+    print(f"{name}: ids agree on {agree.mean() * 100:.4f}% of pixels, {int(tie.sum())} exact ties, "
+          f"{int((~agree & ~tie).sum())} other")
+    assert not (~agree & ~tie).any()
+    assert tie.mean() <= 0.005
+    both = agree & (rid >= 0)
+    assert np.array_equal(dist[both], fx["distance"][both])
+    assert np.array_equal(nrm[both], fx["normal"][both])
+
+
+# (mode, relative distance tolerance, minimum id agreement)
+LOOSE = [(native.ISECT_FAST, 5e-4, 0.995), (native.ISECT_WATERTIGHT, 5e-4, 0.995)]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", SCENES)
+@pytest.mark.parametrize("mode,rtol,min_agree", LOOSE)
+def test_fast_modes_agree_within_tolerance(lib, name, mode, rtol, min_agree):
+    fx = load(name)
+    scene = m.Scene.from_string(str(fx["scene"]))
+    rays = fx["rays"]
+    dist, pid, _, nrm = scene.intersect(rays[:, :3], rays[:, 3:], mode)
+    rid = ref_ids(fx)
+    agree = pid == rid
+    print(f"{name} mode {mode}: ids agree on {agree.mean() * 100:.4f}%")
+    assert agree.mean() >= min_agree
+    both = agree & (rid >= 0)
     d_ref = fx["distance"][both]
-    assert np.all(np.abs(dist[both] - d_ref) <= REL_TOL * np.maximum(d_ref, 1.0))
-    n_ref = fx["normal"][both]
-    assert np.all(np.abs(nrm[both] - n_ref) <= REL_TOL)
+    assert np.all(np.abs(dist[both] - d_ref) <= rtol * d_ref)
 
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("name", SCENES)
-def test_occlusion_matches_closest_hit(lib, name):
+@pytest.mark.parametrize("mode", [native.ISECT_FAST, native.ISECT_WATERTIGHT, native.ISECT_EXACT])
+def test_occlusion_matches_closest_hit(lib, name, mode):
     fx = load(name)
     scene = m.Scene.from_string(str(fx["scene"]))
     rays = fx["rays"]
-    dist, pid, _, _ = scene.intersect(rays[:, :3], rays[:, 3:])
+    dist, pid, _, _ = scene.intersect(rays[:, :3], rays[:, 3:], mode)
     hit = pid >= 0
     far = np.where(hit, dist * 1.001, np.float32(1e30)).astype(np.float32)
     near = np.where(hit, dist * 0.999, np.float32(1e30)).astype(np.float32)
-    occ_far = scene.occluded(rays[:, :3], rays[:, 3:], far)
-    occ_near = scene.occluded(rays[:, :3], rays[:, 3:], near)
-    assert np.array_equal(occ_far, hit)
-    assert not occ_near[hit].any()
+    assert np.array_equal(scene.occluded(rays[:, :3], rays[:, 3:], far, mode), hit)
+    assert not scene.occluded(rays[:, :3], rays[:, 3:], near, mode)[hit].any()
 
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("name", SCENES)
 @pytest.mark.parametrize("integrator", ["normals", "albedo", "depth"])
-def test_debug_integrators_match_reference(lib, name, integrator):
+def test_debug_integrators_are_bitwise_equal(lib, name, integrator):
+    """NormalsTracer/AlbedoTracer/DepthTracer (muon/integration.cc:47-72) at
+    sample 0: film values and 8-bit output equal the reference's."""
     fx = load(name)
     scene = m.Scene.from_string(str(fx["scene"]))
     film = scene.render(integrator=integrator, pixel_samples=1)
     assert np.all(film.count == 1)
-    h, w = film.height, film.width
-    got = film.sum.reshape(-1, 3)
+    got = film.sum.reshape(-1, 3).astype(np.float32)
     hit = fx["hit"] == 1
+    f = np.float32
     if integrator == "normals":
-        ref = np.where(hit[:, None], fx["normal"] * np.float32(0.5) + np.float32(0.5), 0)
+        ref = np.where(hit[:, None], fx["normal"] * f(0.5) + f(0.5), f(0))
     elif integrator == "albedo":
-        ref = np.where(hit[:, None], fx["albedo"], 0)
+        ref = np.where(hit[:, None], fx["albedo"], f(0))
     else:
-        ref = np.where(hit[:, None], np.float32(1) / (np.float32(1) + fx["distance"][:, None]), 0)
-    dist, pid, _, _ = scene.intersect(fx["rays"][:, :3], fx["rays"][:, 3:])
-    same = pid == np.where(hit, fx["prim_id"], -1)
-    err = np.abs(got - ref)[same]
-    assert np.all(err <= REL_TOL * np.maximum(np.abs(ref[same]), 1.0)), err.max()
-    # 8-bit output as Film::WriteOutput would write it
+        ref = np.where(hit[:, None], f(1) / (f(1) + fx["distance"][:, None]), f(0))
+    _, pid, _, _ = scene.intersect(fx["rays"][:, :3], fx["rays"][:, 3:], native.ISECT_EXACT)
+    same = pid == ref_ids(fx)
+    assert np.array_equal(got[same], ref[same].astype(np.float32))
     img = film.tonemap(1.0).reshape(-1, 3)
-    ref8 = (np.clip(ref.astype(np.float32), 0, 1) * np.float32(255)).astype(np.uint8)
-    diff = (img != ref8).any(axis=1).mean()
-    print(f"{name}/{integrator}: {diff * 100:.4f}% of pixels differ in 8-bit output")
-    assert diff <= 0.001
+    ref8 = (np.minimum(np.maximum(ref.astype(np.float32), f(0)), f(1)) * f(255)).astype(np.uint8)
+    differ = (img != ref8).any(axis=1)
+    print(f"{name}/{integrator}: {int(differ.sum())} of {len(differ)} pixels differ in 8-bit output "
+          f"({int((differ & ~same).sum())} of them at exact ties)")
+    assert not (differ & same).any()

@@ -1,0 +1,113 @@
+"""Statistical parity of the GPU path tracer with the reference.
+
+The fixtures hold FP64 films of 16 independent single-thread renders by the
+reference's own code (distinct seeds, 64 spp each; make_fixtures.py). The GPU
+renders the same scene text with its own counter-based RNG, so agreement is
+statistical: per pixel, z = (mean_gpu - mean_ref) / sqrt(se_gpu^2 + se_ref^2)
+with standard errors from the sample variances. Under the null hypothesis
+|z| > 4 is rare; the test allows 0.5% of pixels beyond it (heavy-tailed
+light paths) and requires the image means to agree within 4 standard errors.
+Reference samples that are not finite (the reference's GGX/Phong evaluation
+can divide 0 by 0) are left out pixel by pixel.
+"""
+import numpy as np
+import pytest
+
+import muon_gb300 as m
+from conftest import GOLDEN
+from muon_gb300 import native
+
+CASES = ["cornell", "cornell_nee_on", "cornell_nee_off", "feature_mix", "sphere_field"]
+GPU_SPP = 2048
+
+
+def reference_stats(fx):
+    sums, sqs = fx["sums"], fx["sum_sq"]
+    spp = int(fx["spp"])
+    finite = np.isfinite(sums).all(axis=-1) & np.isfinite(sqs).all(axis=-1)  # (runs, h, w)
+    runs = finite.sum(axis=0)
+    s = np.where(finite[..., None], sums, 0).sum(axis=0)
+    q = np.where(finite[..., None], sqs, 0).sum(axis=0)
+    n = (runs * spp)[..., None].astype(np.float64)
+    mean = s / np.maximum(n, 1)
+    var = np.maximum(q / np.maximum(n, 1) - mean * mean, 0) * n / np.maximum(n - 1, 1)
+    return mean, var / np.maximum(n, 1), runs
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", CASES)
+@pytest.mark.parametrize("mode", [native.ISECT_EXACT, native.ISECT_FAST])
+def test_path_tracer_converges_to_reference(lib, name, mode):
+    fx = np.load(f"{GOLDEN}/pt_{name}.npz")
+    scene = m.Scene.from_string(str(fx["scene"]))
+    film = scene.render(pixel_samples=GPU_SPP, seed=7, intersect_mode=mode)
+    assert np.isfinite(film.sum).all() and np.isfinite(film.sum_sq).all()
+    mean_g, se2_g = film.mean(), film.variance_of_mean()
+    mean_r, se2_r, runs = reference_stats(fx)
+    ok = runs >= 8
+    denom = np.sqrt(se2_g + se2_r)
+    z = np.where(denom > 0, (mean_g - mean_r) / np.where(denom > 0, denom, 1), 0.0)[ok]
+    frac = (np.abs(z) > 4).mean()
+    img_g, img_r = mean_g[ok].mean(), mean_r[ok].mean()
+    se_img = np.sqrt(se2_g[ok].sum() + se2_r[ok].sum()) / ok.sum()
+    rmse = np.sqrt(((mean_g - mean_r)[ok] ** 2).mean())
+    print(f"{name} mode {mode}: |z|>4 on {frac * 100:.3f}% of pixels, image mean gpu {img_g:.5f} ref {img_r:.5f} "
+          f"({(img_g - img_r) / se_img:+.2f} se), rmse {rmse:.5f}")
+    assert frac <= 0.005
+    assert abs(img_g - img_r) <= 4 * se_img
+
+
+@pytest.mark.gpu
+def test_render_is_deterministic_and_seeded(lib):
+    fx = np.load(f"{GOLDEN}/pt_cornell.npz")
+    scene = m.Scene.from_string(str(fx["scene"]))
+    a = scene.render(pixel_samples=16, seed=3)
+    b = scene.render(pixel_samples=16, seed=3)
+    c = scene.render(pixel_samples=16, seed=4)
+    assert np.array_equal(a.sum, b.sum) and np.array_equal(a.sum_sq, b.sum_sq)
+    assert not np.array_equal(a.sum, c.sum)
+
+
+@pytest.mark.gpu
+def test_wave_size_does_not_change_the_image(lib):
+    fx = np.load(f"{GOLDEN}/pt_cornell.npz")
+    scene = m.Scene.from_string(str(fx["scene"]))
+    a = scene.render(pixel_samples=32, seed=3, wave_paths=0)
+    b = scene.render(pixel_samples=32, seed=3, wave_paths=1000)
+    assert np.array_equal(a.count, b.count)
+    assert np.allclose(a.sum, b.sum, rtol=1e-12, atol=0)
+
+
+@pytest.mark.gpu
+def test_progressive_accumulation_matches_one_render(lib):
+    fx = np.load(f"{GOLDEN}/pt_cornell.npz")
+    scene = m.Scene.from_string(str(fx["scene"]))
+    full = scene.render(pixel_samples=32, seed=5)
+    h, w = full.height, full.width
+    acc = m.FilmResult(np.zeros((h, w, 3)), np.zeros((h, w, 3)), np.zeros((h, w), dtype=np.uint32))
+    f = acc._cfilm()
+    from muon_gb300.native import check, load
+    import ctypes as C
+    for off in (0, 16):
+        p = scene.params(pixel_samples=16, seed=5, sample_offset=off, flags=native.RENDER_ACCUMULATE)
+        check(load().muon_gpu_render(scene._h, C.byref(p), C.byref(f)))
+    assert np.array_equal(acc.count, full.count)
+    assert np.allclose(acc.sum, full.sum, rtol=1e-9, atol=1e-12)
+
+
+@pytest.mark.gpu
+def test_counted_rays_follow_the_reference_definition(lib):
+    """Primary rays = samples; secondary = MIS rays + continuation rays
+    (muon/integration.cc:34-38, 483); shadow rays are not counted as rays.
+    Per-sample counts match the reference's within sampling noise."""
+    fx = np.load(f"{GOLDEN}/pt_cornell.npz")
+    scene = m.Scene.from_string(str(fx["scene"]))
+    scene.render(pixel_samples=256, seed=1)
+    st = scene.stats()
+    h, w = scene.height, scene.width
+    assert st["primary_rays"] == h * w * 256
+    ref = fx["counters"].astype(np.float64)  # runs x (primary, secondary, object tests, bounds tests)
+    ref_ratio = ref[:, 1].sum() / ref[:, 0].sum()
+    gpu_ratio = st["secondary_rays"] / st["primary_rays"]
+    print(f"secondary per primary: gpu {gpu_ratio:.4f} reference {ref_ratio:.4f}")
+    assert abs(gpu_ratio - ref_ratio) <= 0.01 * ref_ratio

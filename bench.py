@@ -1,0 +1,334 @@
+"""Benchmark: path-traced Mrays/s on the random sphere field.
+
+Workload (one step = one full frame): 512 seeded spheres (centres U[-10,10]^3,
+radii U[0.2,1]), Lambertian / Phong / GGX materials, ground quad, one 2x2
+quad light of emission 10; 512x512 pixels, 64 samples per pixel, max depth 8,
+next-event estimation with MIS, BRDF importance sampling, FP32 shading, FP64
+film. Synthetic and seeded (muon_gb300.scenes.sphere_field).
+
+Metric: Mrays/s counted as the reference counts rays (primary + secondary,
+the MIS-sampled ray included; shadow rays excluded, muon/integration.cc:34-38,
+483), over device time with the scene resident and the film in device memory.
+`e2e` is the same metric through the public API with host buffers: scene
+upload (BVH build + copy) and the host film read-back inside every step.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+With N > 1 (torchrun), every rank renders its own replica of the frame with a
+distinct seed (weak scaling; the FP64 films of replicas merge by addition).
+`--impl reference` times the reference algorithm on the host cores: the
+reference build when it runs on this machine, else the oracle's restatement.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOAD = {"workload": "sphere_field", "spheres": 512, "width": 512, "height": 512, "spp": 64, "max_depth": 8,
+            "nee": "mis", "importance_sampling": "brdf", "seed": 1}
+METRIC = "Mrays/s"
+
+
+def scene_text() -> str:
+    from muon_gb300 import scenes
+
+    w = WORKLOAD
+    return scenes.sphere_field(w["width"], w["height"], w["spp"], w["max_depth"], w["spheres"], w["seed"], w["nee"])
+
+
+def peaks() -> dict:
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return {"hbm_gbs": d["hbm_gbs"], "source": "measured"}
+    return {"hbm_gbs": 6800.0, "source": "fallback"}
+
+
+class ClockSampler:
+    """Samples SM clocks and throttle reasons with nvidia-smi while running."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.samples: list[list[str]] = []
+        self._stop = threading.Event()
+        self._t = threading.Thread(target=self._run, daemon=True)
+
+    def _run(self):
+        while not self._stop.is_set():
+            try:
+                out = subprocess.run(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                                      "--format=csv,noheader,nounits"], capture_output=True, text=True, timeout=5)
+                if out.returncode == 0:
+                    self.samples.append([x.strip() for x in out.stdout.strip().split(",")])
+            except Exception:
+                pass
+            self._stop.wait(0.2)
+
+    def __enter__(self):
+        self._t.start()
+        return self
+
+    def __exit__(self, *a):
+        self._stop.set()
+        self._t.join(timeout=10)
+
+    def summary(self) -> dict:
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for s in self.samples for k in range(4) if len(s) > 2 + k and s[2 + k] == "Active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.samples)}
+
+
+def algorithmic_bytes(st: dict, slots: int) -> dict:
+    """Bytes each kernel class must move per frame by its algorithm.
+
+    Traversal (extend / occlude): 64 B per BVH node visited (two child boxes
+    and links; box tests count 2 per node), 64 B per primitive record tested,
+    plus the ray/hit records: extend reads a 32 B ray and writes an 8 B hit;
+    occlude reads a 4 B queue entry, a 16 B origin and a 16 B direction.
+    Shade, per shaded path: reads ray 32 + hit 8 + radiance 16 + throughput 16
+    + previous slots 16*S, writes radiance 16 + slots 32*S (value and
+    direction); per continuation +48 (ray 32, throughput 16); per shadow ray +4.
+    """
+    ext = 32 * st["extend_box_tests"] + 64 * st["extend_prim_tests"] + 40 * st["extend_rays"]
+    occ = 32 * st["occlude_box_tests"] + 64 * st["occlude_prim_tests"] + 36 * st["occlude_rays"]
+    shaded = st["extend_rays"]
+    cont = max(0, st["extend_rays"] - st["primary_rays"])
+    shade = shaded * (88 + 48 * slots) + 48 * cont + 4 * st["shadow_rays"]
+    return {"extend": ext, "occlude": occ, "shade": shade}
+
+
+def run_ours(args) -> None:
+    import torch
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    else:
+        torch.cuda.set_device(0)
+
+    from muon_gb300 import build as native_build
+
+    native_build.build()
+    import muon_gb300 as m
+    from muon_gb300 import native
+
+    text = scene_text()
+    scene = m.Scene.from_string(text)
+    seed = 1000 + rank
+    params = scene.params(seed=seed, intersect_mode=native.ISECT_EXACT)
+    h, w = scene.height, scene.width
+    d_sum = torch.zeros((h, w, 3), dtype=torch.float64, device="cuda")
+    d_sq = torch.zeros((h, w, 3), dtype=torch.float64, device="cuda")
+    d_cnt = torch.zeros((h, w), dtype=torch.int32, device="cuda")
+    render = lambda p: scene.render_device(p, d_sum.data_ptr(), d_sq.data_ptr(), d_cnt.data_ptr())
+
+    # traversal work per frame (stats kernels), outside the timed region
+    cal = scene.params(seed=seed, intersect_mode=native.ISECT_EXACT, flags=native.RENDER_STATS)
+    render(cal)
+    cal_stats = scene.stats()
+    slots = 2  # one area light sample + the MIS ray per path vertex
+
+    stream = torch.cuda.ExternalStream(scene.stream())
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")  # 256 MiB > 129 MB L2
+    for _ in range(args.warmup):
+        render(params)
+    torch.cuda.synchronize()
+
+    per_step, st_steps = [], []
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clocks:
+        t0 = time.perf_counter()
+        for k in range(args.steps):
+            flush.zero_()
+            stream.wait_stream(torch.cuda.current_stream())
+            ev[k][0].record(stream)
+            render(params)
+            ev[k][1].record(stream)
+            st_steps.append(scene.stats())
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+        wall = time.perf_counter() - t0
+    per_step = [a.elapsed_time(b) for a, b in ev]
+    dev_ms = sum(per_step)
+    counted = sum(s["primary_rays"] + s["secondary_rays"] for s in st_steps)
+    launches = sum(s["kernel_launches"] for s in st_steps)
+
+    t = torch.tensor([dev_ms, float(counted)], dtype=torch.float64, device="cuda")
+    if world > 1:
+        tmax = t.clone()
+        torch.distributed.all_reduce(tmax, op=torch.distributed.ReduceOp.MAX)
+        tsum = t.clone()
+        torch.distributed.all_reduce(tsum, op=torch.distributed.ReduceOp.SUM)
+        dev_ms_max, counted_all = float(tmax[0]), float(tsum[1])
+    else:
+        dev_ms_max, counted_all = dev_ms, float(counted)
+    value = counted_all / (dev_ms_max * 1e3)
+
+    # end to end through the public API with host buffers
+    e2e_steps = max(2, min(args.steps, 5))
+    parsed = m.parse_string(text)
+    desc_bytes = (parsed.desc.num_triangles * 80 + parsed.desc.num_spheres * 32 + parsed.desc.num_materials * 56 +
+                  parsed.desc.num_lights * 52 + parsed.desc.num_transforms * 192)
+    film_bytes = h * w * (3 * 8 * 2 + 4)
+    m.Scene(parsed).render(params)  # warm
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    e2e_counted = 0
+    for _ in range(e2e_steps):
+        sc = m.Scene(parsed)
+        sc.render(params)
+        st = sc.stats()
+        e2e_counted += st["primary_rays"] + st["secondary_rays"]
+        sc.close()
+    e2e_s = time.perf_counter() - t0
+    e2e_value = e2e_counted / e2e_s / 1e6
+
+    if rank != 0:
+        return
+
+    # roofline of the dominant kernel class
+    last = st_steps[-1]
+    alg = algorithmic_bytes(cal_stats, slots)
+    times = {"extend": last["extend_ms"], "occlude": last["occlude_ms"], "shade": last["shade_ms"]}
+    dom = max(times, key=times.get)
+    n_launch = {"extend": last["extend_launches"], "occlude": last["occlude_launches"],
+                "shade": last["extend_launches"]}[dom]
+    per_launch_bytes = alg[dom] / max(1, n_launch)
+    per_launch_ms = times[dom] / max(1, n_launch)
+    pk = peaks()
+    achieved = per_launch_bytes / (per_launch_ms * 1e-3) / 1e9
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(tpath):
+        traffic = json.load(open(tpath)).get(dom)
+
+    cpu = cpu_baseline(text) if world == 1 else None
+    line = {
+        "metric": METRIC, "value": round(value, 2), "unit": METRIC, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(dev_ms_max / args.steps, 4), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded sphere field)",
+        "config": dict(WORKLOAD, parallelism=f"replicas{world}", intersect_mode="exact",
+                       l2="flushed between steps (256 MiB write)", counted_rays_per_step=counted // args.steps),
+        "e2e": {"value": round(e2e_value, 2), "unit": METRIC, "h2d_bytes_per_step": int(desc_bytes),
+                "d2h_bytes_per_step": int(film_bytes),
+                "note": "scene upload (BVH build + copy) + render + host film read-back per step"},
+        "gpu_launches": int(launches),
+        "roofline": {"kernel": dom, "bound": "hbm", "achieved": round(achieved, 1), "peak": pk["hbm_gbs"],
+                     "unit": "GB/s", "frac": round(achieved / pk["hbm_gbs"], 4), "traffic": traffic,
+                     "peak_source": pk["source"], "per_launch_bytes": int(per_launch_bytes),
+                     "per_launch_ms": round(per_launch_ms, 4), "kernel_ms_per_step": {k: round(v, 3) for k, v in times.items()}},
+        "clocks": clocks.summary(),
+        "wall_s": round(wall, 3),
+    }
+    if cpu:
+        line["cpu_baseline"] = cpu
+    print(json.dumps(line), flush=True)
+
+
+def _reference_binary() -> str | None:
+    """The reference build (oracle/_ref) when it exists and runs here."""
+    exe = os.path.join(ROOT, "oracle", "_ref", "muon_ref")
+    if not os.path.exists(exe):
+        return None
+    try:
+        r = subprocess.run([exe, "--help"], capture_output=True, timeout=10)
+        return exe if r.returncode in (0, 1) else None
+    except Exception:
+        return None
+
+
+def reference_rate(text: str, spp: int, threads: int) -> tuple[float, float, str]:
+    """Counted Mrays/s of the reference algorithm on `threads` host threads for
+    the workload at `spp` samples per pixel; returns (rate, seconds, kind)."""
+    from oracle import port
+
+    t0 = time.perf_counter()
+    f = port.render(text, spp=spp, seed=1, threads=threads)
+    el = time.perf_counter() - t0
+    counted = f.counters["primary"] + f.counters["secondary"]
+    return counted / el / 1e6, el, "port"
+
+
+def cpu_baseline(text: str) -> dict:
+    threads = os.cpu_count() or 1
+    rate1, el1, kind = reference_rate(text, 1, threads)
+    spp = max(1, min(64, int(10.0 / max(el1, 1e-3))))
+    rate, el, kind = reference_rate(text, spp, threads)
+    return {"value": round(rate, 3), "unit": METRIC, "cores": threads, "kind": kind,
+            "sample": f"full 512x512 frame at {spp} spp (of 64), {el:.1f} s on {threads} threads"}
+
+
+def run_reference(args) -> None:
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    if rank != 0:
+        return
+    from oracle import build as oracle_build
+
+    oracle_build.build()
+    text = scene_text()
+    threads = os.cpu_count() or 1
+    rate1, el1, kind = reference_rate(text, 1, threads)
+    spp = max(1, min(64, int(5.0 / max(el1, 1e-3))))
+    for _ in range(args.warmup):
+        reference_rate(text, 1, threads)
+    rates, times = [], []
+    for _ in range(args.steps):
+        r, el, kind = reference_rate(text, spp, threads)
+        rates.append(r)
+        times.append(el)
+    value = sum(rates) / len(rates)
+    line = {"metric": METRIC, "value": round(value, 3), "unit": METRIC, "impl": "reference", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * sum(times) / len(times), 1),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded sphere field)",
+            "config": dict(WORKLOAD, parallelism=f"host threads {threads}"),
+            "cpu_baseline": {"value": round(value, 3), "unit": METRIC, "cores": threads, "kind": kind,
+                             "sample": f"full 512x512 frame at {spp} spp (of 64) per step"},
+            "e2e": {"value": round(value, 3), "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    a = ap.parse_args()
+    if a.warmup < 3:
+        a.warmup = 3
+    if a.impl == "reference":
+        run_reference(a)
+    else:
+        run_ours(a)
+
+
+if __name__ == "__main__":
+    main()

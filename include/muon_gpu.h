@@ -226,6 +226,17 @@ typedef struct MuonStats {
   uint64_t kernel_launches;
   uint64_t bvh_nodes;
   uint64_t primitives;
+  /* traversal work split by kernel class, for roofline accounting; the test
+   * counts are filled only with MUON_RENDER_STATS (box tests count the two
+   * child boxes of every node visited) */
+  uint64_t extend_rays;
+  uint64_t extend_launches;
+  uint64_t extend_box_tests;
+  uint64_t extend_prim_tests;
+  uint64_t occlude_rays;
+  uint64_t occlude_launches;
+  uint64_t occlude_box_tests;
+  uint64_t occlude_prim_tests;
 } MuonStats;
 
 /* ---- host side: scene files (muon/parser.{h,cc}) ---------------------- */
@@ -281,6 +292,10 @@ int muon_gpu_occluded(MuonScene *scene, const MuonRay *rays, const float *max_di
 
 /* Counters and device timings of the last render (muon/stats.h:11-44). */
 int muon_gpu_stats(const MuonScene *scene, MuonStats *stats);
+
+/* The CUDA stream (cudaStream_t) all of this scene's work is launched on, for
+ * callers that time or order work around it with CUDA events. */
+int muon_gpu_scene_stream(const MuonScene *scene, void **stream);
 
 /* Thread-local description of the last failure on this thread. */
 const char *muon_gpu_last_error(void);

@@ -208,6 +208,12 @@ class Scene:
         check(load().muon_gpu_stats(self._h, C.byref(s)))
         return {name: getattr(s, name) for name, _ in native.Stats._fields_}
 
+    def stream(self) -> int:
+        """The cudaStream_t this scene launches on, as an integer handle."""
+        v = C.c_void_p()
+        check(load().muon_gpu_scene_stream(self._h, C.byref(v)))
+        return v.value or 0
+
     def close(self) -> None:
         if getattr(self, "_h", None):
             load().muon_gpu_scene_destroy(self._h)

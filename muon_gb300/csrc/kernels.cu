@@ -253,10 +253,10 @@ __global__ void __launch_bounds__(kBlock) OccludeKernel(DevScene s, const uint32
     if (h >= 0) contrib[slot] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
   }
   if (kStats) {
-    AddStat(stats, kStatBoxTests, c.box_tests);
-    AddStat(stats, kStatBoxHits, c.box_hits);
-    AddStat(stats, kStatPrimTests, c.prim_tests);
-    AddStat(stats, kStatPrimHits, c.prim_hits);
+    AddStat(stats, kStatOccBoxTests, c.box_tests);
+    AddStat(stats, kStatOccBoxHits, c.box_hits);
+    AddStat(stats, kStatOccPrimTests, c.prim_tests);
+    AddStat(stats, kStatOccPrimHits, c.prim_hits);
   }
   if (overflow) atomicAdd(stats + kStatOverflow, 1ull);
 }

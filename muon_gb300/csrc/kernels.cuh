@@ -22,6 +22,10 @@ enum Stat : int {
   kStatPrimTests,
   kStatPrimHits,
   kStatOverflow,
+  kStatOccBoxTests,
+  kStatOccBoxHits,
+  kStatOccPrimTests,
+  kStatOccPrimHits,
   kNumStats
 };
 

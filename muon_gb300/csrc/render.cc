@@ -259,7 +259,7 @@ void RenderDevice(MuonScene *sc, const MuonRenderParams &p, double *d_sum, doubl
 
   cudaEvent_t t0 = sc->NextEvent(2)->a, t1 = sc->events[0].b;
   CUDA_TRY(cudaEventRecord(t0, st));
-  uint64_t primary = 0, shadow = 0, launches = 0;
+  uint64_t primary = 0, shadow = 0, launches = 0, ext_rays = 0, ext_launches = 0, occ_launches = 0;
   const bool traces = !(p.max_depth >= 0 && sp.max_trace_depth < 0);
   for (int64_t p0 = 0; p0 < npix_total; p0 += pix_per_wave) {
     const int npix = static_cast<int>(std::min<int64_t>(pix_per_wave, npix_total - p0));
@@ -284,6 +284,8 @@ void RenderDevice(MuonScene *sc, const MuonRenderParams &p, double *d_sum, doubl
           LaunchExtend(sc->dev, b, buf, n_cur, p.intersect_mode, stats_on, st);
           if (ev) CUDA_TRY(cudaEventRecord(ev->b, st));
           ++launches;
+          ++ext_launches;
+          ext_rays += static_cast<uint64_t>(n_cur);
           if (!pt) {
             LaunchShadeDebug(sc->dev, w, b, p.integrator, n_cur, p.intersect_mode, st);
             ++launches;
@@ -303,6 +305,7 @@ void RenderDevice(MuonScene *sc, const MuonRenderParams &p, double *d_sum, doubl
             LaunchOcclude(sc->dev, b, slots, n_sh, p.intersect_mode, stats_on, st);
             if (eo) CUDA_TRY(cudaEventRecord(eo->b, st));
             ++launches;
+            ++occ_launches;
           }
           shadow += static_cast<uint64_t>(n_sh);
           n_cur = n_next;
@@ -323,10 +326,18 @@ void RenderDevice(MuonScene *sc, const MuonRenderParams &p, double *d_sum, doubl
   o.primary_rays = primary;
   o.secondary_rays = hstats[kStatSecondary];
   o.shadow_rays = shadow;
-  o.bounds_tests = hstats[kStatBoxTests];
-  o.bounds_hits = hstats[kStatBoxHits];
-  o.object_tests = hstats[kStatPrimTests];
-  o.object_hits = hstats[kStatPrimHits];
+  o.bounds_tests = hstats[kStatBoxTests] + hstats[kStatOccBoxTests];
+  o.bounds_hits = hstats[kStatBoxHits] + hstats[kStatOccBoxHits];
+  o.object_tests = hstats[kStatPrimTests] + hstats[kStatOccPrimTests];
+  o.object_hits = hstats[kStatPrimHits] + hstats[kStatOccPrimHits];
+  o.extend_rays = ext_rays;
+  o.extend_launches = ext_launches;
+  o.extend_box_tests = hstats[kStatBoxTests];
+  o.extend_prim_tests = hstats[kStatPrimTests];
+  o.occlude_rays = shadow;
+  o.occlude_launches = occ_launches;
+  o.occlude_box_tests = hstats[kStatOccBoxTests];
+  o.occlude_prim_tests = hstats[kStatOccPrimTests];
   o.paths = static_cast<uint64_t>(npix_total) * spp;
   o.kernel_launches = launches;
   o.bvh_nodes = static_cast<uint64_t>(sc->img.nodes.size());
@@ -548,6 +559,12 @@ int muon_gpu_occluded(MuonScene *scene, const MuonRay *rays, const float *max_di
 int muon_gpu_stats(const MuonScene *scene, MuonStats *stats) {
   if (!scene || !stats) return Fail(MUON_ERR_INVALID_ARG, "null argument");
   *stats = scene->last;
+  return MUON_OK;
+}
+
+int muon_gpu_scene_stream(const MuonScene *scene, void **stream) {
+  if (!scene || !stream) return Fail(MUON_ERR_INVALID_ARG, "null argument");
+  *stream = static_cast<void *>(scene->stream);
   return MUON_OK;
 }
 

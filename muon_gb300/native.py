@@ -95,7 +95,10 @@ class Stats(C.Structure):
                 ("object_tests", C.c_uint64), ("object_hits", C.c_uint64), ("bounds_tests", C.c_uint64),
                 ("bounds_hits", C.c_uint64), ("paths", C.c_uint64), ("render_ms", C.c_double),
                 ("extend_ms", C.c_double), ("occlude_ms", C.c_double), ("shade_ms", C.c_double),
-                ("kernel_launches", C.c_uint64), ("bvh_nodes", C.c_uint64), ("primitives", C.c_uint64)]
+                ("kernel_launches", C.c_uint64), ("bvh_nodes", C.c_uint64), ("primitives", C.c_uint64),
+                ("extend_rays", C.c_uint64), ("extend_launches", C.c_uint64), ("extend_box_tests", C.c_uint64),
+                ("extend_prim_tests", C.c_uint64), ("occlude_rays", C.c_uint64), ("occlude_launches", C.c_uint64),
+                ("occlude_box_tests", C.c_uint64), ("occlude_prim_tests", C.c_uint64)]
 
 
 # Every entry point declared in include/muon_gpu.h: name -> (restype, argtypes)
@@ -118,6 +121,7 @@ SIGNATURES = {
     "muon_gpu_occluded": (C.c_int, [C.c_void_p, C.POINTER(Ray), C.POINTER(C.c_float), C.c_int64, C.c_int32,
                                     C.POINTER(C.c_uint8)]),
     "muon_gpu_stats": (C.c_int, [C.c_void_p, C.POINTER(Stats)]),
+    "muon_gpu_scene_stream": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p)]),
     "muon_gpu_last_error": (C.c_char_p, []),
 }
 

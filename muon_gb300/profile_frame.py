@@ -1,0 +1,40 @@
+"""Renders a benchmark frame a few times, for profilers.
+
+    python -m muon_gb300.profile_frame [--workload sphere_field] [--frames 1]
+        [--warmup 2] [--mode exact|fast] [--width 512 --height 512 --spp 64]
+
+Used as the target of the ncu captures summarised in profiles/: the same
+workload as bench.py, without its timing, e2e and CPU-baseline parts.
+"""
+from __future__ import annotations
+
+import argparse
+
+from . import Scene, native, scenes
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--workload", default="sphere_field", choices=sorted(scenes.WORKLOADS))
+    ap.add_argument("--frames", type=int, default=1)
+    ap.add_argument("--warmup", type=int, default=2)
+    ap.add_argument("--mode", default="exact", choices=["exact", "fast", "watertight"])
+    ap.add_argument("--width", type=int, default=512)
+    ap.add_argument("--height", type=int, default=512)
+    ap.add_argument("--spp", type=int, default=64)
+    a = ap.parse_args()
+    text = scenes.WORKLOADS[a.workload](width=a.width, height=a.height, spp=a.spp)
+    scene = Scene.from_string(text)
+    mode = {"exact": native.ISECT_EXACT, "fast": native.ISECT_FAST, "watertight": native.ISECT_WATERTIGHT}[a.mode]
+    for _ in range(a.warmup):
+        scene.render(intersect_mode=mode)
+    for _ in range(a.frames):
+        scene.render(intersect_mode=mode)
+    st = scene.stats()
+    print(f"{a.workload} {a.width}x{a.height}x{a.spp}: {st['render_ms']:.3f} ms, "
+          f"{st['kernel_launches']} launches, counted rays {st['primary_rays'] + st['secondary_rays']}")
+    scene.close()
+
+
+if __name__ == "__main__":
+    main()

@@ -42,11 +42,11 @@ HIT_SCENES = {
 
 # (scene text, runs, spp per run)
 PT_SCENES = {
-    "cornell": (lambda: scenes.cornell(48, 48, 64, 5, 1, "pathtracer"), 16, 64),
-    "feature_mix": (lambda: scenes.feature_mix(48, 48, 64, "pathtracer", "mis", 5), 16, 64),
-    "sphere_field": (lambda: scenes.sphere_field(48, 48, 64, 8), 16, 64),
-    "cornell_nee_on": (lambda: scenes.cornell(48, 48, 64, 5, 1, "pathtracer", "on"), 16, 64),
-    "cornell_nee_off": (lambda: scenes.cornell(48, 48, 64, 5, 1, "pathtracer", "off"), 16, 64),
+    "cornell": (lambda: scenes.cornell(32, 32, 64, 5, 1, "pathtracer"), 32, 1024),
+    "feature_mix": (lambda: scenes.feature_mix(32, 32, 64, "pathtracer", "mis", 5), 32, 1024),
+    "sphere_field": (lambda: scenes.sphere_field(32, 32, 64, 8), 32, 512),
+    "cornell_nee_on": (lambda: scenes.cornell(32, 32, 64, 5, 1, "pathtracer", "on"), 32, 1024),
+    "cornell_nee_off": (lambda: scenes.cornell(32, 32, 64, 5, 1, "pathtracer", "off"), 32, 1024),
 }
 
 

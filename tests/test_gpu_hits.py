@@ -102,6 +102,7 @@ def test_debug_integrators_are_bitwise_equal(lib, name, integrator):
         ref = np.where(hit[:, None], fx["albedo"], f(0))
     else:
         ref = np.where(hit[:, None], f(1) / (f(1) + fx["distance"][:, None]), f(0))
+        ref = np.repeat(ref, 3, axis=1)
     _, pid, _, _ = scene.intersect(fx["rays"][:, :3], fx["rays"][:, 3:], native.ISECT_EXACT)
     same = pid == ref_ids(fx)
     assert np.array_equal(got[same], ref[same].astype(np.float32))

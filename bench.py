@@ -102,16 +102,18 @@ def algorithmic_bytes(st: dict, slots: int) -> dict:
     and links; box tests count 2 per node), 64 B per primitive record tested,
     plus the ray/hit records: extend reads a 32 B ray and writes an 8 B hit;
     occlude reads a 4 B queue entry, a 16 B origin and a 16 B direction.
-    Shade, per shaded path: reads ray 32 + hit 8 + radiance 16 + throughput 16
-    + previous slots 16*S, writes radiance 16 + slots 32*S (value and
+    Shade, per shaded path: reads ray 32 + hit 8 + radiance 16 + throughput 16,
+    writes radiance 16 + link 4 (counted in fold) + slots 48*S (clear, value,
     direction); per continuation +48 (ray 32, throughput 16); per shadow ray +4.
+    Fold, per shaded path: reads radiance 16 + slots 16*S + link 4, writes 16.
     """
     ext = 32 * st["extend_box_tests"] + 64 * st["extend_prim_tests"] + 40 * st["extend_rays"]
     occ = 32 * st["occlude_box_tests"] + 64 * st["occlude_prim_tests"] + 36 * st["occlude_rays"]
     shaded = st["extend_rays"]
     cont = max(0, st["extend_rays"] - st["primary_rays"])
     shade = shaded * (88 + 48 * slots) + 48 * cont + 4 * st["shadow_rays"]
-    return {"extend": ext, "occlude": occ, "shade": shade}
+    fold = shaded * (16 + 16 * slots + 4 + 16)
+    return {"extend": ext, "occlude": occ, "shade": shade, "fold": fold}
 
 
 def run_ours(args) -> None:
@@ -137,7 +139,9 @@ def run_ours(args) -> None:
     text = scene_text()
     scene = m.Scene.from_string(text)
     seed = 1000 + rank
-    params = scene.params(seed=seed, intersect_mode=native.ISECT_EXACT)
+    # Every kernel is timed with CUDA events inside the frame's graph; the
+    # frame time below includes that cost.
+    params = scene.params(seed=seed, intersect_mode=native.ISECT_EXACT, flags=native.RENDER_TIMING)
     h, w = scene.height, scene.width
     d_sum = torch.zeros((h, w, 3), dtype=torch.float64, device="cuda")
     d_sq = torch.zeros((h, w, 3), dtype=torch.float64, device="cuda")
@@ -215,10 +219,11 @@ def run_ours(args) -> None:
     # roofline of the dominant kernel class
     last = st_steps[-1]
     alg = algorithmic_bytes(cal_stats, slots)
-    times = {"extend": last["extend_ms"], "occlude": last["occlude_ms"], "shade": last["shade_ms"]}
+    times = {"extend": last["extend_ms"], "occlude": last["occlude_ms"], "shade": last["shade_ms"],
+             "fold": last["fold_ms"]}
     dom = max(times, key=times.get)
     n_launch = {"extend": last["extend_launches"], "occlude": last["occlude_launches"],
-                "shade": last["extend_launches"]}[dom]
+                "shade": last["extend_launches"], "fold": last["extend_launches"]}[dom]
     per_launch_bytes = alg[dom] / max(1, n_launch)
     per_launch_ms = times[dom] / max(1, n_launch)
     pk = peaks()
@@ -318,7 +323,7 @@ def run_reference(args) -> None:
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=60)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     a = ap.parse_args()

@@ -91,6 +91,8 @@ extern "C" {
 /* render flags */
 #define MUON_RENDER_STATS 1u      /* count bounds/object tests (slower)        */
 #define MUON_RENDER_ACCUMULATE 2u /* add into the caller's film, do not zero   */
+#define MUON_RENDER_TIMING 4u     /* time every kernel with CUDA events        */
+#define MUON_RENDER_NO_GRAPH 8u   /* launch kernel by kernel, no CUDA graph    */
 
 /* ---- scene description (flattened muon::Scene, muon/scene.h:22-95) ---- */
 typedef struct MuonTransformDesc {
@@ -220,9 +222,10 @@ typedef struct MuonStats {
   uint64_t bounds_hits;
   uint64_t paths;
   double render_ms;      /* device time of the last render               */
-  double extend_ms;      /* closest-hit traversal kernels               */
-  double occlude_ms;     /* any-hit traversal kernels                   */
-  double shade_ms;       /* camera, shading and film kernels            */
+  double extend_ms;      /* closest-hit traversal kernels (MUON_RENDER_TIMING) */
+  double occlude_ms;     /* any-hit traversal kernels (MUON_RENDER_TIMING)     */
+  double shade_ms;       /* shading kernels (MUON_RENDER_TIMING)               */
+  double fold_ms;        /* radiance fold kernels (MUON_RENDER_TIMING)         */
   uint64_t kernel_launches;
   uint64_t bvh_nodes;
   uint64_t primitives;

@@ -16,6 +16,7 @@
 // reserves the block's range with a single atomicAdd.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <type_traits>
 
 #include "dev_shade.cuh"
@@ -179,11 +180,19 @@ __device__ __forceinline__ Rng MakeRng(const WaveInfo &w, int path, uint32_t bou
   return r;
 }
 
+
+// Device-counted loops: `bound` (a host-known upper bound of the queue) sizes
+// the grid, the true length is read on the device, and blocks stride over it.
+#define QUEUE_LOOP(j, n)                                                                     \
+  for (int j##_base = blockIdx.x * kBlock; j##_base < (n); j##_base += gridDim.x * kBlock)
+
 // ---- camera ------------------------------------------------------------
 // Sampler::NextSample (muon/sampling.cc:80-121): sample 0 at the pixel centre,
-// later samples jittered uniformly inside the pixel.
-__global__ void __launch_bounds__(kBlock) CameraKernel(DevCamera cam, WaveInfo w, PathBuffers b, int slots) {
+// later samples jittered uniformly inside the pixel. Fills bounce 0's queue in
+// path order and clears each path's final radiance.
+__global__ void __launch_bounds__(kBlock) CameraKernel(DevCamera cam, WaveInfo w, PathBuffers b, WaveCounters wc) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i == 0) *wc.count(0) = static_cast<uint32_t>(w.n);
   if (i >= w.n) return;
   int pixel = w.p0 + i / w.ns;
   uint32_t sample = w.sample_offset + static_cast<uint32_t>(w.s0 + i % w.ns);
@@ -206,312 +215,321 @@ __global__ void __launch_bounds__(kBlock) CameraKernel(DevCamera cam, WaveInfo w
   CastRay(cam, x, y, &o, &d);
   b.ray_o[0][i] = make_float4(o.x, o.y, o.z, __int_as_float(i));
   b.ray_d[0][i] = make_float4(d.x, d.y, d.z, INFINITY);
-  b.tp[i] = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
-  b.rad[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-  for (int k = 0; k < slots; ++k) b.contrib[static_cast<int64_t>(i) * slots + k] = make_float4(0, 0, 0, 0);
+  b.tp[0][i] = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
+  b.rad[0][i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+  b.final_rad[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
 }
 
 // ---- extend / occlude ------------------------------------------------------
 template <bool kStats, int kTri>
-__global__ void __launch_bounds__(kBlock) ExtendKernel(DevScene s, const float4 *__restrict__ ray_o,
-                                                       const float4 *__restrict__ ray_d, int n, int2 *hits,
-                                                       unsigned long long *stats) {
-  int j = blockIdx.x * blockDim.x + threadIdx.x;
+__global__ void __launch_bounds__(kBlock) ExtendKernel(DevScene s, PathBuffers b, WaveCounters wc, int bounce) {
+  const int n = static_cast<int>(*wc.count(bounce));
+  const float4 *__restrict__ ray_o = b.ray_o[bounce & 1];
+  const float4 *__restrict__ ray_d = b.ray_d[bounce & 1];
   TraceCounters c;
   bool overflow = false;
-  if (j < n) {
+  for (int j = blockIdx.x * kBlock + threadIdx.x; j < n; j += gridDim.x * kBlock) {
     float4 o4 = ray_o[j], d4 = ray_d[j];
     float t, t_obj = 0.0f;
     int h = Trace<false, kStats, kTri>(s, f3(o4.x, o4.y, o4.z), f3(d4.x, d4.y, d4.z), d4.w, &t, &c, &overflow,
                                        &t_obj);
-    hits[j] = make_int2(__float_as_int(kTri == MUON_ISECT_EXACT ? t_obj : t), h);
+    b.hits[j] = make_int2(__float_as_int(kTri == MUON_ISECT_EXACT ? t_obj : t), h);
   }
   if (kStats) {
-    AddStat(stats, kStatBoxTests, c.box_tests);
-    AddStat(stats, kStatBoxHits, c.box_hits);
-    AddStat(stats, kStatPrimTests, c.prim_tests);
-    AddStat(stats, kStatPrimHits, c.prim_hits);
+    AddStat(b.stats, kStatBoxTests, c.box_tests);
+    AddStat(b.stats, kStatBoxHits, c.box_hits);
+    AddStat(b.stats, kStatPrimTests, c.prim_tests);
+    AddStat(b.stats, kStatPrimHits, c.prim_hits);
   }
-  if (overflow) atomicAdd(stats + kStatOverflow, 1ull);
+  if (overflow) atomicAdd(b.stats + kStatOverflow, 1ull);
 }
 
-// Shadow queue entries are slot indices; slot k of path p is p * S + k. A
-// blocked slot's contribution is zeroed.
+// Shadow queue entries are slot indices (entry * S + slot). A blocked slot's
+// contribution is zeroed.
 template <bool kStats, int kTri>
-__global__ void __launch_bounds__(kBlock) OccludeKernel(DevScene s, const uint32_t *__restrict__ shq, int slots,
-                                                        int n, const float4 *__restrict__ org,
-                                                        const float4 *__restrict__ slot_dir, float4 *contrib,
-                                                        unsigned long long *stats) {
-  int j = blockIdx.x * blockDim.x + threadIdx.x;
+__global__ void __launch_bounds__(kBlock) OccludeKernel(DevScene s, PathBuffers b, WaveCounters wc, int bounce,
+                                                        int slots) {
+  const int n = static_cast<int>(*wc.shadow(bounce));
   TraceCounters c;
   bool overflow = false;
-  if (j < n) {
-    uint32_t slot = shq[j];
-    float4 o4 = org[slot / slots], d4 = slot_dir[slot];
+  for (int j = blockIdx.x * kBlock + threadIdx.x; j < n; j += gridDim.x * kBlock) {
+    uint32_t slot = b.shq[j];
+    float4 o4 = b.org[slot / slots], d4 = b.slot_dir[slot];
     float t;
     int h = Trace<true, kStats, kTri>(s, f3(o4.x, o4.y, o4.z), f3(d4.x, d4.y, d4.z), d4.w, &t, &c, &overflow);
-    if (h >= 0) contrib[slot] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    if (h >= 0) b.contrib[slot] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
   }
   if (kStats) {
-    AddStat(stats, kStatOccBoxTests, c.box_tests);
-    AddStat(stats, kStatOccBoxHits, c.box_hits);
-    AddStat(stats, kStatOccPrimTests, c.prim_tests);
-    AddStat(stats, kStatOccPrimHits, c.prim_hits);
+    AddStat(b.stats, kStatOccBoxTests, c.box_tests);
+    AddStat(b.stats, kStatOccBoxHits, c.box_hits);
+    AddStat(b.stats, kStatOccPrimTests, c.prim_tests);
+    AddStat(b.stats, kStatOccPrimHits, c.prim_hits);
   }
-  if (overflow) atomicAdd(stats + kStatOverflow, 1ull);
+  if (overflow) atomicAdd(b.stats + kStatOverflow, 1ull);
 }
 
 // ---- deterministic integrators --------------------------------------------
 // NormalsTracer / AlbedoTracer / DepthTracer (muon/integration.cc:47-72).
 template <int kMode>
-__global__ void __launch_bounds__(kBlock) ShadeDebugKernel(DevScene s, PathBuffers b, int integrator, int n) {
-  int j = blockIdx.x * blockDim.x + threadIdx.x;
-  if (j >= n) return;
-  float4 o4 = b.ray_o[0][j], d4 = b.ray_d[0][j];
-  int path = __float_as_int(o4.w);
-  int2 h = b.hits[j];
-  float4 out = make_float4(0, 0, 0, 0);
-  if (h.y >= 0) {
-    float3 p, nrm;
-    float dist;
-    int mat, light, pid;
-    Surface<kMode>(s, h.y, f3(o4.x, o4.y, o4.z), f3(d4.x, d4.y, d4.z), __int_as_float(h.x), &p, &nrm, &dist, &mat,
-                   &light, &pid);
-    using mm::add;
-    using mm::mul;
-    if (integrator == MUON_INTEGRATOR_NORMALS) {
-      out = make_float4(add(mul(nrm.x, 0.5f), 0.5f), add(mul(nrm.y, 0.5f), 0.5f), add(mul(nrm.z, 0.5f), 0.5f), 0.0f);
-    } else if (integrator == MUON_INTEGRATOR_ALBEDO) {
-      Mat m = LoadMat(s.materials, mat);
-      out = make_float4(add(m.kd.x, m.ks.x), add(m.kd.y, m.ks.y), add(m.kd.z, m.ks.z), 0.0f);
-    } else {
-      float v = mm::div(1.0f, add(1.0f, dist));
-      out = make_float4(v, v, v, 0.0f);
+__global__ void __launch_bounds__(kBlock) ShadeDebugKernel(DevScene s, PathBuffers b, WaveCounters wc,
+                                                           int integrator) {
+  const int n = static_cast<int>(*wc.count(0));
+  for (int j = blockIdx.x * kBlock + threadIdx.x; j < n; j += gridDim.x * kBlock) {
+    float4 o4 = b.ray_o[0][j], d4 = b.ray_d[0][j];
+    int path = __float_as_int(o4.w);
+    int2 h = b.hits[j];
+    float4 out = make_float4(0, 0, 0, 0);
+    if (h.y >= 0) {
+      float3 p, nrm;
+      float dist;
+      int mat, light, pid;
+      Surface<kMode>(s, h.y, f3(o4.x, o4.y, o4.z), f3(d4.x, d4.y, d4.z), __int_as_float(h.x), &p, &nrm, &dist, &mat,
+                     &light, &pid);
+      using mm::add;
+      using mm::mul;
+      if (integrator == MUON_INTEGRATOR_NORMALS) {
+        out = make_float4(add(mul(nrm.x, 0.5f), 0.5f), add(mul(nrm.y, 0.5f), 0.5f), add(mul(nrm.z, 0.5f), 0.5f),
+                          0.0f);
+      } else if (integrator == MUON_INTEGRATOR_ALBEDO) {
+        Mat m = LoadMat(s.materials, mat);
+        out = make_float4(add(m.kd.x, m.ks.x), add(m.kd.y, m.ks.y), add(m.kd.z, m.ks.z), 0.0f);
+      } else {
+        float v = mm::div(1.0f, add(1.0f, dist));
+        out = make_float4(v, v, v, 0.0f);
+      }
     }
+    b.final_rad[path] = out;
   }
-  b.rad[path] = out;
 }
 
-
 // ---- path tracer shading ----------------------------------------------------
-// PathTracer::Shade for one path vertex at depth `bounce`
+// PathTracer::Shade for every queued path vertex at depth `bounce`
 // (muon/integration.cc:205-328). Each shadow slot receives the radiance it
-// adds if its shadow ray is unblocked; the shadow rays themselves go to the
-// compacted queue as slot indices. The previous bounce's slots (already
-// resolved by the occlusion pass) are folded into the path radiance first.
+// adds if its shadow ray turns out unblocked; the shadow rays go to the
+// compacted shadow queue as slot indices, continuing paths to the next
+// bounce's queue (with their throughput and a link from this entry).
 constexpr int kMaskSlots = 64;
 
 template <int kMode>
 __global__ void __launch_bounds__(kBlock) ShadePathKernel(DevScene s, WaveInfo w, ShadeParams sp, PathBuffers b,
-                                                          int buf, int n, int bounce) {
-  const int j = blockIdx.x * blockDim.x + threadIdx.x;
-  const bool active = j < n;
+                                                          WaveCounters wc, int bounce) {
+  const int n = static_cast<int>(*wc.count(bounce));
+  const int cur = bounce & 1, nxt = cur ^ 1;
   const int S = sp.slots;
-  uint32_t want_cont = 0, nshadow = 0;
-  unsigned long long mask = 0;  // nonzero slots (first 64)
-  int path = 0;
-  float3 cont_o = f3(0, 0, 0), cont_d = f3(0, 0, 0);
   unsigned long long counted = 0;  // secondary rays in the reference's sense
+  QUEUE_LOOP(j, n) {
+    const int jj = j_base + threadIdx.x;
+    const bool active = jj < n;
+    uint32_t want_cont = 0, nshadow = 0;
+    unsigned long long mask = 0;  // nonzero slots (first 64)
+    int path = 0;
+    float3 cont_o = f3(0, 0, 0), cont_d = f3(0, 0, 0), cont_tp = f3(0, 0, 0);
+    if (active) {
+      const float4 o4 = b.ray_o[cur][jj], d4 = b.ray_d[cur][jj];
+      path = __float_as_int(o4.w);
+      const float3 o = f3(o4.x, o4.y, o4.z), d = f3(d4.x, d4.y, d4.z);
+      const int2 h = b.hits[jj];
+      float4 *contrib = b.contrib + static_cast<int64_t>(jj) * S;
+      float4 *sdir = b.slot_dir + static_cast<int64_t>(jj) * S;
+      for (int k = 0; k < S; ++k) contrib[k] = make_float4(0, 0, 0, 0);
+      float3 L = f3(b.rad[cur][jj]);
+      const float3 tp = f3(b.tp[cur][jj]);
 
-  if (active) {
-    const float4 o4 = b.ray_o[buf][j], d4 = b.ray_d[buf][j];
-    path = __float_as_int(o4.w);
-    const float3 o = f3(o4.x, o4.y, o4.z), d = f3(d4.x, d4.y, d4.z);
-    const int2 h = b.hits[j];
-    float4 *contrib = b.contrib + static_cast<int64_t>(path) * S;
-    float4 *sdir = b.slot_dir + static_cast<int64_t>(path) * S;
-    float4 r4 = b.rad[path];
-    float3 L = f3(r4.x, r4.y, r4.z);
-    if (bounce > 0) {
-      for (int k = 0; k < S; ++k) {
-        float4 c = contrib[k];
-        L = L + f3(c.x, c.y, c.z);
-        contrib[k] = make_float4(0, 0, 0, 0);
-      }
-    }
-    const float4 t4 = b.tp[path];
-    const float3 tp = f3(t4.x, t4.y, t4.z);
+      if (h.y >= 0) {
+        float3 p, nrm;
+        float hit_dist;
+        int mat_id, light_id, pid;
+        Surface<kMode>(s, h.y, o, d, __int_as_float(h.x), &p, &nrm, &hit_dist, &mat_id, &light_id, &pid);
+        const Mat m = LoadMat(s.materials, mat_id);
+        const float3 shift = p + kEps * nrm;
+        Rng rng = MakeRng(w, path, static_cast<uint32_t>(bounce));
+        const bool direct = bounce >= sp.min_depth;
+        const bool mis = direct && sp.nee == MUON_NEE_MIS;
 
-    if (h.y >= 0) {
-      float3 p, nrm;
-      float hit_dist;
-      int mat_id, light_id, pid;
-      Surface<kMode>(s, h.y, o, d, __int_as_float(h.x), &p, &nrm, &hit_dist, &mat_id, &light_id, &pid);
-      const Mat m = LoadMat(s.materials, mat_id);
-      const float3 shift = p + kEps * nrm;
-      Rng rng = MakeRng(w, path, static_cast<uint32_t>(bounce));
-      auto emit = [&](int slot, float3 c, float3 dir, float maxd) {
-        contrib[slot] = make_float4(c.x, c.y, c.z, 0.0f);
-        sdir[slot] = make_float4(dir.x, dir.y, dir.z, maxd);
-        ++nshadow;
-        if (slot < kMaskSlots) mask |= 1ull << slot;
-      };
-
-      if (bounce >= sp.min_depth) {
-        // Emission: only at the first vertex when lights are sampled, and only
-        // from the front face (muon/integration.cc:257-264).
-        if ((sp.nee == MUON_NEE_OFF || bounce == 0) && !(dot3(nrm, -d) < 0.0f)) L = L + tp * m.ke;
-        if (sp.nee != MUON_NEE_OFF) {
-          const bool mis = sp.nee == MUON_NEE_MIS;
-          int slot = 0;
-          // Area lights: ShadeDirectNEE (muon/integration.cc:371-462).
-          for (int li = 0; li < s.num_lights; ++li) {
-            const DevLight &l = s.lights[li];
-            const float3 corner = f3(l.corner), e0 = f3(l.edge0), e1 = f3(l.edge1), rev = f3(l.rev_normal);
-            const float3 lcol = f3(l.color);
-            const float scale = l.color.w / static_cast<float>(sp.light_samples);
-            const float inv_strata = 1.0f / static_cast<float>(sp.strata);
-            for (int si = 0; si < sp.strata; ++si) {
-              for (int sj = 0; sj < sp.strata; ++sj) {
-                for (int sk = 0; sk < sp.per_section; ++sk, ++slot) {
-                  float u = rng.Next(), v = rng.Next();
-                  float fu = (static_cast<float>(si) + u) * inv_strata;
-                  float fv = (static_cast<float>(sj) + v) * inv_strata;
-                  float3 lp = corner + fu * e0 + fv * e1 - kEps * rev;
-                  float3 ptl = lp - shift;
-                  float dist = sqrtf(dot3(ptl, ptl));
-                  float3 ldir = ptl * (1.0f / dist);
-                  float ci = fmaxf(dot3(nrm, ldir), 0.0f);
-                  float cl = fmaxf(dot3(rev, ldir), 0.0f);
-                  if (ci == 0.0f || cl == 0.0f) continue;
-                  float3 c = BrdfEval(m, ldir, d, nrm) * (ci * cl / (dist * dist));
-                  if (mis) {
-                    float lpdf = NeePdf(s, shift, ldir);
-                    float bpdf = IsPdf(sp.is_mode, m, ldir, d, nrm);
-                    c = c * PowerHeuristic(lpdf, bpdf);
-                  }
-                  c = tp * lcol * (c * scale);
-                  if (nonzero3(c)) emit(slot, c, ldir, dist);
-                }
+        if (direct) {
+          // Emission: only at the first vertex when lights are sampled, and
+          // only from the front face (muon/integration.cc:257-264).
+          if ((sp.nee == MUON_NEE_OFF || bounce == 0) && !(dot3(nrm, -d) < 0.0f)) L = L + tp * m.ke;
+          if (sp.nee != MUON_NEE_OFF) {
+            int slot = 0;
+            // Area lights: ShadeDirectNEE (muon/integration.cc:371-462).
+#pragma unroll 1
+            for (int li = 0; li < s.num_lights; ++li) {
+              const DevLight &l = s.lights[li];
+              const float3 corner = f3(l.corner), e0 = f3(l.edge0), e1 = f3(l.edge1), rev = f3(l.rev_normal);
+              const float3 lcol = f3(l.color) * (l.color.w / static_cast<float>(sp.light_samples));
+              const float inv_strata = 1.0f / static_cast<float>(sp.strata);
+#pragma unroll 1
+              for (int q = 0; q < sp.per_light; ++q, ++slot) {
+                const int si = (q / sp.per_section) / sp.strata, sj = (q / sp.per_section) % sp.strata;
+                float u = rng.Next(), v = rng.Next();
+                float fu = (static_cast<float>(si) + u) * inv_strata;
+                float fv = (static_cast<float>(sj) + v) * inv_strata;
+                float3 ptl = corner + fu * e0 + fv * e1 - kEps * rev - shift;
+                float dist = sqrtf(dot3(ptl, ptl));
+                float3 ldir = ptl * (1.0f / dist);
+                float ci = fmaxf(dot3(nrm, ldir), 0.0f);
+                float cl = fmaxf(dot3(rev, ldir), 0.0f);
+                if (ci == 0.0f || cl == 0.0f) continue;
+                float3 c = BrdfEval(m, ldir, d, nrm) * (ci * cl / (dist * dist));
+                if (mis) c = c * PowerHeuristic(NeePdf(s, shift, ldir), IsPdf(sp.is_mode, m, ldir, d, nrm));
+                c = tp * lcol * c;
+                if (!nonzero3(c)) continue;
+                contrib[slot] = make_float4(c.x, c.y, c.z, 0.0f);
+                sdir[slot] = make_float4(ldir.x, ldir.y, ldir.z, dist);
+                ++nshadow;
+                if (slot < kMaskSlots) mask |= 1ull << slot;
               }
             }
-          }
-          // Point and directional lights (muon/integration.cc:350-369,
-          // muon/lighting.cc:38-64).
-          for (int li = 0; li < s.num_other_lights; ++li, ++slot) {
-            const DevLight &l = s.other_lights[li];
-            float3 lcol = f3(l.color);
-            float3 ldir;
-            float dist;
-            if (__float_as_int(l.corner.w) == MUON_LIGHT_POINT) {
-              float3 ptl = f3(l.corner) - p;
-              ldir = normalize3(ptl);
-              dist = length3(ptl);
-              float att = l.edge0.x + l.edge0.y * dist + l.edge0.z * dist * dist;
-              lcol = lcol / att;
-              lcol = lcol / (dist * dist);
-            } else {
-              ldir = f3(l.corner);
-              dist = INFINITY;
+            // Point and directional lights (muon/integration.cc:350-369,
+            // muon/lighting.cc:38-64).
+#pragma unroll 1
+            for (int li = 0; li < s.num_other_lights; ++li, ++slot) {
+              const DevLight &l = s.other_lights[li];
+              float3 lcol = f3(l.color);
+              float3 ldir;
+              float dist;
+              if (__float_as_int(l.corner.w) == MUON_LIGHT_POINT) {
+                float3 ptl = f3(l.corner) - p;
+                ldir = normalize3(ptl);
+                dist = length3(ptl);
+                float att = l.edge0.x + l.edge0.y * dist + l.edge0.z * dist * dist;
+                lcol = lcol / att;
+                lcol = lcol / (dist * dist);
+              } else {
+                ldir = f3(l.corner);
+                dist = INFINITY;
+              }
+              float ci = fmaxf(dot3(nrm, ldir), 0.0f);
+              float3 c = tp * lcol * BrdfEval(m, ldir, d, nrm) * ci;
+              if (!nonzero3(c)) continue;
+              contrib[slot] = make_float4(c.x, c.y, c.z, 0.0f);
+              sdir[slot] = make_float4(ldir.x, ldir.y, ldir.z, dist);
+              ++nshadow;
+              if (slot < kMaskSlots) mask |= 1ull << slot;
             }
-            float ci = fmaxf(dot3(nrm, ldir), 0.0f);
-            float3 c = tp * lcol * BrdfEval(m, ldir, d, nrm) * ci;
-            if (nonzero3(c)) emit(slot, c, ldir, dist);
           }
-          // BRDF-sampled light hit: ShadeDirectImportanceSampling
-          // (muon/integration.cc:468-501). The sampled ray's closest hit is a
-          // light triangle exactly when some light triangle is hit at t_L and
-          // no primitive is hit before t_L, so it becomes an any-hit query up
-          // to t_L, and needs no traversal at all when it meets no light.
-          if (mis) {
-            float3 dir, ntp;
-            float bpdf;
-            if (SampleReflection(sp.is_mode, m, nrm, d, tp, rng, &dir, &bpdf, &ntp)) {
+        }
+        // Two BRDF samples share one code path: first the MIS light-hit ray
+        // (ShadeDirectImportanceSampling, muon/integration.cc:468-501), then
+        // the continuation (ShadeIndirect, muon/integration.cc:294-328).
+#pragma unroll 1
+        for (int pass = mis ? 0 : 1; pass < 2; ++pass) {
+          float3 dir, ntp;
+          float pdf;
+          if (!SampleReflection(sp.is_mode, m, nrm, d, tp, rng, &dir, &pdf, &ntp)) continue;
+          if (pass == 0) {
+            ++counted;
+            // The sampled ray's closest hit is a light triangle exactly when
+            // some light triangle is hit at t_L and nothing is hit before
+            // t_L: an any-hit query up to t_L, none if no light is met. Same
+            // triangle test and ray preparation as the traversal, so t_L is
+            // bit-identical to what the query compares against.
+            float best = INFINITY;
+            int best_light = -1;
+            RayPre rp = Prepare<kMode>(shift, dir);
+            const PrimRecord *lts = kMode == MUON_ISECT_EXACT ? s.light_tris_obj : s.light_tris;
+#pragma unroll 1
+            for (int lt = 0; lt < 2 * s.num_lights; ++lt) {
+              if (!s.light_tri_ok[lt]) continue;
+              PrimRecord lp = LoadPrim(lts, lt);
+              float t_obj;
+              float t = PrimTest<kMode>(s, rp, lp, __float_as_uint(lp.p3.w), &t_obj);
+              if (t > 0.0f && t < best) best = t, best_light = lt >> 1;
+            }
+            if (best_light < 0) continue;
+            float3 c = ntp * f3(s.lights[best_light].color) * PowerHeuristic(pdf, NeePdf(s, shift, dir));
+            if (!nonzero3(c)) continue;
+            const int slot = sp.mis_slot;
+            contrib[slot] = make_float4(c.x, c.y, c.z, 0.0f);
+            sdir[slot] = make_float4(dir.x, dir.y, dir.z, best);
+            ++nshadow;
+            if (slot < kMaskSlots) mask |= 1ull << slot;
+          } else {
+            bool survive = true;
+            if (sp.rr) {
+              float q = fminf(max3c(ntp), 1.0f);
+              if (q < rng.Next()) survive = false;
+              else ntp = ntp / q;
+            }
+            const int next_depth = bounce + 1;
+            const bool depth_ok = sp.max_trace_depth < 0 || next_depth <= sp.max_trace_depth;
+            if (survive && depth_ok && next_depth < sp.max_bounces) {
+              want_cont = 1;
               ++counted;
-              float best = INFINITY;
-              int best_light = -1;
-              // Same triangle test and ray preparation as the traversal, so the
-              // light's distance is bit-identical to the one the any-hit
-              // query will compare against.
-              RayPre rp = Prepare<kMode>(shift, dir);
-              const PrimRecord *lts = kMode == MUON_ISECT_EXACT ? s.light_tris_obj : s.light_tris;
-              for (int lt = 0; lt < 2 * s.num_lights; ++lt) {
-                if (!s.light_tri_ok[lt]) continue;
-                PrimRecord lp = LoadPrim(lts, lt);
-                float t_obj;
-                float t = PrimTest<kMode>(s, rp, lp, __float_as_uint(lp.p3.w), &t_obj);
-                if (t > 0.0f && t < best) best = t, best_light = lt >> 1;
-              }
-              if (best_light >= 0) {
-                float wgt = PowerHeuristic(bpdf, NeePdf(s, shift, dir));
-                float3 c = ntp * f3(s.lights[best_light].color) * wgt;
-                if (nonzero3(c)) emit(sp.mis_slot, c, dir, best);
-              }
+              cont_o = shift;
+              cont_d = dir;
+              cont_tp = ntp;
             }
           }
         }
+        if (nshadow) b.org[jj] = make_float4(shift.x, shift.y, shift.z, 0.0f);
       }
-      // Indirect: ShadeIndirect (muon/integration.cc:294-328).
-      float3 dir, ntp;
-      float pdf;
-      if (SampleReflection(sp.is_mode, m, nrm, d, tp, rng, &dir, &pdf, &ntp)) {
-        bool survive = true;
-        if (sp.rr) {
-          float q = fminf(max3c(ntp), 1.0f);
-          if (q < rng.Next()) survive = false;
-          else ntp = ntp / q;
-        }
-        const int next_depth = bounce + 1;
-        const bool depth_ok = sp.max_trace_depth < 0 || next_depth <= sp.max_trace_depth;
-        if (survive && depth_ok && next_depth < sp.max_bounces) {
-          want_cont = 1;
-          ++counted;
-          cont_o = shift;
-          cont_d = dir;
-          b.tp[path] = make_float4(ntp.x, ntp.y, ntp.z, 0.0f);
-        }
-      }
-      if (nshadow) b.org[path] = make_float4(shift.x, shift.y, shift.z, 0.0f);
+      b.rad[cur][jj] = make_float4(L.x, L.y, L.z, 0.0f);
     }
-    b.rad[path] = make_float4(L.x, L.y, L.z, 0.0f);
-  }
 
-  uint32_t off_c, off_s;
-  BlockReserve(want_cont, nshadow, b.counters + kCntNext, b.counters + kCntShadow, &off_c, &off_s);
-  if (want_cont) {
-    b.ray_o[buf ^ 1][off_c] = make_float4(cont_o.x, cont_o.y, cont_o.z, __int_as_float(path));
-    b.ray_d[buf ^ 1][off_c] = make_float4(cont_d.x, cont_d.y, cont_d.z, INFINITY);
-  }
-  if (nshadow) {
-    const uint32_t base = static_cast<uint32_t>(path) * static_cast<uint32_t>(S);
-    uint32_t k = off_s;
-    if (S <= kMaskSlots) {
-      while (mask) {
-        int slot = __ffsll(static_cast<long long>(mask)) - 1;
-        mask &= mask - 1;
-        b.shq[k++] = base + slot;
-      }
-    } else {
-      const float4 *contrib = b.contrib + static_cast<int64_t>(path) * S;
-      for (int slot = 0; slot < S; ++slot) {
-        float4 c = contrib[slot];
-        if (c.x != 0.0f || c.y != 0.0f || c.z != 0.0f) b.shq[k++] = base + slot;
+    uint32_t off_c, off_s;
+    BlockReserve(want_cont, nshadow, wc.count(bounce + 1), wc.shadow(bounce), &off_c, &off_s);
+    if (active) b.link[jj] = want_cont ? static_cast<int32_t>(off_c) : -1;
+    if (want_cont) {
+      b.ray_o[nxt][off_c] = make_float4(cont_o.x, cont_o.y, cont_o.z, __int_as_float(path));
+      b.ray_d[nxt][off_c] = make_float4(cont_d.x, cont_d.y, cont_d.z, INFINITY);
+      b.tp[nxt][off_c] = make_float4(cont_tp.x, cont_tp.y, cont_tp.z, 0.0f);
+    }
+    if (nshadow) {
+      const uint32_t base = static_cast<uint32_t>(jj) * static_cast<uint32_t>(S);
+      uint32_t k = off_s;
+      if (S <= kMaskSlots) {
+        while (mask) {
+          int slot = __ffsll(static_cast<long long>(mask)) - 1;
+          mask &= mask - 1;
+          b.shq[k++] = base + slot;
+        }
+      } else {
+        const float4 *contrib = b.contrib + static_cast<int64_t>(jj) * S;
+        for (int slot = 0; slot < S; ++slot) {
+          float4 c = contrib[slot];
+          if (c.x != 0.0f || c.y != 0.0f || c.z != 0.0f) b.shq[k++] = base + slot;
+        }
       }
     }
   }
   AddStat(b.stats, kStatSecondary, counted);
 }
 
+// ---- fold -----------------------------------------------------------------------
+// After the occlusion pass of a bounce: each entry's radiance plus its
+// unblocked shadow slots moves to its next-bounce entry, or to the path's
+// final radiance when the path ends here.
+__global__ void __launch_bounds__(kBlock) FoldKernel(PathBuffers b, WaveCounters wc, int bounce, int slots) {
+  const int n = static_cast<int>(*wc.count(bounce));
+  const int cur = bounce & 1, nxt = cur ^ 1;
+  for (int j = blockIdx.x * kBlock + threadIdx.x; j < n; j += gridDim.x * kBlock) {
+    float4 r = b.rad[cur][j];
+    const float4 *c = b.contrib + static_cast<int64_t>(j) * slots;
+    for (int k = 0; k < slots; ++k) {
+      float4 v = c[k];
+      r.x += v.x, r.y += v.y, r.z += v.z;
+    }
+    int next = b.link[j];
+    if (next >= 0) b.rad[nxt][next] = r;
+    else b.final_rad[__float_as_int(b.ray_o[cur][j].w)] = r;
+  }
+}
+
 // ---- film ----------------------------------------------------------------------
 // Film::SetPixel accumulation (muon/film.cc:10-19) in FP64: one thread per
 // pixel adds its samples in sample order, so the film is reproducible.
-__global__ void __launch_bounds__(kBlock) FilmKernel(WaveInfo w, PathBuffers b, int slots, double *sum,
-                                                     double *sum_sq, uint32_t *count) {
+__global__ void __launch_bounds__(kBlock) FilmKernel(WaveInfo w, PathBuffers b, double *sum, double *sum_sq,
+                                                     uint32_t *count) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= w.npix) return;
   const int pixel = w.p0 + i;
   double s0 = 0, s1 = 0, s2 = 0, q0 = 0, q1 = 0, q2 = 0;
   for (int k = 0; k < w.ns; ++k) {
-    const int path = i * w.ns + k;
-    float4 r = b.rad[path];
-    float x = r.x, y = r.y, z = r.z;
-    const float4 *c = b.contrib + static_cast<int64_t>(path) * slots;
-    for (int q = 0; q < slots; ++q) {
-      float4 v = c[q];
-      x += v.x, y += v.y, z += v.z;
-    }
-    s0 += x, s1 += y, s2 += z;
-    q0 += static_cast<double>(x) * x, q1 += static_cast<double>(y) * y, q2 += static_cast<double>(z) * z;
+    float4 r = b.final_rad[i * w.ns + k];
+    s0 += r.x, s1 += r.y, s2 += r.z;
+    q0 += static_cast<double>(r.x) * r.x, q1 += static_cast<double>(r.y) * r.y, q2 += static_cast<double>(r.z) * r.z;
   }
   sum[3 * pixel + 0] += s0;
   sum[3 * pixel + 1] += s1;
@@ -567,6 +585,13 @@ __global__ void __launch_bounds__(kBlock) OccludedRaysKernel(DevScene s, const f
 
 inline unsigned Blocks(int64_t n) { return static_cast<unsigned>((n + kBlock - 1) / kBlock); }
 
+int g_persistent_blocks = 152 * 8;
+
+// Grid for a device-counted launch whose queue holds at most `bound` entries.
+inline unsigned CountedBlocks(int64_t bound) {
+  return static_cast<unsigned>(std::max<int64_t>(1, std::min<int64_t>(Blocks(bound), g_persistent_blocks)));
+}
+
 // Calls f(std::integral_constant<int, mode>) for a runtime intersection mode.
 template <class F>
 void WithMode(int mode, F &&f) {
@@ -577,49 +602,56 @@ void WithMode(int mode, F &&f) {
 
 }  // namespace
 
-void LaunchCamera(const DevCamera &cam, const WaveInfo &w, const PathBuffers &b, int slots, cudaStream_t st) {
-  if (w.n > 0) CameraKernel<<<Blocks(w.n), kBlock, 0, st>>>(cam, w, b, slots);
+void SetPersistentGrid(int blocks) { g_persistent_blocks = std::max(1, blocks); }
+
+void LaunchCamera(const DevCamera &cam, const WaveInfo &w, const PathBuffers &b, WaveCounters wc, cudaStream_t st) {
+  CameraKernel<<<Blocks(std::max(w.n, 1)), kBlock, 0, st>>>(cam, w, b, wc);
 }
 
-void LaunchExtend(const DevScene &s, const PathBuffers &b, int buf, int n, int isect, bool stats, cudaStream_t st) {
-  if (n <= 0) return;
+void LaunchExtend(const DevScene &s, const PathBuffers &b, WaveCounters wc, int bounce, int bound, int isect,
+                  bool stats, cudaStream_t st) {
+  if (bound <= 0) return;
   WithMode(isect, [&](auto m) {
     constexpr int M = decltype(m)::value;
-    if (stats) ExtendKernel<true, M><<<Blocks(n), kBlock, 0, st>>>(s, b.ray_o[buf], b.ray_d[buf], n, b.hits, b.stats);
-    else ExtendKernel<false, M><<<Blocks(n), kBlock, 0, st>>>(s, b.ray_o[buf], b.ray_d[buf], n, b.hits, b.stats);
+    if (stats) ExtendKernel<true, M><<<CountedBlocks(bound), kBlock, 0, st>>>(s, b, wc, bounce);
+    else ExtendKernel<false, M><<<CountedBlocks(bound), kBlock, 0, st>>>(s, b, wc, bounce);
   });
 }
 
-void LaunchShadeDebug(const DevScene &s, const WaveInfo &w, const PathBuffers &b, int integrator, int n, int isect,
+void LaunchShadeDebug(const DevScene &s, const PathBuffers &b, WaveCounters wc, int integrator, int bound, int isect,
                       cudaStream_t st) {
-  (void)w;
-  if (n <= 0) return;
+  if (bound <= 0) return;
   WithMode(isect, [&](auto m) {
-    ShadeDebugKernel<decltype(m)::value><<<Blocks(n), kBlock, 0, st>>>(s, b, integrator, n);
+    ShadeDebugKernel<decltype(m)::value><<<CountedBlocks(bound), kBlock, 0, st>>>(s, b, wc, integrator);
   });
 }
 
-void LaunchShadePath(const DevScene &s, const WaveInfo &w, const ShadeParams &sp, const PathBuffers &b, int buf,
-                     int n, int bounce, cudaStream_t st) {
-  if (n <= 0) return;
+void LaunchShadePath(const DevScene &s, const WaveInfo &w, const ShadeParams &sp, const PathBuffers &b,
+                     WaveCounters wc, int bounce, int bound, cudaStream_t st) {
+  if (bound <= 0) return;
   WithMode(sp.isect, [&](auto m) {
-    ShadePathKernel<decltype(m)::value><<<Blocks(n), kBlock, 0, st>>>(s, w, sp, b, buf, n, bounce);
+    ShadePathKernel<decltype(m)::value><<<CountedBlocks(bound), kBlock, 0, st>>>(s, w, sp, b, wc, bounce);
   });
 }
 
-void LaunchOcclude(const DevScene &s, const PathBuffers &b, int slots, int n, int isect, bool stats,
-                   cudaStream_t st) {
-  if (n <= 0) return;
+void LaunchOcclude(const DevScene &s, const PathBuffers &b, WaveCounters wc, int bounce, int slots, int bound,
+                   int isect, bool stats, cudaStream_t st) {
+  if (bound <= 0 || slots <= 0) return;
   WithMode(isect, [&](auto m) {
     constexpr int M = decltype(m)::value;
-    if (stats) OccludeKernel<true, M><<<Blocks(n), kBlock, 0, st>>>(s, b.shq, slots, n, b.org, b.slot_dir, b.contrib, b.stats);
-    else OccludeKernel<false, M><<<Blocks(n), kBlock, 0, st>>>(s, b.shq, slots, n, b.org, b.slot_dir, b.contrib, b.stats);
+    if (stats) OccludeKernel<true, M><<<CountedBlocks(bound), kBlock, 0, st>>>(s, b, wc, bounce, slots);
+    else OccludeKernel<false, M><<<CountedBlocks(bound), kBlock, 0, st>>>(s, b, wc, bounce, slots);
   });
 }
 
-void LaunchFilm(const WaveInfo &w, const PathBuffers &b, int slots, double *sum, double *sum_sq, uint32_t *count,
+void LaunchFold(const PathBuffers &b, WaveCounters wc, int bounce, int slots, int bound, cudaStream_t st) {
+  if (bound <= 0) return;
+  FoldKernel<<<CountedBlocks(bound), kBlock, 0, st>>>(b, wc, bounce, slots);
+}
+
+void LaunchFilm(const WaveInfo &w, const PathBuffers &b, double *sum, double *sum_sq, uint32_t *count,
                 cudaStream_t st) {
-  if (w.npix > 0) FilmKernel<<<Blocks(w.npix), kBlock, 0, st>>>(w, b, slots, sum, sum_sq, count);
+  if (w.npix > 0) FilmKernel<<<Blocks(w.npix), kBlock, 0, st>>>(w, b, sum, sum_sq, count);
 }
 
 void LaunchIntersectRays(const DevScene &s, const float *rays, int64_t n, int isect, float *out_hit, cudaStream_t st) {

@@ -10,8 +10,6 @@
 
 namespace muon_gpu {
 
-// Device counters (uint32) used by the queue kernels.
-enum Counter : int { kCntNext = 0, kCntShadow = 1, kNumCounters = 4 };
 // Device statistics (uint64).
 enum Stat : int {
   kStatPrimary = 0,
@@ -32,7 +30,7 @@ enum Stat : int {
 // One wavefront: `n` paths covering pixels [p0, p0 + npix) with samples
 // [s0, s0 + ns) each; path i is pixel p0 + i / ns, sample s0 + i % ns.
 struct WaveInfo {
-  int32_t width;      // film width (pixel index = y * width + x)
+  int32_t width;  // film width (pixel index = y * width + x)
   int32_t p0, npix;
   int32_t s0, ns;
   int32_t n;
@@ -41,17 +39,32 @@ struct WaveInfo {
   uint64_t seed;
 };
 
+// Queue counters of one wavefront, all on the device so that a wavefront is a
+// fixed launch sequence: count(k) = paths queued at bounce k (count(0) = n),
+// shadow(k) = shadow rays emitted at bounce k.
+struct WaveCounters {
+  uint32_t *c;
+  __host__ __device__ uint32_t *count(int k) const { return c + 2 * k; }
+  __host__ __device__ uint32_t *shadow(int k) const { return c + 2 * k + 1; }
+};
+
+// Path state lives in queue order: entry j of bounce k's queue holds its ray,
+// hit, throughput and radiance at index j, so every per-path access in the
+// bounce kernels is coalesced. `link[j]` is the entry's index in the next
+// bounce's queue (-1 when the path ends there); `final_rad[path]` receives
+// the radiance of a path when it ends (path = wave-local sample index).
 struct PathBuffers {
-  float4 *ray_o[2];   // path-ray queue: (origin, path id bits)
-  float4 *ray_d[2];   // path-ray queue: (direction, tmax)
-  int2 *hits;         // (t bits, leaf slot) per queued ray
-  float4 *tp;         // throughput per path
-  float4 *rad;        // radiance per path
-  float4 *org;        // shadow-ray origin per path (the shifted hit point)
-  float4 *contrib;    // S shadow slots per path: (radiance if unblocked, -)
-  float4 *slot_dir;   // S shadow slots per path: (direction, max distance)
-  uint32_t *shq;      // shadow queue: slot indices
-  uint32_t *counters;
+  float4 *ray_o[2];   // (origin, path id bits)
+  float4 *ray_d[2];   // (direction, tmax)
+  float4 *tp[2];      // throughput
+  float4 *rad[2];     // radiance so far
+  int2 *hits;         // (t bits, leaf slot)
+  int32_t *link;      // next-queue index or -1
+  float4 *final_rad;  // per path
+  float4 *org;        // shadow-ray origin per queue entry
+  float4 *contrib;    // S slots per queue entry: radiance if unblocked
+  float4 *slot_dir;   // S slots per queue entry: (direction, max distance)
+  uint32_t *shq;      // shadow queue: slot indices (entry * S + slot)
   unsigned long long *stats;
 };
 
@@ -62,21 +75,27 @@ struct ShadeParams {
   int32_t max_trace_depth;  // deepest Trace() depth that casts a ray; -1 = unbounded
   int32_t strata, per_section, per_light;  // samples per quad light = strata^2 * per_section
   int32_t light_samples;
-  int32_t slots;           // shadow slots per path
-  int32_t mis_slot;        // slot index of the MIS ray, -1 if none
+  int32_t slots;     // shadow slots per path
+  int32_t mis_slot;  // slot index of the MIS ray, -1 if none
   int32_t isect;
   int32_t max_bounces;
 };
 
-void LaunchCamera(const DevCamera &cam, const WaveInfo &w, const PathBuffers &b, int slots, cudaStream_t st);
-void LaunchExtend(const DevScene &s, const PathBuffers &b, int buf, int n, int isect, bool stats,
-                  cudaStream_t st);
-void LaunchShadeDebug(const DevScene &s, const WaveInfo &w, const PathBuffers &b, int integrator, int n, int isect,
+// Upper bound on the blocks of the device-counted launches (they loop over
+// their queue with a grid stride); set from the SM count at scene creation.
+void SetPersistentGrid(int blocks);
+
+void LaunchCamera(const DevCamera &cam, const WaveInfo &w, const PathBuffers &b, WaveCounters wc, cudaStream_t st);
+void LaunchExtend(const DevScene &s, const PathBuffers &b, WaveCounters wc, int bounce, int bound, int isect,
+                  bool stats, cudaStream_t st);
+void LaunchShadeDebug(const DevScene &s, const PathBuffers &b, WaveCounters wc, int integrator, int bound, int isect,
                       cudaStream_t st);
-void LaunchShadePath(const DevScene &s, const WaveInfo &w, const ShadeParams &sp, const PathBuffers &b, int buf,
-                     int n, int bounce, cudaStream_t st);
-void LaunchOcclude(const DevScene &s, const PathBuffers &b, int slots, int n, int isect, bool stats, cudaStream_t st);
-void LaunchFilm(const WaveInfo &w, const PathBuffers &b, int slots, double *sum, double *sum_sq, uint32_t *count,
+void LaunchShadePath(const DevScene &s, const WaveInfo &w, const ShadeParams &sp, const PathBuffers &b,
+                     WaveCounters wc, int bounce, int bound, cudaStream_t st);
+void LaunchOcclude(const DevScene &s, const PathBuffers &b, WaveCounters wc, int bounce, int slots, int bound,
+                   int isect, bool stats, cudaStream_t st);
+void LaunchFold(const PathBuffers &b, WaveCounters wc, int bounce, int slots, int bound, cudaStream_t st);
+void LaunchFilm(const WaveInfo &w, const PathBuffers &b, double *sum, double *sum_sq, uint32_t *count,
                 cudaStream_t st);
 // Ray-level queries for the batched Intersect/HasIntersection seams.
 void LaunchIntersectRays(const DevScene &s, const float *rays, int64_t n, int isect, float *out_hit,

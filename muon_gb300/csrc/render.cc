@@ -25,7 +25,7 @@ namespace {
 
 constexpr int kDefaultWavePaths = 1 << 21;
 constexpr int kMaxBounces = 256;  // hard cap for unbounded depth without Russian roulette
-constexpr int kMaxEventPairs = 4096;
+constexpr int kMaxEventPairs = 16384;
 
 struct CudaError {
   cudaError_t code;
@@ -83,16 +83,24 @@ struct MuonScene {
   DeviceBuffer nodes, prims, prims_obj, shade, smooth, smooth_obj, transforms, materials, lights, light_tris,
       light_tris_obj, light_tri_ok, other_lights;
   // work arrays
-  DeviceBuffer ray_o[2], ray_d[2], hits, tp, rad, org, contrib, slot_dir, shq, counters, stats;
+  DeviceBuffer ray_o[2], ray_d[2], tp[2], rad[2], hits, link, final_rad, org, contrib, slot_dir, shq, counters, stats;
   DeviceBuffer film_sum, film_sq, film_cnt, ray_in, ray_out, ray_aux;
   int64_t wave_cap = 0;
   int slots_cap = -1;
-  uint32_t *h_counters = nullptr;  // pinned
+  uint32_t *h_counters = nullptr;  // pinned, one WaveCounters block per wave
+  size_t h_counters_len = 0;
   std::vector<EventPair> events;
   int events_used = 0;
   MuonStats last{};
+  // Instantiated CUDA graph of the last bounded-depth render and the launch
+  // configuration it was captured for.
+  cudaGraphExec_t graph = nullptr;
+  std::string graph_key;
+  int graph_events = 0;
+  uint64_t graph_launches = 0;
 
   ~MuonScene() {
+    if (graph) cudaGraphExecDestroy(graph);
     for (EventPair &e : events) {
       if (e.a) cudaEventDestroy(e.a);
       if (e.b) cudaEventDestroy(e.b);
@@ -119,30 +127,34 @@ struct MuonScene {
     for (int k = 0; k < 2; ++k) {
       b.ray_o[k] = ray_o[k].as<float4>();
       b.ray_d[k] = ray_d[k].as<float4>();
+      b.tp[k] = tp[k].as<float4>();
+      b.rad[k] = rad[k].as<float4>();
     }
     b.hits = hits.as<int2>();
-    b.tp = tp.as<float4>();
-    b.rad = rad.as<float4>();
+    b.link = link.as<int32_t>();
+    b.final_rad = final_rad.as<float4>();
     b.org = org.as<float4>();
     b.contrib = contrib.as<float4>();
     b.slot_dir = slot_dir.as<float4>();
     b.shq = shq.as<uint32_t>();
-    b.counters = counters.as<uint32_t>();
     b.stats = stats.as<unsigned long long>();
     return b;
   }
 
-  void EnsureWork(int64_t paths, int slots) {
-    if (paths <= wave_cap && slots <= slots_cap) return;
+  // Grows the per-wavefront arrays; returns true if any pointer changed.
+  bool EnsureWork(int64_t paths, int slots) {
+    if (paths <= wave_cap && slots <= slots_cap) return false;
     int64_t p = std::max(paths, wave_cap);
     int s = std::max(slots, slots_cap);
     for (int k = 0; k < 2; ++k) {
       ray_o[k].Ensure(p * sizeof(float4));
       ray_d[k].Ensure(p * sizeof(float4));
+      tp[k].Ensure(p * sizeof(float4));
+      rad[k].Ensure(p * sizeof(float4));
     }
     hits.Ensure(p * sizeof(int2));
-    tp.Ensure(p * sizeof(float4));
-    rad.Ensure(p * sizeof(float4));
+    link.Ensure(p * sizeof(int32_t));
+    final_rad.Ensure(p * sizeof(float4));
     org.Ensure(p * sizeof(float4));
     size_t sl = static_cast<size_t>(p) * std::max(s, 1);
     contrib.Ensure(sl * sizeof(float4));
@@ -150,6 +162,25 @@ struct MuonScene {
     shq.Ensure(sl * sizeof(uint32_t));
     wave_cap = p;
     slots_cap = s;
+    return true;
+  }
+
+  // Grows the device and pinned host counter arrays; returns true if the
+  // device pointer changed.
+  bool EnsureCounters(size_t words) {
+    if (words <= h_counters_len) return false;
+    counters.Ensure(words * sizeof(uint32_t));
+    if (h_counters) cudaFreeHost(h_counters);
+    h_counters = nullptr;
+    CUDA_TRY(cudaMallocHost(reinterpret_cast<void **>(&h_counters), words * sizeof(uint32_t)));
+    h_counters_len = words;
+    return true;
+  }
+
+  void DropGraph() {
+    if (graph) cudaGraphExecDestroy(graph);
+    graph = nullptr;
+    graph_key.clear();
   }
 };
 
@@ -214,10 +245,18 @@ int ValidateParams(const MuonRenderParams &p) {
 }
 
 // Renders into a device film. Throws CudaError.
+//
+// Bounded depth: every wavefront is a fixed launch sequence (camera; per
+// bounce extend, shade, occlude, fold; film) whose kernels read their queue
+// lengths from device counters, so the whole frame is captured once into a
+// CUDA graph and replayed; the host synchronises once per frame. Unbounded
+// depth (max_depth -1): the host reads the queue length after every bounce and
+// stops when no path continues.
 void RenderDevice(MuonScene *sc, const MuonRenderParams &p, double *d_sum, double *d_sq, uint32_t *d_cnt) {
   cudaStream_t st = sc->stream;
   const bool pt = p.integrator == MUON_INTEGRATOR_PATHTRACER;
   const bool stats_on = (p.flags & MUON_RENDER_STATS) != 0;
+  const bool timing = (p.flags & MUON_RENDER_TIMING) != 0;
   ShadeParams sp{};
   sp.integrator = p.integrator;
   sp.nee = p.next_event_estimation;
@@ -246,81 +285,142 @@ void RenderDevice(MuonScene *sc, const MuonRenderParams &p, double *d_sum, doubl
   const int spp = p.pixel_samples;
   int64_t budget = p.wave_paths > 0 ? p.wave_paths : kDefaultWavePaths;
   // Keep per-wave slot storage within ~4 GiB.
-  const int64_t per_path = 160 + 36 * static_cast<int64_t>(std::max(slots, 1));
+  const int64_t per_path = 200 + 36 * static_cast<int64_t>(std::max(slots, 1));
   budget = std::max<int64_t>(1, std::min<int64_t>(budget, (int64_t(4) << 30) / per_path));
   const int ns = static_cast<int>(std::min<int64_t>(spp, budget));
   const int64_t pix_per_wave = std::max<int64_t>(1, budget / ns);
-  sc->EnsureWork(std::min<int64_t>(pix_per_wave, npix_total) * ns, slots);
-  sc->counters.Ensure(sizeof(uint32_t) * kNumCounters);
-  sc->stats.Ensure(sizeof(unsigned long long) * kNumStats);
-  CUDA_TRY(cudaMemsetAsync(sc->stats.ptr, 0, sizeof(unsigned long long) * kNumStats, st));
-  PathBuffers b = sc->Buffers();
-  sc->events_used = 0;
-
-  cudaEvent_t t0 = sc->NextEvent(2)->a, t1 = sc->events[0].b;
-  CUDA_TRY(cudaEventRecord(t0, st));
-  uint64_t primary = 0, shadow = 0, launches = 0, ext_rays = 0, ext_launches = 0, occ_launches = 0;
-  const bool traces = !(p.max_depth >= 0 && sp.max_trace_depth < 0);
+  std::vector<WaveInfo> waves;
   for (int64_t p0 = 0; p0 < npix_total; p0 += pix_per_wave) {
-    const int npix = static_cast<int>(std::min<int64_t>(pix_per_wave, npix_total - p0));
     for (int s0 = 0; s0 < spp; s0 += ns) {
       WaveInfo w{};
       w.width = W;
       w.p0 = static_cast<int32_t>(p0);
-      w.npix = npix;
+      w.npix = static_cast<int>(std::min<int64_t>(pix_per_wave, npix_total - p0));
       w.s0 = s0;
       w.ns = std::min(ns, spp - s0);
-      w.n = npix * w.ns;
+      w.n = w.npix * w.ns;
       w.sample_offset = static_cast<uint32_t>(p.sample_offset);
       w.seed = p.seed;
-      LaunchCamera(sc->cam, w, b, slots, st);
+      waves.push_back(w);
+    }
+  }
+  // A path traces at depths 0..max_trace_depth; with max_depth 0 and lights
+  // sampled, Trace() casts no ray at all.
+  const bool traces = !(p.max_depth >= 0 && sp.max_trace_depth < 0);
+  const bool bounded = !pt || sp.max_trace_depth >= 0;
+  const int bounces = !traces ? 0 : (!pt ? 1 : (bounded ? sp.max_trace_depth + 1 : kMaxBounces));
+  const size_t stride = 2 * static_cast<size_t>(bounces + 2);
+  bool moved = sc->EnsureWork(std::min<int64_t>(pix_per_wave, npix_total) * ns, slots);
+  moved |= sc->EnsureCounters(stride * waves.size());
+  sc->stats.Ensure(sizeof(unsigned long long) * kNumStats);
+  PathBuffers b = sc->Buffers();
+
+  uint64_t launches = 0;
+  int timed_pairs = 1;
+  // Records the launch sequence of the whole frame on `st`.
+  auto enqueue = [&](bool host_loop) {
+    sc->events_used = 1;  // pair 0 brackets the frame
+    CUDA_TRY(cudaMemsetAsync(sc->counters.ptr, 0, stride * waves.size() * sizeof(uint32_t), st));
+    CUDA_TRY(cudaMemsetAsync(sc->stats.ptr, 0, sizeof(unsigned long long) * kNumStats, st));
+    for (size_t wi = 0; wi < waves.size(); ++wi) {
+      const WaveInfo &w = waves[wi];
+      WaveCounters wc{sc->counters.as<uint32_t>() + wi * stride};
+      LaunchCamera(sc->cam, w, b, wc, st);
       ++launches;
-      int n_cur = w.n, buf = 0;
-      if (traces) {
-        primary += static_cast<uint64_t>(w.n);
-        for (int bounce = 0; n_cur > 0; ++bounce) {
-          EventPair *ev = sc->NextEvent(0);
-          if (ev) CUDA_TRY(cudaEventRecord(ev->a, st));
-          LaunchExtend(sc->dev, b, buf, n_cur, p.intersect_mode, stats_on, st);
-          if (ev) CUDA_TRY(cudaEventRecord(ev->b, st));
-          ++launches;
-          ++ext_launches;
-          ext_rays += static_cast<uint64_t>(n_cur);
-          if (!pt) {
-            LaunchShadeDebug(sc->dev, w, b, p.integrator, n_cur, p.intersect_mode, st);
-            ++launches;
-            break;
-          }
-          CUDA_TRY(cudaMemsetAsync(b.counters, 0, sizeof(uint32_t) * kNumCounters, st));
-          LaunchShadePath(sc->dev, w, sp, b, buf, n_cur, bounce, st);
-          ++launches;
-          CUDA_TRY(cudaMemcpyAsync(sc->h_counters, b.counters, sizeof(uint32_t) * kNumCounters,
-                                   cudaMemcpyDeviceToHost, st));
+      auto timed = [&](int kind, auto &&launch) {
+        // External event nodes when captured, so they time the kernels
+        // inside the replayed graph.
+        EventPair *ev = timing ? sc->NextEvent(kind) : nullptr;
+        if (ev) CUDA_TRY(cudaEventRecordWithFlags(ev->a, st, cudaEventRecordExternal));
+        launch();
+        if (ev) CUDA_TRY(cudaEventRecordWithFlags(ev->b, st, cudaEventRecordExternal));
+        ++launches;
+      };
+      for (int k = 0; k < bounces; ++k) {
+        timed(0, [&] { LaunchExtend(sc->dev, b, wc, k, w.n, p.intersect_mode, stats_on, st); });
+        if (!pt) {
+          timed(2, [&] { LaunchShadeDebug(sc->dev, b, wc, p.integrator, w.n, p.intersect_mode, st); });
+          break;
+        }
+        timed(2, [&] { LaunchShadePath(sc->dev, w, sp, b, wc, k, w.n, st); });
+        if (slots > 0) {
+          timed(1, [&] {
+            LaunchOcclude(sc->dev, b, wc, k, slots, static_cast<int>(std::min<int64_t>(int64_t(w.n) * slots, INT32_MAX)),
+                          p.intersect_mode, stats_on, st);
+          });
+        }
+        timed(3, [&] { LaunchFold(b, wc, k, slots, w.n, st); });
+        if (host_loop) {
+          CUDA_TRY(cudaMemcpyAsync(sc->h_counters, wc.count(k + 1), sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
           CUDA_TRY(cudaStreamSynchronize(st));
-          const int n_sh = static_cast<int>(sc->h_counters[kCntShadow]);
-          const int n_next = static_cast<int>(sc->h_counters[kCntNext]);
-          if (n_sh > 0) {
-            EventPair *eo = sc->NextEvent(1);
-            if (eo) CUDA_TRY(cudaEventRecord(eo->a, st));
-            LaunchOcclude(sc->dev, b, slots, n_sh, p.intersect_mode, stats_on, st);
-            if (eo) CUDA_TRY(cudaEventRecord(eo->b, st));
-            ++launches;
-            ++occ_launches;
-          }
-          shadow += static_cast<uint64_t>(n_sh);
-          n_cur = n_next;
-          buf ^= 1;
+          if (sc->h_counters[0] == 0) break;
         }
       }
-      LaunchFilm(w, b, slots, d_sum, d_sq, d_cnt, st);
+      LaunchFilm(w, b, d_sum, d_sq, d_cnt, st);
       ++launches;
     }
+    timed_pairs = sc->events_used;
+  };
+
+  cudaEvent_t t0 = sc->NextEvent(2)->a;
+  cudaEvent_t t1 = sc->events[0].b;
+  char keybuf[512];
+  std::snprintf(keybuf, sizeof(keybuf), "%d %d %d %d %d %d %d %d %d %d %llu %d %d %u %p %p %p %zu %d", p.integrator,
+                p.pixel_samples, p.light_samples, p.light_stratify, p.next_event_estimation, p.russian_roulette,
+                p.importance_sampling, p.min_depth, p.max_depth, p.sample_offset, (unsigned long long)p.seed,
+                p.intersect_mode, p.wave_paths, p.flags, (void *)d_sum, (void *)d_sq, (void *)d_cnt, waves.size(),
+                bounces);
+  const bool use_graph = bounded && !(p.flags & MUON_RENDER_NO_GRAPH);
+  if (moved) sc->DropGraph();
+  CUDA_TRY(cudaEventRecord(t0, st));
+  if (use_graph) {
+    if (sc->graph_key != keybuf || !sc->graph) {
+      sc->DropGraph();
+      cudaGraph_t g = nullptr;
+      launches = 0;
+      CUDA_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+      try {
+        enqueue(false);
+      } catch (...) {
+        cudaGraph_t dummy = nullptr;
+        cudaStreamEndCapture(st, &dummy);
+        if (dummy) cudaGraphDestroy(dummy);
+        throw;
+      }
+      CUDA_TRY(cudaStreamEndCapture(st, &g));
+      cudaError_t e = cudaGraphInstantiate(&sc->graph, g, 0);
+      cudaGraphDestroy(g);
+      if (e != cudaSuccess) throw CudaError{e, "cudaGraphInstantiate"};
+      sc->graph_key = keybuf;
+      sc->graph_events = timed_pairs;
+      sc->graph_launches = launches;
+    }
+    CUDA_TRY(cudaGraphLaunch(sc->graph, st));
+    launches = sc->graph_launches;
+    timed_pairs = sc->graph_events;
+  } else {
+    enqueue(!bounded);
   }
   CUDA_TRY(cudaEventRecord(t1, st));
   CUDA_TRY(cudaGetLastError());
   unsigned long long hstats[kNumStats];
   CUDA_TRY(cudaMemcpyAsync(hstats, sc->stats.ptr, sizeof(hstats), cudaMemcpyDeviceToHost, st));
+  CUDA_TRY(cudaMemcpyAsync(sc->h_counters, sc->counters.ptr, stride * waves.size() * sizeof(uint32_t),
+                           cudaMemcpyDeviceToHost, st));
   CUDA_TRY(cudaStreamSynchronize(st));
+  uint64_t primary = 0, ext_rays = 0, shadow = 0, ext_launches = 0, occ_launches = 0;
+  for (size_t wi = 0; wi < waves.size(); ++wi) {
+    const uint32_t *c = sc->h_counters + wi * stride;
+    if (traces) primary += static_cast<uint64_t>(waves[wi].n);
+    for (int k = 0; k < bounces; ++k) {
+      ext_rays += c[2 * k];
+      shadow += c[2 * k + 1];
+      if (c[2 * k] > 0) {
+        ++ext_launches;
+        if (slots > 0) ++occ_launches;
+      }
+    }
+  }
   MuonStats &o = sc->last;
   o = MuonStats{};
   o.primary_rays = primary;
@@ -330,6 +430,10 @@ void RenderDevice(MuonScene *sc, const MuonRenderParams &p, double *d_sum, doubl
   o.bounds_hits = hstats[kStatBoxHits] + hstats[kStatOccBoxHits];
   o.object_tests = hstats[kStatPrimTests] + hstats[kStatOccPrimTests];
   o.object_hits = hstats[kStatPrimHits] + hstats[kStatOccPrimHits];
+  o.paths = static_cast<uint64_t>(npix_total) * spp;
+  o.kernel_launches = launches;
+  o.bvh_nodes = static_cast<uint64_t>(sc->img.nodes.size());
+  o.primitives = static_cast<uint64_t>(sc->img.num_prims);
   o.extend_rays = ext_rays;
   o.extend_launches = ext_launches;
   o.extend_box_tests = hstats[kStatBoxTests];
@@ -338,20 +442,17 @@ void RenderDevice(MuonScene *sc, const MuonRenderParams &p, double *d_sum, doubl
   o.occlude_launches = occ_launches;
   o.occlude_box_tests = hstats[kStatOccBoxTests];
   o.occlude_prim_tests = hstats[kStatOccPrimTests];
-  o.paths = static_cast<uint64_t>(npix_total) * spp;
-  o.kernel_launches = launches;
-  o.bvh_nodes = static_cast<uint64_t>(sc->img.nodes.size());
-  o.primitives = static_cast<uint64_t>(sc->img.num_prims);
   float ms = 0.0f;
   CUDA_TRY(cudaEventElapsedTime(&ms, t0, t1));
   o.render_ms = ms;
-  for (int i = 1; i < sc->events_used; ++i) {
+  for (int i = 1; i < timed_pairs; ++i) {
     float e = 0.0f;
     CUDA_TRY(cudaEventElapsedTime(&e, sc->events[i].a, sc->events[i].b));
     if (sc->events[i].kind == 0) o.extend_ms += e;
     else if (sc->events[i].kind == 1) o.occlude_ms += e;
+    else if (sc->events[i].kind == 2) o.shade_ms += e;
+    else o.fold_ms += e;
   }
-  o.shade_ms = std::max(0.0, o.render_ms - o.extend_ms - o.occlude_ms);
   if (hstats[kStatOverflow]) SetLastError("BVH traversal stack overflowed; results may miss hits");
 }
 
@@ -374,8 +475,10 @@ int muon_gpu_scene_create(const MuonSceneDesc *desc, MuonScene **out) {
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return Fail(MUON_ERR_CUDA, "no CUDA device available");
     CUDA_TRY(cudaGetDevice(&sc->device));
+    int sms = 0;
+    CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, sc->device));
+    SetPersistentGrid(sms * 8);
     CUDA_TRY(cudaStreamCreateWithFlags(&sc->stream, cudaStreamNonBlocking));
-    CUDA_TRY(cudaMallocHost(reinterpret_cast<void **>(&sc->h_counters), sizeof(uint32_t) * kNumCounters));
     cudaStream_t st = sc->stream;
     const SceneImage &im = sc->img;
     Upload(sc->nodes, im.nodes, st);

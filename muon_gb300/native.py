@@ -21,7 +21,7 @@ IMPORTANCE = {"hemisphere": 0, "cosine": 1, "brdf": 2}
 ISECT_FAST, ISECT_WATERTIGHT, ISECT_EXACT = 0, 1, 2
 ACCEL_LINEAR, ACCEL_BVH = 0, 1
 PARTITION = {"uniform": 0, "midpoint": 1, "sah": 2}
-RENDER_STATS, RENDER_ACCUMULATE = 1, 2
+RENDER_STATS, RENDER_ACCUMULATE, RENDER_TIMING, RENDER_NO_GRAPH = 1, 2, 4, 8
 
 
 class TransformDesc(C.Structure):
@@ -95,6 +95,7 @@ class Stats(C.Structure):
                 ("object_tests", C.c_uint64), ("object_hits", C.c_uint64), ("bounds_tests", C.c_uint64),
                 ("bounds_hits", C.c_uint64), ("paths", C.c_uint64), ("render_ms", C.c_double),
                 ("extend_ms", C.c_double), ("occlude_ms", C.c_double), ("shade_ms", C.c_double),
+                ("fold_ms", C.c_double),
                 ("kernel_launches", C.c_uint64), ("bvh_nodes", C.c_uint64), ("primitives", C.c_uint64),
                 ("extend_rays", C.c_uint64), ("extend_launches", C.c_uint64), ("extend_box_tests", C.c_uint64),
                 ("extend_prim_tests", C.c_uint64), ("occlude_rays", C.c_uint64), ("occlude_launches", C.c_uint64),

@@ -186,6 +186,14 @@ __device__ __forceinline__ Rng MakeRng(const WaveInfo &w, int path, uint32_t bou
 #define QUEUE_LOOP(j, n)                                                                     \
   for (int j##_base = blockIdx.x * kBlock; j##_base < (n); j##_base += gridDim.x * kBlock)
 
+// Double-buffered arrays are chosen with selects, not by indexing the
+// parameter arrays with a runtime value (which would copy them to local
+// memory).
+template <class T>
+__device__ __forceinline__ T *Pick(T *const (&a)[2], int i) {
+  return i ? a[1] : a[0];
+}
+
 // ---- camera ------------------------------------------------------------
 // Sampler::NextSample (muon/sampling.cc:80-121): sample 0 at the pixel centre,
 // later samples jittered uniformly inside the pixel. Fills bounce 0's queue in
@@ -224,8 +232,8 @@ __global__ void __launch_bounds__(kBlock) CameraKernel(DevCamera cam, WaveInfo w
 template <bool kStats, int kTri>
 __global__ void __launch_bounds__(kBlock) ExtendKernel(DevScene s, PathBuffers b, WaveCounters wc, int bounce) {
   const int n = static_cast<int>(*wc.count(bounce));
-  const float4 *__restrict__ ray_o = b.ray_o[bounce & 1];
-  const float4 *__restrict__ ray_d = b.ray_d[bounce & 1];
+  const float4 *__restrict__ ray_o = Pick(b.ray_o, bounce & 1);
+  const float4 *__restrict__ ray_d = Pick(b.ray_d, bounce & 1);
   TraceCounters c;
   bool overflow = false;
   for (int j = blockIdx.x * kBlock + threadIdx.x; j < n; j += gridDim.x * kBlock) {
@@ -325,15 +333,15 @@ __global__ void __launch_bounds__(kBlock) ShadePathKernel(DevScene s, WaveInfo w
     int path = 0;
     float3 cont_o = f3(0, 0, 0), cont_d = f3(0, 0, 0), cont_tp = f3(0, 0, 0);
     if (active) {
-      const float4 o4 = b.ray_o[cur][jj], d4 = b.ray_d[cur][jj];
+      const float4 o4 = Pick(b.ray_o, cur)[jj], d4 = Pick(b.ray_d, cur)[jj];
       path = __float_as_int(o4.w);
       const float3 o = f3(o4.x, o4.y, o4.z), d = f3(d4.x, d4.y, d4.z);
       const int2 h = b.hits[jj];
       float4 *contrib = b.contrib + static_cast<int64_t>(jj) * S;
       float4 *sdir = b.slot_dir + static_cast<int64_t>(jj) * S;
       for (int k = 0; k < S; ++k) contrib[k] = make_float4(0, 0, 0, 0);
-      float3 L = f3(b.rad[cur][jj]);
-      const float3 tp = f3(b.tp[cur][jj]);
+      float3 L = f3(Pick(b.rad, cur)[jj]);
+      const float3 tp = f3(Pick(b.tp, cur)[jj]);
 
       if (h.y >= 0) {
         float3 p, nrm;
@@ -465,16 +473,16 @@ __global__ void __launch_bounds__(kBlock) ShadePathKernel(DevScene s, WaveInfo w
         }
         if (nshadow) b.org[jj] = make_float4(shift.x, shift.y, shift.z, 0.0f);
       }
-      b.rad[cur][jj] = make_float4(L.x, L.y, L.z, 0.0f);
+      Pick(b.rad, cur)[jj] = make_float4(L.x, L.y, L.z, 0.0f);
     }
 
     uint32_t off_c, off_s;
     BlockReserve(want_cont, nshadow, wc.count(bounce + 1), wc.shadow(bounce), &off_c, &off_s);
     if (active) b.link[jj] = want_cont ? static_cast<int32_t>(off_c) : -1;
     if (want_cont) {
-      b.ray_o[nxt][off_c] = make_float4(cont_o.x, cont_o.y, cont_o.z, __int_as_float(path));
-      b.ray_d[nxt][off_c] = make_float4(cont_d.x, cont_d.y, cont_d.z, INFINITY);
-      b.tp[nxt][off_c] = make_float4(cont_tp.x, cont_tp.y, cont_tp.z, 0.0f);
+      Pick(b.ray_o, nxt)[off_c] = make_float4(cont_o.x, cont_o.y, cont_o.z, __int_as_float(path));
+      Pick(b.ray_d, nxt)[off_c] = make_float4(cont_d.x, cont_d.y, cont_d.z, INFINITY);
+      Pick(b.tp, nxt)[off_c] = make_float4(cont_tp.x, cont_tp.y, cont_tp.z, 0.0f);
     }
     if (nshadow) {
       const uint32_t base = static_cast<uint32_t>(jj) * static_cast<uint32_t>(S);
@@ -505,15 +513,15 @@ __global__ void __launch_bounds__(kBlock) FoldKernel(PathBuffers b, WaveCounters
   const int n = static_cast<int>(*wc.count(bounce));
   const int cur = bounce & 1, nxt = cur ^ 1;
   for (int j = blockIdx.x * kBlock + threadIdx.x; j < n; j += gridDim.x * kBlock) {
-    float4 r = b.rad[cur][j];
+    float4 r = Pick(b.rad, cur)[j];
     const float4 *c = b.contrib + static_cast<int64_t>(j) * slots;
     for (int k = 0; k < slots; ++k) {
       float4 v = c[k];
       r.x += v.x, r.y += v.y, r.z += v.z;
     }
     int next = b.link[j];
-    if (next >= 0) b.rad[nxt][next] = r;
-    else b.final_rad[__float_as_int(b.ray_o[cur][j].w)] = r;
+    if (next >= 0) Pick(b.rad, nxt)[next] = r;
+    else b.final_rad[__float_as_int(Pick(b.ray_o, cur)[j].w)] = r;
   }
 }
 

@@ -293,6 +293,25 @@ int muon_gpu_intersect(MuonScene *scene, const MuonRay *rays, int64_t n, int32_t
 int muon_gpu_occluded(MuonScene *scene, const MuonRay *rays, const float *max_distance, int64_t n,
                       int32_t intersect_mode, uint8_t *occluded);
 
+/* No counterpart in the reference. For callers that must not allocate device
+ * memory while rendering — a host application whose own allocator reserves
+ * the GPU's memory at start-up, or a real-time loop that allocates nothing
+ * after initialisation: renders like muon_gpu_render_device (path tracer or
+ * normals/albedo/depth; same film layout and flags) but takes every byte of
+ * working memory from one fixed buffer of MUON_NOALLOC_SCRATCH_BYTES that the
+ * library declares statically on each GPU it is loaded on, and calls no
+ * cudaMalloc/cudaFree, pinned-host allocation, CUDA graph or event API. The
+ * scene must already exist (muon_gpu_scene_create, which does allocate).
+ * Paths in flight per wavefront are limited to what fits in the buffer
+ * (about MUON_NOALLOC_SCRATCH_BYTES / (172 + 36 * shadow slots per path));
+ * a larger wave_paths is rejected with MUON_ERR_INVALID_ARG. The first call
+ * on a device looks up the buffer's device address. All calls share the one
+ * buffer: calls whose GPU work overlaps (other streams, scenes or threads)
+ * race and corrupt each other's results. muon_gpu_stats is not updated. */
+#define MUON_NOALLOC_SCRATCH_BYTES (64u << 20)
+int muon_gpu_render_noalloc(MuonScene *scene, const MuonRenderParams *params, double *d_sum, double *d_sum_sq,
+                            uint32_t *d_count);
+
 /* Counters and device timings of the last render (muon/stats.h:11-44). */
 int muon_gpu_stats(const MuonScene *scene, MuonStats *stats);
 

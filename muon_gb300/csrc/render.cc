@@ -17,6 +17,7 @@
 
 #include "host_scene.h"
 #include "kernels.cuh"
+#include "scene_access.h"
 #include "scene_build.h"
 
 using namespace muon_gpu;
@@ -672,3 +673,18 @@ int muon_gpu_scene_stream(const MuonScene *scene, void **stream) {
 }
 
 }  // extern "C"
+
+namespace muon_gpu {
+
+bool GetSceneView(const MuonScene *scene, SceneView *out) {
+  if (!scene || !out) return false;
+  out->dev = &scene->dev;
+  out->cam = &scene->cam;
+  out->stream = scene->stream;
+  out->device = scene->device;
+  out->width = scene->img.width;
+  out->height = scene->img.height;
+  return true;
+}
+
+}  // namespace muon_gpu

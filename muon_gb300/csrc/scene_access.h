@@ -1,0 +1,23 @@
+// Read-only view of a MuonScene's device-side state for entry points that
+// live outside render.cc.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "../../include/muon_gpu.h"
+#include "dev_layout.h"
+
+namespace muon_gpu {
+
+struct SceneView {
+  const DevScene *dev;
+  const DevCamera *cam;
+  cudaStream_t stream;
+  int device;
+  int width, height;
+};
+
+// Fills `out` from a scene created by muon_gpu_scene_create; false if null.
+bool GetSceneView(const MuonScene *scene, SceneView *out);
+
+}  // namespace muon_gpu

@@ -22,6 +22,7 @@ ISECT_FAST, ISECT_WATERTIGHT, ISECT_EXACT = 0, 1, 2
 ACCEL_LINEAR, ACCEL_BVH = 0, 1
 PARTITION = {"uniform": 0, "midpoint": 1, "sah": 2}
 RENDER_STATS, RENDER_ACCUMULATE, RENDER_TIMING, RENDER_NO_GRAPH = 1, 2, 4, 8
+NOALLOC_SCRATCH_BYTES = 64 << 20
 
 
 class TransformDesc(C.Structure):
@@ -118,6 +119,8 @@ SIGNATURES = {
     "muon_gpu_render": (C.c_int, [C.c_void_p, C.POINTER(RenderParams), C.POINTER(Film)]),
     "muon_gpu_render_device": (C.c_int, [C.c_void_p, C.POINTER(RenderParams), C.c_void_p, C.c_void_p,
                                          C.c_void_p]),
+    "muon_gpu_render_noalloc": (C.c_int, [C.c_void_p, C.POINTER(RenderParams), C.c_void_p, C.c_void_p,
+                                          C.c_void_p]),
     "muon_gpu_intersect": (C.c_int, [C.c_void_p, C.POINTER(Ray), C.c_int64, C.c_int32, C.POINTER(Hit)]),
     "muon_gpu_occluded": (C.c_int, [C.c_void_p, C.POINTER(Ray), C.POINTER(C.c_float), C.c_int64, C.c_int32,
                                     C.POINTER(C.c_uint8)]),

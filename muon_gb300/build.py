@@ -25,7 +25,7 @@ CUDA_UNITS = ["kernels.cu", "noalloc.cu"]
 HOST_UNITS = ["scene_parser.cc", "scene_build.cc", "host_api.cc", "render.cc"]
 CXXFLAGS = ["-std=c++17", "-O2", "-fPIC", "-ffp-contract=off", "-Wall", "-Wno-unused-function"]
 NVFLAGS = [ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off",
-           "--extended-lambda"]
+           "--extended-lambda"] + os.environ.get("MUON_NVCC_EXTRA", "").split()
 
 
 def _run(cmd: list[str]) -> None:

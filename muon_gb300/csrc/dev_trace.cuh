@@ -311,4 +311,94 @@ __device__ __forceinline__ int Trace(const DevScene &s, float3 o, float3 d, floa
   return hit;
 }
 
+// ---- resumable traversal for persistent kernels ---------------------------
+// The state of one ray's traversal, kept across the refill points of a
+// persistent kernel.
+struct TravState {
+  int node, sp, hit;
+  float tmax, t_obj;
+  int stack[kStackSize];
+};
+
+__device__ __forceinline__ void TravBegin(TravState &t, float tmax) {
+  t.node = 0;
+  t.sp = 0;
+  t.hit = -1;
+  t.tmax = tmax;
+  t.t_obj = 0.0f;
+}
+
+// Advances a traversal (same visiting order and acceptance as Trace). Returns
+// true when the ray is finished; returns false, with the state kept, when
+// fewer than `min_active` lanes of the warp are still traversing, so that the
+// finished lanes can take new rays.
+template <bool kAnyHit, bool kStats, int kTriTest>
+__device__ __forceinline__ bool TravRun(const DevScene &s, const RayPre &r, TravState &t, TraceCounters *cnt,
+                                        bool *overflow, int min_active) {
+  if (s.num_nodes == 0) return true;
+  while (true) {
+    while (t.node >= 0) {
+      const float4 *q = reinterpret_cast<const float4 *>(s.nodes + t.node);
+      float4 n0 = __ldg(q), n1 = __ldg(q + 1), n2 = __ldg(q + 2);
+      int4 n3 = __ldg(reinterpret_cast<const int4 *>(q + 3));
+      float c0lox = n0.x * r.idir.x - r.ood.x, c0hix = n0.y * r.idir.x - r.ood.x;
+      float c0loy = n0.z * r.idir.y - r.ood.y, c0hiy = n0.w * r.idir.y - r.ood.y;
+      float c0loz = n2.x * r.idir.z - r.ood.z, c0hiz = n2.y * r.idir.z - r.ood.z;
+      float c1lox = n1.x * r.idir.x - r.ood.x, c1hix = n1.y * r.idir.x - r.ood.x;
+      float c1loy = n1.z * r.idir.y - r.ood.y, c1hiy = n1.w * r.idir.y - r.ood.y;
+      float c1loz = n2.z * r.idir.z - r.ood.z, c1hiz = n2.w * r.idir.z - r.ood.z;
+      float c0min = fmaxf(fmaxf(fminf(c0lox, c0hix), fminf(c0loy, c0hiy)), fmaxf(fminf(c0loz, c0hiz), 0.0f));
+      float c0max = fminf(fminf(fmaxf(c0lox, c0hix), fmaxf(c0loy, c0hiy)), fminf(fmaxf(c0loz, c0hiz), t.tmax));
+      float c1min = fmaxf(fmaxf(fminf(c1lox, c1hix), fminf(c1loy, c1hiy)), fmaxf(fminf(c1loz, c1hiz), 0.0f));
+      float c1max = fminf(fminf(fmaxf(c1lox, c1hix), fmaxf(c1loy, c1hiy)), fminf(fmaxf(c1loz, c1hiz), t.tmax));
+      bool h0 = c0min <= c0max, h1 = c1min <= c1max;
+      if (kStats) {
+        cnt->box_tests += 2;
+        cnt->box_hits += (int)h0 + (int)h1;
+      }
+      if (!h0 && !h1) {
+        if (t.sp == 0) {
+          t.node = kEmptyLink;
+          break;
+        }
+        t.node = t.stack[--t.sp];
+      } else {
+        int near = h0 ? n3.x : n3.y;
+        if (h0 && h1) {
+          int far = n3.y;
+          if (c1min < c0min) {
+            near = n3.y;
+            far = n3.x;
+          }
+          if (t.sp < kStackSize) t.stack[t.sp++] = far;
+          else *overflow = true;
+        }
+        t.node = near;
+      }
+    }
+    if (t.node == kEmptyLink) return true;
+    int i = ~t.node;
+    const PrimRecord *recs = kTriTest == MUON_ISECT_EXACT ? s.prims_obj : s.prims;
+    while (true) {
+      PrimRecord p = LoadPrim(recs, i);
+      uint32_t flags = __float_as_uint(p.p3.w);
+      float t_obj = 0.0f;
+      float d = PrimTest<kTriTest>(s, r, p, flags, &t_obj);
+      if (kStats) cnt->prim_tests += 1;
+      if (d > 0.0f && d < t.tmax) {
+        if (kStats) cnt->prim_hits += 1;
+        t.tmax = d;
+        t.hit = i;
+        t.t_obj = t_obj;
+        if (kAnyHit) return true;
+      }
+      if (flags & kPrimLast) break;
+      ++i;
+    }
+    if (t.sp == 0) return true;
+    t.node = t.stack[--t.sp];
+    if (__popc(__activemask()) < min_active) return false;
+  }
+}
+
 }  // namespace muon_gpu

@@ -229,6 +229,50 @@ __global__ void __launch_bounds__(kBlock) CameraKernel(DevCamera cam, WaveInfo w
 }
 
 // ---- extend / occlude ------------------------------------------------------
+// Persistent traversal: each warp takes rays from a per-launch counter, 32 at
+// a time, and a lane whose ray is done takes the next one as soon as fewer
+// than kRefillThreshold lanes of its warp are still traversing, so warps stay
+// full while the work per ray varies (dynamic fetch, after Aila and Laine,
+// "Understanding the Efficiency of Ray Traversal on GPUs", HPG 2009).
+constexpr int kRefillThreshold = 20;
+
+template <bool kAnyHit, bool kStats, int kMode, class Load, class Finish>
+__device__ __forceinline__ void PersistentTraverse(const DevScene &s, int n, uint32_t *fetch, Load load,
+                                                   Finish finish, TraceCounters &c, bool &overflow) {
+  const int lane = threadIdx.x & 31;
+  int ray = -1;
+  bool exhausted = false;
+  RayPre r;
+  TravState t;
+  while (true) {
+    const unsigned need = __ballot_sync(0xffffffffu, ray < 0 && !exhausted);
+    if (need) {
+      const int leader = __ffs(need) - 1;
+      uint32_t base = 0;
+      if (lane == leader) base = atomicAdd(fetch, static_cast<uint32_t>(__popc(need)));
+      base = __shfl_sync(0xffffffffu, base, leader);
+      if (ray < 0 && !exhausted) {
+        const uint32_t mine = base + static_cast<uint32_t>(__popc(need & ((1u << lane) - 1u)));
+        if (mine < static_cast<uint32_t>(n)) {
+          ray = static_cast<int>(mine);
+          float3 o, d;
+          float tmax;
+          load(ray, &o, &d, &tmax);
+          r = Prepare<kMode>(o, d);
+          TravBegin(t, tmax);
+        } else {
+          exhausted = true;
+        }
+      }
+    }
+    if (!__any_sync(0xffffffffu, ray >= 0)) break;
+    if (ray >= 0 && TravRun<kAnyHit, kStats, kMode>(s, r, t, &c, &overflow, kRefillThreshold)) {
+      finish(ray, t);
+      ray = -1;
+    }
+  }
+}
+
 template <bool kStats, int kTri>
 __global__ void __launch_bounds__(kBlock) ExtendKernel(DevScene s, PathBuffers b, WaveCounters wc, int bounce) {
   const int n = static_cast<int>(*wc.count(bounce));
@@ -236,13 +280,18 @@ __global__ void __launch_bounds__(kBlock) ExtendKernel(DevScene s, PathBuffers b
   const float4 *__restrict__ ray_d = Pick(b.ray_d, bounce & 1);
   TraceCounters c;
   bool overflow = false;
-  for (int j = blockIdx.x * kBlock + threadIdx.x; j < n; j += gridDim.x * kBlock) {
-    float4 o4 = ray_o[j], d4 = ray_d[j];
-    float t, t_obj = 0.0f;
-    int h = Trace<false, kStats, kTri>(s, f3(o4.x, o4.y, o4.z), f3(d4.x, d4.y, d4.z), d4.w, &t, &c, &overflow,
-                                       &t_obj);
-    b.hits[j] = make_int2(__float_as_int(kTri == MUON_ISECT_EXACT ? t_obj : t), h);
-  }
+  PersistentTraverse<false, kStats, kTri>(
+      s, n, wc.fetch_extend(bounce),
+      [&](int j, float3 *o, float3 *d, float *tmax) {
+        float4 o4 = ray_o[j], d4 = ray_d[j];
+        *o = f3(o4.x, o4.y, o4.z);
+        *d = f3(d4.x, d4.y, d4.z);
+        *tmax = d4.w;
+      },
+      [&](int j, const TravState &t) {
+        b.hits[j] = make_int2(__float_as_int(kTri == MUON_ISECT_EXACT ? t.t_obj : t.tmax), t.hit);
+      },
+      c, overflow);
   if (kStats) {
     AddStat(b.stats, kStatBoxTests, c.box_tests);
     AddStat(b.stats, kStatBoxHits, c.box_hits);
@@ -260,13 +309,19 @@ __global__ void __launch_bounds__(kBlock) OccludeKernel(DevScene s, PathBuffers 
   const int n = static_cast<int>(*wc.shadow(bounce));
   TraceCounters c;
   bool overflow = false;
-  for (int j = blockIdx.x * kBlock + threadIdx.x; j < n; j += gridDim.x * kBlock) {
-    uint32_t slot = b.shq[j];
-    float4 o4 = b.org[slot / slots], d4 = b.slot_dir[slot];
-    float t;
-    int h = Trace<true, kStats, kTri>(s, f3(o4.x, o4.y, o4.z), f3(d4.x, d4.y, d4.z), d4.w, &t, &c, &overflow);
-    if (h >= 0) b.contrib[slot] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-  }
+  PersistentTraverse<true, kStats, kTri>(
+      s, n, wc.fetch_occlude(bounce),
+      [&](int j, float3 *o, float3 *d, float *tmax) {
+        uint32_t slot = b.shq[j];
+        float4 o4 = b.org[slot / slots], d4 = b.slot_dir[slot];
+        *o = f3(o4.x, o4.y, o4.z);
+        *d = f3(d4.x, d4.y, d4.z);
+        *tmax = d4.w;
+      },
+      [&](int j, const TravState &t) {
+        if (t.hit >= 0) b.contrib[b.shq[j]] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+      },
+      c, overflow);
   if (kStats) {
     AddStat(b.stats, kStatOccBoxTests, c.box_tests);
     AddStat(b.stats, kStatOccBoxHits, c.box_hits);
@@ -317,9 +372,14 @@ __global__ void __launch_bounds__(kBlock) ShadeDebugKernel(DevScene s, PathBuffe
 // compacted shadow queue as slot indices, continuing paths to the next
 // bounce's queue (with their throughput and a link from this entry).
 constexpr int kMaskSlots = 64;
+// Minimum resident blocks per SM the shading kernel is compiled for (sets its
+// register budget: 2 -> up to 128 registers, 3 -> 80).
+#ifndef MUON_SHADE_MIN_BLOCKS
+#define MUON_SHADE_MIN_BLOCKS 2
+#endif
 
 template <int kMode>
-__global__ void __launch_bounds__(kBlock) ShadePathKernel(DevScene s, WaveInfo w, ShadeParams sp, PathBuffers b,
+__global__ void __launch_bounds__(kBlock, MUON_SHADE_MIN_BLOCKS) ShadePathKernel(DevScene s, WaveInfo w, ShadeParams sp, PathBuffers b,
                                                           WaveCounters wc, int bounce) {
   const int n = static_cast<int>(*wc.count(bounce));
   const int cur = bounce & 1, nxt = cur ^ 1;
@@ -594,10 +654,15 @@ __global__ void __launch_bounds__(kBlock) OccludedRaysKernel(DevScene s, const f
 inline unsigned Blocks(int64_t n) { return static_cast<unsigned>((n + kBlock - 1) / kBlock); }
 
 int g_persistent_blocks = 152 * 8;
+int g_traversal_blocks = 152 * 4;
 
 // Grid for a device-counted launch whose queue holds at most `bound` entries.
 inline unsigned CountedBlocks(int64_t bound) {
   return static_cast<unsigned>(std::max<int64_t>(1, std::min<int64_t>(Blocks(bound), g_persistent_blocks)));
+}
+
+inline unsigned TraversalBlocks(int64_t bound) {
+  return static_cast<unsigned>(std::max<int64_t>(1, std::min<int64_t>(Blocks(bound), g_traversal_blocks)));
 }
 
 // Calls f(std::integral_constant<int, mode>) for a runtime intersection mode.
@@ -612,6 +677,17 @@ void WithMode(int mode, F &&f) {
 
 void SetPersistentGrid(int blocks) { g_persistent_blocks = std::max(1, blocks); }
 
+void SetTraversalGrid(int sms) {
+  // Enough resident blocks to fill every SM once; the persistent traversal
+  // kernels hand out rays themselves.
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, ExtendKernel<false, MUON_ISECT_EXACT>, kBlock, 0) !=
+          cudaSuccess ||
+      per_sm < 1)
+    per_sm = 4;
+  g_traversal_blocks = std::max(1, sms * per_sm);
+}
+
 void LaunchCamera(const DevCamera &cam, const WaveInfo &w, const PathBuffers &b, WaveCounters wc, cudaStream_t st) {
   CameraKernel<<<Blocks(std::max(w.n, 1)), kBlock, 0, st>>>(cam, w, b, wc);
 }
@@ -621,8 +697,9 @@ void LaunchExtend(const DevScene &s, const PathBuffers &b, WaveCounters wc, int 
   if (bound <= 0) return;
   WithMode(isect, [&](auto m) {
     constexpr int M = decltype(m)::value;
-    if (stats) ExtendKernel<true, M><<<CountedBlocks(bound), kBlock, 0, st>>>(s, b, wc, bounce);
-    else ExtendKernel<false, M><<<CountedBlocks(bound), kBlock, 0, st>>>(s, b, wc, bounce);
+    const unsigned g = TraversalBlocks(bound);
+    if (stats) ExtendKernel<true, M><<<g, kBlock, 0, st>>>(s, b, wc, bounce);
+    else ExtendKernel<false, M><<<g, kBlock, 0, st>>>(s, b, wc, bounce);
   });
 }
 
@@ -647,8 +724,9 @@ void LaunchOcclude(const DevScene &s, const PathBuffers &b, WaveCounters wc, int
   if (bound <= 0 || slots <= 0) return;
   WithMode(isect, [&](auto m) {
     constexpr int M = decltype(m)::value;
-    if (stats) OccludeKernel<true, M><<<CountedBlocks(bound), kBlock, 0, st>>>(s, b, wc, bounce, slots);
-    else OccludeKernel<false, M><<<CountedBlocks(bound), kBlock, 0, st>>>(s, b, wc, bounce, slots);
+    const unsigned g = TraversalBlocks(bound);
+    if (stats) OccludeKernel<true, M><<<g, kBlock, 0, st>>>(s, b, wc, bounce, slots);
+    else OccludeKernel<false, M><<<g, kBlock, 0, st>>>(s, b, wc, bounce, slots);
   });
 }
 

@@ -44,9 +44,14 @@ struct WaveInfo {
 // shadow(k) = shadow rays emitted at bounce k.
 struct WaveCounters {
   uint32_t *c;
-  __host__ __device__ uint32_t *count(int k) const { return c + 2 * k; }
-  __host__ __device__ uint32_t *shadow(int k) const { return c + 2 * k + 1; }
+  __host__ __device__ uint32_t *count(int k) const { return c + 4 * k; }
+  __host__ __device__ uint32_t *shadow(int k) const { return c + 4 * k + 1; }
+  // rays handed out so far by the persistent traversal kernels of bounce k
+  __host__ __device__ uint32_t *fetch_extend(int k) const { return c + 4 * k + 2; }
+  __host__ __device__ uint32_t *fetch_occlude(int k) const { return c + 4 * k + 3; }
 };
+// Words of one wavefront's counter block for `bounces` bounces.
+inline size_t WaveCounterWords(int bounces) { return 4 * static_cast<size_t>(bounces + 2); }
 
 // Path state lives in queue order: entry j of bounce k's queue holds its ray,
 // hit, throughput and radiance at index j, so every per-path access in the
@@ -82,8 +87,10 @@ struct ShadeParams {
 };
 
 // Upper bound on the blocks of the device-counted launches (they loop over
-// their queue with a grid stride); set from the SM count at scene creation.
+// their queue with a grid stride), and the block count of the persistent
+// traversal kernels; set from the SM count at scene creation.
 void SetPersistentGrid(int blocks);
+void SetTraversalGrid(int sms);
 
 void LaunchCamera(const DevCamera &cam, const WaveInfo &w, const PathBuffers &b, WaveCounters wc, cudaStream_t st);
 void LaunchExtend(const DevScene &s, const PathBuffers &b, WaveCounters wc, int bounce, int bound, int isect,

@@ -95,7 +95,7 @@ size_t BytesFor(int64_t paths, int slots, int bounces) {
   c.Take<float4>(sl);
   c.Take<float4>(sl);
   c.Take<uint32_t>(sl);
-  c.Take<uint32_t>(2 * static_cast<size_t>(bounces + 2));
+  c.Take<uint32_t>(WaveCounterWords(bounces));
   c.Take<unsigned long long>(kNumStats);
   return c.used;
 }
@@ -177,7 +177,7 @@ extern "C" int muon_gpu_render_noalloc(MuonScene *scene, const MuonRenderParams 
   b.contrib = c.Take<float4>(sl);
   b.slot_dir = c.Take<float4>(sl);
   b.shq = c.Take<uint32_t>(sl);
-  const size_t stride = 2 * static_cast<size_t>(bounces + 2);
+  const size_t stride = WaveCounterWords(bounces);
   uint32_t *counters = c.Take<uint32_t>(stride);
   b.stats = c.Take<unsigned long long>(kNumStats);
 

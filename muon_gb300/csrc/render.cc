@@ -24,7 +24,7 @@ using namespace muon_gpu;
 
 namespace {
 
-constexpr int kDefaultWavePaths = 1 << 21;
+constexpr int kDefaultWavePaths = 1 << 24;
 constexpr int kMaxBounces = 256;  // hard cap for unbounded depth without Russian roulette
 constexpr int kMaxEventPairs = 16384;
 
@@ -285,9 +285,9 @@ void RenderDevice(MuonScene *sc, const MuonRenderParams &p, double *d_sum, doubl
   const int64_t npix_total = static_cast<int64_t>(W) * H;
   const int spp = p.pixel_samples;
   int64_t budget = p.wave_paths > 0 ? p.wave_paths : kDefaultWavePaths;
-  // Keep per-wave slot storage within ~4 GiB.
+  // Keep per-wave path state within ~8 GiB.
   const int64_t per_path = 200 + 36 * static_cast<int64_t>(std::max(slots, 1));
-  budget = std::max<int64_t>(1, std::min<int64_t>(budget, (int64_t(4) << 30) / per_path));
+  budget = std::max<int64_t>(1, std::min<int64_t>(budget, (int64_t(8) << 30) / per_path));
   const int ns = static_cast<int>(std::min<int64_t>(spp, budget));
   const int64_t pix_per_wave = std::max<int64_t>(1, budget / ns);
   std::vector<WaveInfo> waves;
@@ -310,7 +310,7 @@ void RenderDevice(MuonScene *sc, const MuonRenderParams &p, double *d_sum, doubl
   const bool traces = !(p.max_depth >= 0 && sp.max_trace_depth < 0);
   const bool bounded = !pt || sp.max_trace_depth >= 0;
   const int bounces = !traces ? 0 : (!pt ? 1 : (bounded ? sp.max_trace_depth + 1 : kMaxBounces));
-  const size_t stride = 2 * static_cast<size_t>(bounces + 2);
+  const size_t stride = WaveCounterWords(bounces);
   bool moved = sc->EnsureWork(std::min<int64_t>(pix_per_wave, npix_total) * ns, slots);
   moved |= sc->EnsureCounters(stride * waves.size());
   sc->stats.Ensure(sizeof(unsigned long long) * kNumStats);
@@ -413,10 +413,11 @@ void RenderDevice(MuonScene *sc, const MuonRenderParams &p, double *d_sum, doubl
   for (size_t wi = 0; wi < waves.size(); ++wi) {
     const uint32_t *c = sc->h_counters + wi * stride;
     if (traces) primary += static_cast<uint64_t>(waves[wi].n);
+    WaveCounters hc{const_cast<uint32_t *>(c)};
     for (int k = 0; k < bounces; ++k) {
-      ext_rays += c[2 * k];
-      shadow += c[2 * k + 1];
-      if (c[2 * k] > 0) {
+      ext_rays += *hc.count(k);
+      shadow += *hc.shadow(k);
+      if (*hc.count(k) > 0) {
         ++ext_launches;
         if (slots > 0) ++occ_launches;
       }
@@ -479,6 +480,7 @@ int muon_gpu_scene_create(const MuonSceneDesc *desc, MuonScene **out) {
     int sms = 0;
     CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, sc->device));
     SetPersistentGrid(sms * 8);
+    SetTraversalGrid(sms);
     CUDA_TRY(cudaStreamCreateWithFlags(&sc->stream, cudaStreamNonBlocking));
     cudaStream_t st = sc->stream;
     const SceneImage &im = sc->img;

@@ -391,9 +391,15 @@ bool BuildSceneImage(const MuonSceneDesc &desc, SceneImage *img, std::string *er
       return false;
     }
     DevMaterial &d = img->materials[i];
+    // Phong with a zero specular colour is the Lambertian BRDF: its lobe
+    // probability is 0 and its specular term and density vanish
+    // (muon/materials.cc:85-123), so the kernels take the shorter path.
+    int32_t brdf = m.brdf;
+    if (brdf == MUON_BRDF_PHONG && m.specular[0] == 0.0f && m.specular[1] == 0.0f && m.specular[2] == 0.0f)
+      brdf = MUON_BRDF_LAMBERTIAN;
     d.diffuse = MakeF4(m.diffuse[0], m.diffuse[1], m.diffuse[2], m.shininess);
     d.specular = MakeF4(m.specular[0], m.specular[1], m.specular[2], m.roughness);
-    d.emission = MakeF4(m.emission[0], m.emission[1], m.emission[2], IntBits(m.brdf));
+    d.emission = MakeF4(m.emission[0], m.emission[1], m.emission[2], IntBits(brdf));
     d.ambient = MakeF4(m.ambient[0], m.ambient[1], m.ambient[2], Reflectiveness(m));
   }
   // Lights: quad lights feed NEE/MIS; the others only the ray tracer.

@@ -303,7 +303,7 @@ int muon_gpu_occluded(MuonScene *scene, const MuonRay *rays, const float *max_di
  * cudaMalloc/cudaFree, pinned-host allocation, CUDA graph or event API. The
  * scene must already exist (muon_gpu_scene_create, which does allocate).
  * Paths in flight per wavefront are limited to what fits in the buffer
- * (about MUON_NOALLOC_SCRATCH_BYTES / (172 + 36 * shadow slots per path));
+ * (about MUON_NOALLOC_SCRATCH_BYTES / (196 + 36 * shadow slots per path));
  * a larger wave_paths is rejected with MUON_ERR_INVALID_ARG. The first call
  * on a device looks up the buffer's device address. All calls share the one
  * buffer: calls whose GPU work overlaps (other streams, scenes or threads)

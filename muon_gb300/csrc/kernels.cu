@@ -290,6 +290,22 @@ __global__ void __launch_bounds__(kBlock) ExtendKernel(DevScene s, PathBuffers b
       },
       [&](int j, const TravState &t) {
         b.hits[j] = make_int2(__float_as_int(kTri == MUON_ISECT_EXACT ? t.t_obj : t.tmax), t.hit);
+        // Group hits by shading class for the shading kernel (one atomic per
+        // class per group of lanes finishing together); a miss ends its path.
+        int cls = kNumClasses;
+        if (t.hit >= 0) cls = (__ldg(&s.shade[t.hit].s1.w) >> kClassShift) & 7;
+        const unsigned active = __activemask();
+        const unsigned peers = __match_any_sync(active, cls);
+        const int lane = threadIdx.x & 31;
+        const int leader = __ffs(peers) - 1;
+        if (cls < kNumClasses) {
+          uint32_t pos = 0;
+          if (lane == leader) pos = atomicAdd(wc.classes(bounce) + cls, static_cast<uint32_t>(__popc(peers)));
+          pos = __shfl_sync(peers, pos, leader) + static_cast<uint32_t>(__popc(peers & ((1u << lane) - 1u)));
+          b.order[static_cast<int64_t>(cls) * b.order_cap + pos] = j;
+        } else {
+          b.link[j] = -1;
+        }
       },
       c, overflow);
   if (kStats) {
@@ -381,13 +397,31 @@ constexpr int kMaskSlots = 64;
 template <int kMode>
 __global__ void __launch_bounds__(kBlock, MUON_SHADE_MIN_BLOCKS) ShadePathKernel(DevScene s, WaveInfo w, ShadeParams sp, PathBuffers b,
                                                           WaveCounters wc, int bounce) {
-  const int n = static_cast<int>(*wc.count(bounce));
+  // Hits of this bounce, grouped by shading class: position i of the
+  // concatenated class lists is entry order[c * cap + (i - start[c])].
+  __shared__ uint32_t class_start[kNumClasses + 1];
+  if (threadIdx.x == 0) {
+    uint32_t acc = 0;
+    for (int c = 0; c < kNumClasses; ++c) {
+      class_start[c] = acc;
+      acc += wc.classes(bounce)[c];
+    }
+    class_start[kNumClasses] = acc;
+  }
+  __syncthreads();
+  const int n = static_cast<int>(class_start[kNumClasses]);
   const int cur = bounce & 1, nxt = cur ^ 1;
   const int S = sp.slots;
   unsigned long long counted = 0;  // secondary rays in the reference's sense
   QUEUE_LOOP(j, n) {
-    const int jj = j_base + threadIdx.x;
-    const bool active = jj < n;
+    const int ii = j_base + threadIdx.x;
+    const bool active = ii < n;
+    int jj = 0;
+    if (active) {
+      int c = 0;
+      while (c + 1 < kNumClasses && static_cast<uint32_t>(ii) >= class_start[c + 1]) ++c;
+      jj = b.order[static_cast<int64_t>(c) * b.order_cap + (ii - static_cast<int>(class_start[c]))];
+    }
     uint32_t want_cont = 0, nshadow = 0;
     unsigned long long mask = 0;  // nonzero slots (first 64)
     int path = 0;
@@ -574,10 +608,13 @@ __global__ void __launch_bounds__(kBlock) FoldKernel(PathBuffers b, WaveCounters
   const int cur = bounce & 1, nxt = cur ^ 1;
   for (int j = blockIdx.x * kBlock + threadIdx.x; j < n; j += gridDim.x * kBlock) {
     float4 r = Pick(b.rad, cur)[j];
-    const float4 *c = b.contrib + static_cast<int64_t>(j) * slots;
-    for (int k = 0; k < slots; ++k) {
-      float4 v = c[k];
-      r.x += v.x, r.y += v.y, r.z += v.z;
+    // Only shaded entries (hits) wrote shadow slots this bounce.
+    if (b.hits[j].y >= 0) {
+      const float4 *c = b.contrib + static_cast<int64_t>(j) * slots;
+      for (int k = 0; k < slots; ++k) {
+        float4 v = c[k];
+        r.x += v.x, r.y += v.y, r.z += v.z;
+      }
     }
     int next = b.link[j];
     if (next >= 0) Pick(b.rad, nxt)[next] = r;

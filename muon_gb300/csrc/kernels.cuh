@@ -44,14 +44,16 @@ struct WaveInfo {
 // shadow(k) = shadow rays emitted at bounce k.
 struct WaveCounters {
   uint32_t *c;
-  __host__ __device__ uint32_t *count(int k) const { return c + 4 * k; }
-  __host__ __device__ uint32_t *shadow(int k) const { return c + 4 * k + 1; }
+  __host__ __device__ uint32_t *count(int k) const { return c + 16 * k; }
+  __host__ __device__ uint32_t *shadow(int k) const { return c + 16 * k + 1; }
   // rays handed out so far by the persistent traversal kernels of bounce k
-  __host__ __device__ uint32_t *fetch_extend(int k) const { return c + 4 * k + 2; }
-  __host__ __device__ uint32_t *fetch_occlude(int k) const { return c + 4 * k + 3; }
+  __host__ __device__ uint32_t *fetch_extend(int k) const { return c + 16 * k + 2; }
+  __host__ __device__ uint32_t *fetch_occlude(int k) const { return c + 16 * k + 3; }
+  // hits of bounce k per shading class (kNumClasses entries)
+  __host__ __device__ uint32_t *classes(int k) const { return c + 16 * k + 4; }
 };
 // Words of one wavefront's counter block for `bounces` bounces.
-inline size_t WaveCounterWords(int bounces) { return 4 * static_cast<size_t>(bounces + 2); }
+inline size_t WaveCounterWords(int bounces) { return 16 * static_cast<size_t>(bounces + 2); }
 
 // Path state lives in queue order: entry j of bounce k's queue holds its ray,
 // hit, throughput and radiance at index j, so every per-path access in the
@@ -70,6 +72,8 @@ struct PathBuffers {
   float4 *contrib;    // S slots per queue entry: radiance if unblocked
   float4 *slot_dir;   // S slots per queue entry: (direction, max distance)
   uint32_t *shq;      // shadow queue: slot indices (entry * S + slot)
+  int32_t *order;     // hit entries grouped by shading class: class c at c * order_cap
+  int32_t order_cap;  // entries per class (the wavefront size)
   unsigned long long *stats;
 };
 

@@ -18,7 +18,7 @@
 //
 // Limits and rules:
 //  * Paths in flight per wavefront are capped by the buffer: at most
-//    kScratchBytes / (172 + 36 * S) paths, S = shadow slots per path. A
+//    kScratchBytes / (196 + 36 * S) paths, S = shadow slots per path. A
 //    requested wave_paths above that, or a scene whose S leaves room for fewer
 //    than 256 paths, is rejected with MUON_ERR_INVALID_ARG.
 //  * Every call reuses the same buffer and leaves its contents behind; the
@@ -95,6 +95,7 @@ size_t BytesFor(int64_t paths, int slots, int bounces) {
   c.Take<float4>(sl);
   c.Take<float4>(sl);
   c.Take<uint32_t>(sl);
+  c.Take<int32_t>(static_cast<size_t>(paths) * kNumClasses);
   c.Take<uint32_t>(WaveCounterWords(bounces));
   c.Take<unsigned long long>(kNumStats);
   return c.used;
@@ -148,7 +149,7 @@ extern "C" int muon_gpu_render_noalloc(MuonScene *scene, const MuonRenderParams 
   const int bounces = !traces ? 0 : (!pt ? 1 : (bounded ? sp.max_trace_depth + 1 : kNoAllocMaxBounces));
 
   // Paths per wavefront that fit the buffer.
-  int64_t capacity = static_cast<int64_t>(kScratchBytes / (172 + 36 * static_cast<size_t>(std::max(slots, 1))));
+  int64_t capacity = static_cast<int64_t>(kScratchBytes / (196 + 36 * static_cast<size_t>(std::max(slots, 1))));
   capacity &= ~int64_t(255);
   while (capacity > 0 && BytesFor(capacity, slots, bounces) > kScratchBytes) capacity -= 256;
   if (capacity < 256)
@@ -177,6 +178,8 @@ extern "C" int muon_gpu_render_noalloc(MuonScene *scene, const MuonRenderParams 
   b.contrib = c.Take<float4>(sl);
   b.slot_dir = c.Take<float4>(sl);
   b.shq = c.Take<uint32_t>(sl);
+  b.order = c.Take<int32_t>(static_cast<size_t>(budget) * kNumClasses);
+  b.order_cap = static_cast<int32_t>(budget);
   const size_t stride = WaveCounterWords(bounces);
   uint32_t *counters = c.Take<uint32_t>(stride);
   b.stats = c.Take<unsigned long long>(kNumStats);

@@ -84,7 +84,8 @@ struct MuonScene {
   DeviceBuffer nodes, prims, prims_obj, shade, smooth, smooth_obj, transforms, materials, lights, light_tris,
       light_tris_obj, light_tri_ok, other_lights;
   // work arrays
-  DeviceBuffer ray_o[2], ray_d[2], tp[2], rad[2], hits, link, final_rad, org, contrib, slot_dir, shq, counters, stats;
+  DeviceBuffer ray_o[2], ray_d[2], tp[2], rad[2], hits, link, final_rad, org, contrib, slot_dir, shq, order, counters,
+      stats;
   DeviceBuffer film_sum, film_sq, film_cnt, ray_in, ray_out, ray_aux;
   int64_t wave_cap = 0;
   int slots_cap = -1;
@@ -138,6 +139,8 @@ struct MuonScene {
     b.contrib = contrib.as<float4>();
     b.slot_dir = slot_dir.as<float4>();
     b.shq = shq.as<uint32_t>();
+    b.order = order.as<int32_t>();
+    b.order_cap = static_cast<int32_t>(wave_cap);
     b.stats = stats.as<unsigned long long>();
     return b;
   }
@@ -161,6 +164,7 @@ struct MuonScene {
     contrib.Ensure(sl * sizeof(float4));
     slot_dir.Ensure(sl * sizeof(float4));
     shq.Ensure(sl * sizeof(uint32_t));
+    order.Ensure(static_cast<size_t>(p) * kNumClasses * sizeof(int32_t));
     wave_cap = p;
     slots_cap = s;
     return true;

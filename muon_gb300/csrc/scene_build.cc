@@ -487,7 +487,10 @@ bool BuildSceneImage(const MuonSceneDesc &desc, SceneImage *img, std::string *er
     mm::v3 un = mm::xform_dir(nt0, mm::normalize(n_obj));
     ShadeRecord &s = tri_shade[i];
     s.s0 = MakeF4(un.x, un.y, un.z, IntBits(t.material));
-    s.s1 = I4{t.light >= 0 ? quad_index[t.light] : -1, t.prim_id, t.transform, static_cast<int32_t>(flags)};
+    int32_t brdf_eff;
+    std::memcpy(&brdf_eff, &img->materials[t.material].emission.w, 4);
+    const uint32_t shade_flags = flags | (static_cast<uint32_t>(brdf_eff) << kClassShift);
+    s.s1 = I4{t.light >= 0 ? quad_index[t.light] : -1, t.prim_id, t.transform, static_cast<int32_t>(shade_flags)};
     std::memcpy(&r.p3.w, &flags, 4);
     ro.p3 = r.p3;
     ro.p3.x = n_obj.x, ro.p3.y = n_obj.y, ro.p3.z = n_obj.z;
@@ -533,7 +536,10 @@ bool BuildSceneImage(const MuonSceneDesc &desc, SceneImage *img, std::string *er
     std::memcpy(&r.p3.w, &flags, 4);
     ShadeRecord &sh = sph_shade[j];
     sh.s0 = MakeF4(0, 0, 0, IntBits(s.material));
-    sh.s1 = I4{-1, s.prim_id, s.transform, static_cast<int32_t>(flags)};
+    int32_t sph_brdf;
+    std::memcpy(&sph_brdf, &img->materials[s.material].emission.w, 4);
+    const uint32_t sph_flags = flags | (static_cast<uint32_t>(3 + sph_brdf) << kClassShift);
+    sh.s1 = I4{-1, s.prim_id, s.transform, static_cast<int32_t>(sph_flags)};
     // World bounds: the object box's 8 corners transformed (Bounds::Transform,
     // muon/bounds.cc:52-69).
     mm::v3 c = V3(s.center);

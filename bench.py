@@ -13,6 +13,12 @@ the MIS-sampled ray included; shadow rays excluded, muon/integration.cc:34-38,
 upload (BVH build + copy) and the host film read-back inside every step.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                  [--workload sphere_field|dense_mesh]
+
+`--workload dense_mesh` measures the traversal-bound scene instead: a
+1,310,720-triangle displaced icosphere (GGX roughness 0.15) and 10,000 small
+clutter triangles in the Cornell box, 1024x1024, 256 spp, max depth 10, NEE
+with MIS (muon_gb300.scenes.dense_mesh).
 
 With N > 1 (torchrun), every rank renders its own replica of the frame with a
 distinct seed (weak scaling; the FP64 films of replicas merge by addition).
@@ -33,8 +39,15 @@ import time
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-WORKLOAD = {"workload": "sphere_field", "spheres": 512, "width": 512, "height": 512, "spp": 64, "max_depth": 8,
-            "nee": "mis", "importance_sampling": "brdf", "seed": 1}
+WORKLOADS = {
+    # the headline workload
+    "sphere_field": {"workload": "sphere_field", "spheres": 512, "width": 512, "height": 512, "spp": 64,
+                     "max_depth": 8, "nee": "mis", "importance_sampling": "brdf", "seed": 1},
+    # traversal-bound: 1,310,720-triangle displaced icosphere (level 8) + 10k clutter triangles in the Cornell box
+    "dense_mesh": {"workload": "dense_mesh", "triangles": 1320756, "width": 1024, "height": 1024, "spp": 256,
+                   "max_depth": 10, "nee": "mis", "importance_sampling": "brdf", "seed": 1},
+}
+WORKLOAD = dict(WORKLOADS["sphere_field"])
 METRIC = "Mrays/s"
 
 
@@ -42,6 +55,8 @@ def scene_text() -> str:
     from muon_gb300 import scenes
 
     w = WORKLOAD
+    if w["workload"] == "dense_mesh":
+        return scenes.dense_mesh(w["width"], w["height"], w["spp"], w["max_depth"], seed=w["seed"])
     return scenes.sphere_field(w["width"], w["height"], w["spp"], w["max_depth"], w["spheres"], w["seed"], w["nee"])
 
 
@@ -231,13 +246,13 @@ def run_ours(args) -> None:
     traffic = None
     tpath = os.path.join(ROOT, "profiles", "traffic.json")
     if os.path.exists(tpath):
-        traffic = json.load(open(tpath)).get(dom)
+        traffic = json.load(open(tpath)).get(WORKLOAD["workload"], {}).get(dom)
 
     cpu = cpu_baseline(text) if world == 1 else None
     line = {
         "metric": METRIC, "value": round(value, 2), "unit": METRIC, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(dev_ms_max / args.steps, 4), "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded sphere field)",
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": f"synthetic (seeded {WORKLOAD['workload'].replace('_', ' ')})",
         "config": dict(WORKLOAD, parallelism=f"replicas{world}", intersect_mode="exact",
                        l2="flushed between steps (256 MiB write)", counted_rays_per_step=counted // args.steps),
         "e2e": {"value": round(e2e_value, 2), "unit": METRIC, "h2d_bytes_per_step": int(desc_bytes),
@@ -282,11 +297,12 @@ def reference_rate(text: str, spp: int, threads: int) -> tuple[float, float, str
 
 def cpu_baseline(text: str) -> dict:
     threads = os.cpu_count() or 1
+    w, h = WORKLOAD["width"], WORKLOAD["height"]
     rate1, el1, kind = reference_rate(text, 1, threads)
-    spp = max(1, min(64, int(10.0 / max(el1, 1e-3))))
+    spp = max(1, min(WORKLOAD["spp"], int(10.0 / max(el1, 1e-3))))
     rate, el, kind = reference_rate(text, spp, threads)
     return {"value": round(rate, 3), "unit": METRIC, "cores": threads, "kind": kind,
-            "sample": f"full 512x512 frame at {spp} spp (of 64), {el:.1f} s on {threads} threads"}
+            "sample": f"full {w}x{h} frame at {spp} spp (of {WORKLOAD['spp']}), {el:.1f} s on {threads} threads"}
 
 
 def run_reference(args) -> None:
@@ -300,7 +316,7 @@ def run_reference(args) -> None:
     text = scene_text()
     threads = os.cpu_count() or 1
     rate1, el1, kind = reference_rate(text, 1, threads)
-    spp = max(1, min(64, int(5.0 / max(el1, 1e-3))))
+    spp = max(1, min(WORKLOAD["spp"], int(5.0 / max(el1, 1e-3))))
     for _ in range(args.warmup):
         reference_rate(text, 1, threads)
     rates, times = [], []
@@ -312,10 +328,11 @@ def run_reference(args) -> None:
     line = {"metric": METRIC, "value": round(value, 3), "unit": METRIC, "impl": "reference", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * sum(times) / len(times), 1),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-            "data": "synthetic (seeded sphere field)",
+            "data": f"synthetic (seeded {WORKLOAD['workload'].replace('_', ' ')})",
             "config": dict(WORKLOAD, parallelism=f"host threads {threads}"),
             "cpu_baseline": {"value": round(value, 3), "unit": METRIC, "cores": threads, "kind": kind,
-                             "sample": f"full 512x512 frame at {spp} spp (of 64) per step"},
+                             "sample": f"full {WORKLOAD['width']}x{WORKLOAD['height']} frame at {spp} spp "
+                                       f"(of {WORKLOAD['spp']}) per step"},
             "e2e": {"value": round(value, 3), "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -326,7 +343,10 @@ def main() -> None:
     ap.add_argument("--steps", type=int, default=60)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="sphere_field")
     a = ap.parse_args()
+    WORKLOAD.clear()
+    WORKLOAD.update(WORKLOADS[a.workload])
     if a.warmup < 3:
         a.warmup = 3
     if a.impl == "reference":

@@ -17,9 +17,11 @@
 #include "scene_build.h"
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstring>
 #include <limits>
+#include <thread>
 
 namespace muon_gpu {
 
@@ -29,9 +31,12 @@ constexpr int kBins = 32;
 constexpr float kTraversalCost = 1.0f;
 constexpr float kIntersectCost = 1.0f;
 
+// A primitive reference: its box inline (sequential access while binning)
+// and its index in the input.
 struct Ref {
-  float c[3];
+  Aabb box;
   int32_t idx;
+  float C(int k) const { return 0.5f * (box.lo[k] + box.hi[k]); }
 };
 
 struct BuildNode {
@@ -60,32 +65,48 @@ float Area(const Aabb &b) {
   return 2.0f * (dx * dy + dx * dz + dy * dz);
 }
 
+// Nodes of one subtree, in depth-first order with the subtree root first.
+struct Subtree {
+  std::vector<BuildNode> nodes;
+  int max_depth = 0;
+  int64_t leaves = 0;
+  int max_leaf = 0;
+};
+
+// Top-down binned builder. A subtree of at least kParallelRefs references
+// below a split is built on its own thread while the caller builds its
+// sibling; spliced back in the serial order, so the tree does not depend on
+// the number of threads.
 class Builder {
  public:
+  static constexpr int32_t kParallelRefs = 1 << 15;
+
   Builder(const std::vector<Aabb> &boxes, int strategy, int max_leaf)
-      : boxes_(boxes), strategy_(strategy), max_leaf_(std::max(1, max_leaf)) {
+      : strategy_(strategy), max_leaf_(std::max(1, max_leaf)) {
     refs_.resize(boxes.size());
-    for (size_t i = 0; i < boxes.size(); ++i) {
-      for (int k = 0; k < 3; ++k) refs_[i].c[k] = 0.5f * (boxes[i].lo[k] + boxes[i].hi[k]);
-      refs_[i].idx = static_cast<int32_t>(i);
-    }
+    for (size_t i = 0; i < boxes.size(); ++i) refs_[i] = Ref{boxes[i], static_cast<int32_t>(i)};
+    unsigned hw = std::thread::hardware_concurrency();
+    threads_left_ = static_cast<int>(hw > 1 ? hw - 1 : 0);
   }
 
-  int32_t Build(int32_t start, int32_t end, int depth) {
+  // Builds refs_[start, end) into `out`; returns the subtree root's index.
+  int32_t Build(Subtree &out, int32_t start, int32_t end, int depth) {
     BuildNode node;
     node.box = EmptyBox();
     Aabb cbox = EmptyBox();
     for (int32_t i = start; i < end; ++i) {
-      Grow(node.box, boxes_[refs_[i].idx]);
-      Aabb c;
-      for (int k = 0; k < 3; ++k) c.lo[k] = c.hi[k] = refs_[i].c[k];
-      Grow(cbox, c);
+      Grow(node.box, refs_[i].box);
+      for (int k = 0; k < 3; ++k) {
+        float c = refs_[i].C(k);
+        cbox.lo[k] = std::min(cbox.lo[k], c);
+        cbox.hi[k] = std::max(cbox.hi[k], c);
+      }
     }
-    max_depth_ = std::max(max_depth_, depth);
+    out.max_depth = std::max(out.max_depth, depth);
     int32_t n = end - start;
-    int32_t id = static_cast<int32_t>(nodes_.size());
-    nodes_.push_back(node);
-    if (n <= 1) return MakeLeaf(id, start, n);
+    int32_t id = static_cast<int32_t>(out.nodes.size());
+    out.nodes.push_back(node);
+    if (n <= 1) return MakeLeaf(out, id, start, n);
 
     int32_t mid = -1;
     if (strategy_ == MUON_PARTITION_SAH) {
@@ -93,34 +114,40 @@ class Builder {
     } else if (strategy_ == MUON_PARTITION_MIDPOINT) {
       int axis = WidestAxis(cbox);
       float m = 0.5f * (cbox.lo[axis] + cbox.hi[axis]);
-      Ref *p = std::partition(&refs_[start], &refs_[0] + end, [&](const Ref &r) { return r.c[axis] < m; });
+      Ref *p = std::partition(&refs_[start], &refs_[0] + end, [&](const Ref &r) { return r.C(axis) < m; });
       mid = static_cast<int32_t>(p - &refs_[0]);
       if (mid == start || mid == end) mid = -2;
-      if (n <= max_leaf_ && mid == -2) return MakeLeaf(id, start, n);
+      if (n <= max_leaf_ && mid == -2) return MakeLeaf(out, id, start, n);
     } else {
       mid = -2;
     }
-    if (mid == -1) return MakeLeaf(id, start, n);  // SAH chose a leaf
+    if (mid == -1) return MakeLeaf(out, id, start, n);  // SAH chose a leaf
     if (mid == -2) {
       // Median split on the widest centroid axis (also the fallback when
       // every centroid coincides).
       int axis = WidestAxis(cbox);
       mid = start + n / 2;
       std::nth_element(&refs_[start], &refs_[mid], &refs_[0] + end,
-                       [&](const Ref &a, const Ref &b) { return a.c[axis] < b.c[axis]; });
+                       [&](const Ref &a, const Ref &b) { return a.C(axis) < b.C(axis); });
     }
-    int32_t l = Build(start, mid, depth + 1);
-    int32_t r = Build(mid, end, depth + 1);
-    nodes_[id].left = l;
-    nodes_[id].right = r;
+    int32_t l, r;
+    if (end - mid >= kParallelRefs && TakeThread()) {
+      Subtree right;
+      std::thread t([&] { Build(right, mid, end, depth + 1); });
+      l = Build(out, start, mid, depth + 1);
+      t.join();
+      threads_left_.fetch_add(1);
+      r = Splice(out, right);
+    } else {
+      l = Build(out, start, mid, depth + 1);
+      r = Build(out, mid, end, depth + 1);
+    }
+    out.nodes[id].left = l;
+    out.nodes[id].right = r;
     return id;
   }
 
-  std::vector<BuildNode> nodes_;
   std::vector<Ref> refs_;
-  int max_depth_ = 0;
-  int64_t leaves_ = 0;
-  int max_leaf_seen_ = 0;
 
  private:
   static int WidestAxis(const Aabb &b) {
@@ -128,11 +155,32 @@ class Builder {
     return d[0] > d[1] && d[0] > d[2] ? 0 : (d[1] > d[2] ? 1 : 2);
   }
 
-  int32_t MakeLeaf(int32_t id, int32_t start, int32_t n) {
-    nodes_[id].start = start;
-    nodes_[id].count = n;
-    ++leaves_;
-    max_leaf_seen_ = std::max(max_leaf_seen_, n);
+  bool TakeThread() {
+    int v = threads_left_.load();
+    while (v > 0) {
+      if (threads_left_.compare_exchange_weak(v, v - 1)) return true;
+    }
+    return false;
+  }
+
+  // Appends `sub` to `out`, shifting its child indices; returns its root.
+  static int32_t Splice(Subtree &out, const Subtree &sub) {
+    int32_t off = static_cast<int32_t>(out.nodes.size());
+    for (BuildNode x : sub.nodes) {
+      if (x.left >= 0) x.left += off, x.right += off;
+      out.nodes.push_back(x);
+    }
+    out.max_depth = std::max(out.max_depth, sub.max_depth);
+    out.leaves += sub.leaves;
+    out.max_leaf = std::max(out.max_leaf, sub.max_leaf);
+    return off;
+  }
+
+  static int32_t MakeLeaf(Subtree &out, int32_t id, int32_t start, int32_t n) {
+    out.nodes[id].start = start;
+    out.nodes[id].count = n;
+    ++out.leaves;
+    out.max_leaf = std::max(out.max_leaf, n);
     return id;
   }
 
@@ -142,34 +190,40 @@ class Builder {
     float best_cost = std::numeric_limits<float>::infinity();
     int best_axis = -1, best_bin = -1;
     float parent_area = Area(box);
+    Aabb bin_box[3][kBins];
+    int32_t bin_n[3][kBins] = {};
+    float scale[3];
     for (int axis = 0; axis < 3; ++axis) {
       float extent = cbox.hi[axis] - cbox.lo[axis];
-      if (!(extent > 0.0f)) continue;
-      float scale = kBins / extent;
-      Aabb bin_box[kBins];
-      int32_t bin_n[kBins] = {0};
-      for (int b = 0; b < kBins; ++b) bin_box[b] = EmptyBox();
-      for (int32_t i = start; i < end; ++i) {
-        int b = std::min(kBins - 1, static_cast<int>((refs_[i].c[axis] - cbox.lo[axis]) * scale));
+      scale[axis] = extent > 0.0f ? kBins / extent : 0.0f;
+      for (int b = 0; b < kBins; ++b) bin_box[axis][b] = EmptyBox();
+    }
+    for (int32_t i = start; i < end; ++i) {
+      const Aabb &bx = refs_[i].box;
+      for (int axis = 0; axis < 3; ++axis) {
+        int b = std::min(kBins - 1, static_cast<int>((refs_[i].C(axis) - cbox.lo[axis]) * scale[axis]));
         b = std::max(0, b);
-        ++bin_n[b];
-        Grow(bin_box[b], boxes_[refs_[i].idx]);
+        ++bin_n[axis][b];
+        Grow(bin_box[axis][b], bx);
       }
+    }
+    for (int axis = 0; axis < 3; ++axis) {
+      if (!(cbox.hi[axis] - cbox.lo[axis] > 0.0f)) continue;
       float right_area[kBins];
       int32_t right_n[kBins];
       Aabb acc = EmptyBox();
       int32_t cnt = 0;
       for (int b = kBins - 1; b > 0; --b) {
-        Grow(acc, bin_box[b]);
-        cnt += bin_n[b];
+        Grow(acc, bin_box[axis][b]);
+        cnt += bin_n[axis][b];
         right_area[b] = Area(acc);
         right_n[b] = cnt;
       }
       acc = EmptyBox();
       cnt = 0;
       for (int b = 0; b < kBins - 1; ++b) {
-        Grow(acc, bin_box[b]);
-        cnt += bin_n[b];
+        Grow(acc, bin_box[axis][b]);
+        cnt += bin_n[axis][b];
         if (cnt == 0 || right_n[b + 1] == 0) continue;
         float cost = Area(acc) * cnt + right_area[b + 1] * right_n[b + 1];
         if (cost < best_cost) {
@@ -183,11 +237,10 @@ class Builder {
     float split_cost = kTraversalCost + kIntersectCost * best_cost / std::max(parent_area, 1e-30f);
     float leaf_cost = kIntersectCost * n;
     if (n <= max_leaf_ && leaf_cost <= split_cost) return -1;
-    float extent = cbox.hi[best_axis] - cbox.lo[best_axis];
-    float scale = kBins / extent;
+    float sc = scale[best_axis];
     float lo = cbox.lo[best_axis];
     Ref *p = std::partition(&refs_[start], &refs_[0] + end, [&](const Ref &r) {
-      int b = std::min(kBins - 1, static_cast<int>((r.c[best_axis] - lo) * scale));
+      int b = std::min(kBins - 1, static_cast<int>((r.C(best_axis) - lo) * sc));
       return std::max(0, b) <= best_bin;
     });
     int32_t mid = static_cast<int32_t>(p - &refs_[0]);
@@ -195,9 +248,9 @@ class Builder {
     return mid;
   }
 
-  const std::vector<Aabb> &boxes_;
   int strategy_;
   int max_leaf_;
+  std::atomic<int> threads_left_{0};
 };
 
 // Pads a box outwards by a few ulps so that rounding in the slab test cannot
@@ -238,6 +291,7 @@ void BuildBvh(const std::vector<Aabb> &boxes, int accel, int strategy, int max_l
   *stats = BvhBuildStats();
   if (boxes.empty()) return;
   Builder b(boxes, strategy, accel == MUON_ACCEL_LINEAR ? static_cast<int>(boxes.size()) : max_leaf);
+  Subtree tree;
   int32_t root;
   if (accel == MUON_ACCEL_LINEAR) {
     BuildNode leaf;
@@ -245,29 +299,23 @@ void BuildBvh(const std::vector<Aabb> &boxes, int accel, int strategy, int max_l
     for (const Aabb &x : boxes) Grow(leaf.box, x);
     leaf.start = 0;
     leaf.count = static_cast<int32_t>(boxes.size());
-    b.nodes_.push_back(leaf);
-    b.leaves_ = 1;
-    b.max_leaf_seen_ = leaf.count;
+    tree.nodes.push_back(leaf);
+    tree.leaves = 1;
+    tree.max_leaf = leaf.count;
     root = 0;
   } else {
-    root = b.Build(0, static_cast<int32_t>(boxes.size()), 0);
+    root = b.Build(tree, 0, static_cast<int32_t>(boxes.size()), 0);
   }
   order->resize(boxes.size());
   last->assign(boxes.size(), 0);
   for (size_t i = 0; i < boxes.size(); ++i) (*order)[i] = b.refs_[i].idx;
-  const std::vector<BuildNode> &bn = b.nodes_;
+  const std::vector<BuildNode> &bn = tree.nodes;
   for (const BuildNode &x : bn) {
     if (x.left < 0 && x.count > 0) (*last)[x.start + x.count - 1] = 1;
   }
 
   // Depth-first flattening: each interior build node becomes one 64-byte
   // node holding its two children's boxes.
-  auto link_of = [&](int32_t id, std::vector<int32_t> &pending) -> int32_t {
-    const BuildNode &x = bn[id];
-    if (x.left < 0) return ~x.start;
-    pending.push_back(id);
-    return 0;  // patched below
-  };
   nodes->reserve(bn.size() / 2 + 1);
   double sah = 0.0;
   float root_area = std::max(Area(bn[root].box), 1e-30f);
@@ -306,11 +354,10 @@ void BuildBvh(const std::vector<Aabb> &boxes, int accel, int strategy, int max_l
       }
     }
   }
-  (void)link_of;
   stats->nodes = static_cast<int64_t>(nodes->size());
-  stats->leaves = b.leaves_;
-  stats->max_depth = b.max_depth_;
-  stats->max_leaf = b.max_leaf_seen_;
+  stats->leaves = tree.leaves;
+  stats->max_depth = tree.max_depth;
+  stats->max_leaf = tree.max_leaf;
   stats->sah_cost = sah;
 }
 

@@ -221,8 +221,52 @@ def feature_mix(width: int = 128, height: int = 128, spp: int = 1, integrator: s
     return "\n".join(L) + "\n"
 
 
+def _mesh_fast(lines: list[str], V: np.ndarray, F: np.ndarray) -> None:
+    """A mesh block for large meshes (vectorised number formatting)."""
+    lines.append("start_mesh")
+    v32 = V.astype(np.float32)
+    lines.extend("vertex " + " ".join(row) for row in np.char.mod("%.9g", v32).tolist())
+    lines.extend(("tri %d %d %d" % (a, b, c)) for a, b, c in F.tolist())
+    lines.append("end_mesh")
+
+
+def dense_mesh(width: int = 1024, height: int = 1024, spp: int = 256, max_depth: int = 10, level: int = 8,
+               clutter: int = 10000, seed: int = 1) -> str:
+    """Dense mesh in the Cornell box: a subdivided icosphere (level 8:
+    1,310,720 triangles) with seeded value-noise radial displacement of
+    amplitude 0.1, GGX roughness 0.15, smooth vertex normals, radius 0.5 at
+    (0, 0.75, 0); plus `clutter` random small triangles (edges U[0.01, 0.05])
+    inside the box. Both are authored at 1000x object scale under a `scale`
+    transform so that no triangle falls under the reference's 1e-4 rejection."""
+    rng = np.random.default_rng(seed)
+    L = cornell(width, height, spp, max_depth, seed, "pathtracer", "mis").splitlines()
+    V, F = icosphere(level)
+    V = V * (1.0 + 0.1 * value_noise(V, seed, freq=3.0))[:, None]
+    L += ["brdf ggx", "diffuse 0.1 0.1 0.1", "specular 0.6 0.6 0.6", "roughness 0.15",
+          "compute_vertex_normals on", "push_transform", "translate 0 0.75 0", "scale 0.0005 0.0005 0.0005"]
+    _mesh_fast(L, V * 1000.0, F)
+    L += ["pop_transform", "compute_vertex_normals off", "brdf lambertian", "specular 0 0 0",
+          "diffuse 0.6 0.5 0.4", "push_transform", "scale 0.001 0.001 0.001"]
+    centres = rng.uniform([-0.95, 0.05, -0.95], [0.95, 1.95, 0.95], size=(clutter, 3))
+    edge = rng.uniform(0.01, 0.05, size=clutter)
+    d1 = rng.normal(size=(clutter, 3))
+    d1 /= np.linalg.norm(d1, axis=1, keepdims=True)
+    d2 = rng.normal(size=(clutter, 3))
+    d2 -= (d2 * d1).sum(1, keepdims=True) * d1
+    d2 /= np.linalg.norm(d2, axis=1, keepdims=True)
+    a = centres
+    b = centres + d1 * edge[:, None]
+    c = centres + (0.5 * d1 + 0.866 * d2) * edge[:, None]
+    CV = np.stack([a, b, c], axis=1).reshape(-1, 3) * 1000.0
+    CF = np.arange(3 * clutter, dtype=np.int64).reshape(-1, 3)
+    _mesh_fast(L, CV, CF)
+    L.append("pop_transform")
+    return "\n".join(L) + "\n"
+
+
 WORKLOADS = {
     "cornell": cornell,
     "sphere_field": sphere_field,
     "feature_mix": feature_mix,
+    "dense_mesh": dense_mesh,
 }

@@ -38,6 +38,8 @@ HIT_SCENES = {
     "cornell": lambda: scenes.cornell(128, 128, 1, 5, 1, "normals"),
     "sphere_field": lambda: scenes.sphere_field(128, 128, 1, 8).replace("integrator pathtracer", "integrator normals"),
     "feature_mix": lambda: scenes.feature_mix(128, 128, 1, "normals"),
+    "dense_mesh": lambda: scenes.dense_mesh(128, 128, 1, 10, level=4, clutter=500).replace(
+        "integrator pathtracer", "integrator normals"),
 }
 
 # (scene text, runs, spp per run)
@@ -47,6 +49,7 @@ PT_SCENES = {
     "sphere_field": (lambda: scenes.sphere_field(32, 32, 64, 8), 32, 512),
     "cornell_nee_on": (lambda: scenes.cornell(32, 32, 64, 5, 1, "pathtracer", "on"), 32, 1024),
     "cornell_nee_off": (lambda: scenes.cornell(32, 32, 64, 5, 1, "pathtracer", "off"), 32, 1024),
+    "dense_mesh": (lambda: scenes.dense_mesh(32, 32, 64, 10, level=3, clutter=200), 32, 512),
 }
 
 

@@ -17,7 +17,7 @@ import muon_gb300 as m
 from conftest import GOLDEN
 from muon_gb300 import native
 
-SCENES = ["cornell", "sphere_field", "feature_mix"]
+SCENES = ["cornell", "sphere_field", "feature_mix", "dense_mesh"]
 
 
 def load(name):

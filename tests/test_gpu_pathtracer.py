@@ -20,7 +20,7 @@ import muon_gb300 as m
 from conftest import GOLDEN
 from muon_gb300 import native
 
-CASES = ["cornell", "cornell_nee_on", "cornell_nee_off", "feature_mix", "sphere_field"]
+CASES = ["cornell", "cornell_nee_on", "cornell_nee_off", "feature_mix", "sphere_field", "dense_mesh"]
 GPU_SPP = 8192
 
 

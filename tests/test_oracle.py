@@ -69,7 +69,7 @@ def test_oracle_passes_reference_mae_tests(name):
     assert (mae_golden - mae) ** 2 <= STOCHASTIC[name] ** 2, (mae, mae_golden)
 
 
-@pytest.mark.parametrize("name", ["cornell", "sphere_field", "feature_mix"])
+@pytest.mark.parametrize("name", ["cornell", "sphere_field", "feature_mix", "dense_mesh"])
 def test_oracle_hits_equal_reference_build(name):
     fx = np.load(f"{GOLDEN}/hits_{name}.npz")
     text = str(fx["scene"])
@@ -92,7 +92,7 @@ def test_oracle_hits_equal_reference_build(name):
 # field does not, because the reference's sphere test forms b^2 - c from two
 # nearly equal numbers (muon/objects.cc:231-236), which at distances ~34 from
 # spheres of radius ~0.5 loses ~12 bits.
-FP32_VS_FP64 = {"cornell": 1e-5, "feature_mix": 5e-5, "sphere_field": 5e-4}
+FP32_VS_FP64 = {"cornell": 1e-5, "feature_mix": 5e-5, "sphere_field": 5e-4, "dense_mesh": 1e-5}
 
 
 @pytest.mark.parametrize("name", sorted(FP32_VS_FP64))

@@ -104,10 +104,11 @@ struct DevScene {
   const PrimRecord *light_tris_obj;  // the same in the object-space format
   const int32_t *light_tri_ok;  // per light triangle: 1 if it can be hit
   const DevLight *other_lights; // point/directional
+  const DevLight *all_lights;   // every light in scene order (ray tracer)
   int32_t num_nodes;
   int32_t num_lights;
   int32_t num_other_lights;
-  int32_t pad;
+  int32_t num_all_lights;
 };
 
 // Camera::CastRay state (muon/camera.h:9-32) with the host-computed frame.

@@ -381,6 +381,154 @@ __global__ void __launch_bounds__(kBlock) ShadeDebugKernel(DevScene s, PathBuffe
   }
 }
 
+// ---- ray tracer and analytic direct lighting ---------------------------------
+// Raytracer::Shade (muon/integration.cc:74-124) and AnalyticDirect::Shade
+// (muon/integration.cc:126-199), one thread per path. The ray tracer's
+// recursion color_k = local_k + ks_k * color_(k+1) is evaluated from the
+// deepest level back, in the reference's order, for the first kExactLevels
+// levels; deeper levels (max_depth above 7) are summed forward into the
+// value that stands for level kExactLevels.
+constexpr int kExactLevels = 8;
+
+// glm::max / std::max: (a < b) ? b : a (keeps a NaN in a).
+__device__ __forceinline__ float GlmMax(float a, float b) { return a < b ? b : a; }
+
+struct LightInfo {
+  mm::v3 color, dir;
+  float dist;
+  bool area;
+};
+
+// Light::ShadingInfoAt (muon/lighting.cc:38-72): a quad light reports no
+// direction and distance 0.
+__device__ __forceinline__ LightInfo ShadingInfoAt(const DevLight &l, mm::v3 p) {
+  using namespace mm;
+  LightInfo r;
+  const int type = __float_as_int(l.corner.w);
+  r.color = V(l.color);
+  r.area = false;
+  if (type == MUON_LIGHT_DIRECTIONAL) {
+    r.dir = V(l.corner);
+    r.dist = INFINITY;
+  } else if (type == MUON_LIGHT_POINT) {
+    v3 ptl = V(l.corner) - p;
+    r.dir = normalize(ptl);
+    float d = length(ptl);
+    float att = add(add(l.edge0.x, mul(l.edge0.y, d)), mul(mul(l.edge0.z, d), d));
+    r.color = r.color / att;
+    r.dist = d;
+  } else {
+    r.dir = make3(0.0f, 0.0f, 0.0f);
+    r.dist = 0.0f;
+    r.area = true;
+  }
+  return r;
+}
+
+template <bool kStats, int kMode>
+__global__ void __launch_bounds__(kBlock) WhittedKernel(DevScene s, PathBuffers b, WaveInfo w, int integrator,
+                                                        int max_trace_depth) {
+  using namespace mm;
+  const int i = blockIdx.x * kBlock + threadIdx.x;
+  TraceCounters ce, co;
+  bool overflow = false;
+  uint32_t secondary = 0;
+  if (i < w.n) {
+    float4 o4 = b.ray_o[0][i], d4 = b.ray_d[0][i];
+    float3 o = f3(o4.x, o4.y, o4.z), d = f3(d4.x, d4.y, d4.z);
+    v3 local[kExactLevels], ks[kExactLevels];
+    v3 tail = splat3(0.0f), tail_tp = splat3(1.0f);
+    int levels = 0;
+    for (int depth = 0; depth <= max_trace_depth; ++depth) {
+      if (depth > 0) ++secondary;
+      float t, t_obj = 0.0f;
+      const int h = Trace<false, kStats, kMode>(s, o, d, INFINITY, &t, &ce, &overflow, &t_obj);
+      if (h < 0) break;
+      float3 p3, n3;
+      float dist;
+      int mat, light, pid;
+      Surface<kMode>(s, h, o, d, kMode == MUON_ISECT_EXACT ? t_obj : t, &p3, &n3, &dist, &mat, &light, &pid);
+      const v3 p = V(p3), n = V(n3), rd = V(d);
+      const float4 *mq = reinterpret_cast<const float4 *>(s.materials + mat);
+      const float4 kd4 = __ldg(mq), ks4 = __ldg(mq + 1), ke4 = __ldg(mq + 2), ka4 = __ldg(mq + 3);
+      const v3 kd = make3(kd4.x, kd4.y, kd4.z), kspec = make3(ks4.x, ks4.y, ks4.z);
+      const v3 ke = make3(ke4.x, ke4.y, ke4.z), ka = make3(ka4.x, ka4.y, ka4.z);
+      v3 color;
+      bool cont = false;
+      if (integrator == MUON_INTEGRATOR_ANALYTIC_DIRECT) {
+        color = ke;
+        for (int li = 0; li < s.num_all_lights; ++li) {
+          const DevLight l = s.all_lights[li];
+          LightInfo info = ShadingInfoAt(l, p);
+          if (!info.area) continue;
+          v3 vtx[4];
+          vtx[0] = V(l.corner);
+          vtx[1] = V(l.corner) + V(l.edge0);
+          vtx[2] = vtx[1] + V(l.edge1);
+          vtx[3] = V(l.corner) + V(l.edge1);
+          const v3 brdf = kd * 0.318309886183790671537767526745028724f;
+          v3 irr = splat3(0.0f);
+          for (int k = 0; k < 4; ++k) {
+            v3 ui = normalize(vtx[k] - p), un = normalize(vtx[(k + 1) & 3] - p);
+            float theta = acosf(dot(ui, un));
+            irr = irr + theta * normalize(cross(ui, un));
+          }
+          irr = irr * 0.5f;
+          color = color + (brdf * info.color) * dot(irr, n);
+        }
+      } else {
+        color = ka + ke;
+        const v3 shift = p + kEps * n;
+        for (int li = 0; li < s.num_all_lights; ++li) {
+          const DevLight l = s.all_lights[li];
+          LightInfo info = ShadingInfoAt(l, p);
+          // A quad light's zero-length shadow ray can hit nothing.
+          if (!info.area) {
+            float ts;
+            const float3 dir = f3(info.dir.x, info.dir.y, info.dir.z);
+            if (Trace<true, kStats, kMode>(s, f3(shift.x, shift.y, shift.z), dir, info.dist, &ts, &co, &overflow) >= 0)
+              continue;
+          }
+          v3 dc = kd * GlmMax(dot(n, info.dir), 0.0f);
+          v3 half = normalize(info.dir - rd);
+          v3 sc = kspec * powf(GlmMax(dot(n, half), 0.0f), kd4.w);
+          color = color + info.color * (dc + sc);
+        }
+        if (kspec.x > 0.0f || kspec.y > 0.0f || kspec.z > 0.0f) {
+          cont = true;
+          const v3 r = reflect(rd, n);
+          o = f3(shift.x, shift.y, shift.z);
+          d = f3(r.x, r.y, r.z);
+        }
+      }
+      if (levels < kExactLevels) {
+        local[levels] = color;
+        ks[levels] = kspec;
+        ++levels;
+      } else {
+        tail = tail + tail_tp * color;
+        tail_tp = tail_tp * kspec;
+      }
+      if (!cont) break;
+    }
+    v3 c = tail;
+    for (int k = levels - 1; k >= 0; --k) c = local[k] + ks[k] * c;
+    b.final_rad[i] = make_float4(c.x, c.y, c.z, 0.0f);
+  }
+  AddStat(b.stats, kStatSecondary, secondary);
+  if (kStats) {
+    AddStat(b.stats, kStatBoxTests, ce.box_tests);
+    AddStat(b.stats, kStatBoxHits, ce.box_hits);
+    AddStat(b.stats, kStatPrimTests, ce.prim_tests);
+    AddStat(b.stats, kStatPrimHits, ce.prim_hits);
+    AddStat(b.stats, kStatOccBoxTests, co.box_tests);
+    AddStat(b.stats, kStatOccBoxHits, co.box_hits);
+    AddStat(b.stats, kStatOccPrimTests, co.prim_tests);
+    AddStat(b.stats, kStatOccPrimHits, co.prim_hits);
+  }
+  if (overflow) atomicAdd(b.stats + kStatOverflow, 1ull);
+}
+
 // ---- path tracer shading ----------------------------------------------------
 // PathTracer::Shade for every queued path vertex at depth `bounce`
 // (muon/integration.cc:205-328). Each shadow slot receives the radiance it
@@ -745,6 +893,16 @@ void LaunchShadeDebug(const DevScene &s, const PathBuffers &b, WaveCounters wc, 
   if (bound <= 0) return;
   WithMode(isect, [&](auto m) {
     ShadeDebugKernel<decltype(m)::value><<<CountedBlocks(bound), kBlock, 0, st>>>(s, b, wc, integrator);
+  });
+}
+
+void LaunchWhitted(const DevScene &s, const PathBuffers &b, const WaveInfo &w, int integrator, int max_trace_depth,
+                   int isect, bool stats, cudaStream_t st) {
+  if (w.n <= 0) return;
+  WithMode(isect, [&](auto m) {
+    constexpr int M = decltype(m)::value;
+    if (stats) WhittedKernel<true, M><<<Blocks(w.n), kBlock, 0, st>>>(s, b, w, integrator, max_trace_depth);
+    else WhittedKernel<false, M><<<Blocks(w.n), kBlock, 0, st>>>(s, b, w, integrator, max_trace_depth);
   });
 }
 

@@ -101,6 +101,10 @@ void LaunchExtend(const DevScene &s, const PathBuffers &b, WaveCounters wc, int 
                   bool stats, cudaStream_t st);
 void LaunchShadeDebug(const DevScene &s, const PathBuffers &b, WaveCounters wc, int integrator, int bound, int isect,
                       cudaStream_t st);
+// Raytracer / AnalyticDirect for every path of a wave; rays are traced up to
+// depth max_trace_depth (0 = primary rays only).
+void LaunchWhitted(const DevScene &s, const PathBuffers &b, const WaveInfo &w, int integrator, int max_trace_depth,
+                   int isect, bool stats, cudaStream_t st);
 void LaunchShadePath(const DevScene &s, const WaveInfo &w, const ShadeParams &sp, const PathBuffers &b,
                      WaveCounters wc, int bounce, int bound, cudaStream_t st);
 void LaunchOcclude(const DevScene &s, const PathBuffers &b, WaveCounters wc, int bounce, int slots, int bound,

@@ -82,7 +82,7 @@ struct MuonScene {
   DevCamera cam{};
   // scene arrays
   DeviceBuffer nodes, prims, prims_obj, shade, smooth, smooth_obj, transforms, materials, lights, light_tris,
-      light_tris_obj, light_tri_ok, other_lights;
+      light_tris_obj, light_tri_ok, other_lights, all_lights;
   // work arrays
   DeviceBuffer ray_o[2], ray_d[2], tp[2], rad[2], hits, link, final_rad, org, contrib, slot_dir, shq, order, counters,
       stats;
@@ -233,8 +233,6 @@ void ComputeCamera(const MuonCameraDesc &c, DevCamera *out) {
 int ValidateParams(const MuonRenderParams &p) {
   if (p.integrator < MUON_INTEGRATOR_NORMALS || p.integrator > MUON_INTEGRATOR_PATHTRACER)
     return Fail(MUON_ERR_INVALID_ARG, "unknown integrator");
-  if (p.integrator == MUON_INTEGRATOR_RAYTRACER || p.integrator == MUON_INTEGRATOR_ANALYTIC_DIRECT)
-    return Fail(MUON_ERR_INVALID_ARG, "integrator not available on the GPU path yet");
   if (p.pixel_samples < 1) return Fail(MUON_ERR_INVALID_ARG, "pixel_samples must be >= 1");
   if (p.next_event_estimation < MUON_NEE_OFF || p.next_event_estimation > MUON_NEE_MIS)
     return Fail(MUON_ERR_INVALID_ARG, "unknown next_event_estimation mode");
@@ -260,6 +258,8 @@ int ValidateParams(const MuonRenderParams &p) {
 void RenderDevice(MuonScene *sc, const MuonRenderParams &p, double *d_sum, double *d_sq, uint32_t *d_cnt) {
   cudaStream_t st = sc->stream;
   const bool pt = p.integrator == MUON_INTEGRATOR_PATHTRACER;
+  // Raytracer / AnalyticDirect: one kernel follows each path to its end.
+  const bool whitted = p.integrator == MUON_INTEGRATOR_RAYTRACER || p.integrator == MUON_INTEGRATOR_ANALYTIC_DIRECT;
   const bool stats_on = (p.flags & MUON_RENDER_STATS) != 0;
   const bool timing = (p.flags & MUON_RENDER_TIMING) != 0;
   ShadeParams sp{};
@@ -312,7 +312,7 @@ void RenderDevice(MuonScene *sc, const MuonRenderParams &p, double *d_sum, doubl
   // A path traces at depths 0..max_trace_depth; with max_depth 0 and lights
   // sampled, Trace() casts no ray at all.
   const bool traces = !(p.max_depth >= 0 && sp.max_trace_depth < 0);
-  const bool bounded = !pt || sp.max_trace_depth >= 0;
+  const bool bounded = !pt || sp.max_trace_depth >= 0;  // (the ray tracer runs in one launch)
   const int bounces = !traces ? 0 : (!pt ? 1 : (bounded ? sp.max_trace_depth + 1 : kMaxBounces));
   const size_t stride = WaveCounterWords(bounces);
   bool moved = sc->EnsureWork(std::min<int64_t>(pix_per_wave, npix_total) * ns, slots);
@@ -341,7 +341,14 @@ void RenderDevice(MuonScene *sc, const MuonRenderParams &p, double *d_sum, doubl
         if (ev) CUDA_TRY(cudaEventRecordWithFlags(ev->b, st, cudaEventRecordExternal));
         ++launches;
       };
-      for (int k = 0; k < bounces; ++k) {
+      if (whitted && bounces > 0) {
+        // Integrator::Trace's depth cut-off; unbounded depth stops at the
+        // bounce cap (a ray between two mirrors would never end).
+        const int max_d = p.integrator == MUON_INTEGRATOR_ANALYTIC_DIRECT ? 0
+                          : sp.max_trace_depth >= 0 ? sp.max_trace_depth : kMaxBounces - 1;
+        timed(2, [&] { LaunchWhitted(sc->dev, b, w, p.integrator, max_d, p.intersect_mode, stats_on, st); });
+      }
+      for (int k = 0; k < (whitted ? 0 : bounces); ++k) {
         timed(0, [&] { LaunchExtend(sc->dev, b, wc, k, w.n, p.intersect_mode, stats_on, st); });
         if (!pt) {
           timed(2, [&] { LaunchShadeDebug(sc->dev, b, wc, p.integrator, w.n, p.intersect_mode, st); });
@@ -498,6 +505,7 @@ int muon_gpu_scene_create(const MuonSceneDesc *desc, MuonScene **out) {
     Upload(sc->materials, im.materials, st);
     Upload(sc->lights, im.lights, st);
     Upload(sc->other_lights, im.other_lights, st);
+    Upload(sc->all_lights, im.all_lights, st);
     // The two triangles of each quad light (muon/parser.cc:735-747), in the
     // same record format as the BVH's, for the MIS light-hit test.
     std::vector<PrimRecord> lt(2 * im.lights.size()), lt_obj(2 * im.lights.size());
@@ -543,9 +551,11 @@ int muon_gpu_scene_create(const MuonSceneDesc *desc, MuonScene **out) {
     d.light_tris_obj = sc->light_tris_obj.as<PrimRecord>();
     d.light_tri_ok = sc->light_tri_ok.as<int32_t>();
     d.other_lights = sc->other_lights.as<DevLight>();
+    d.all_lights = sc->all_lights.as<DevLight>();
     d.num_nodes = static_cast<int32_t>(im.nodes.size());
     d.num_lights = static_cast<int32_t>(im.lights.size());
     d.num_other_lights = static_cast<int32_t>(im.other_lights.size());
+    d.num_all_lights = static_cast<int32_t>(im.all_lights.size());
     ComputeCamera(im.camera, &sc->cam);
     CUDA_TRY(cudaStreamSynchronize(st));
   } catch (const CudaError &e) {

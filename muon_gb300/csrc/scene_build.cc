@@ -467,9 +467,11 @@ bool BuildSceneImage(const MuonSceneDesc &desc, SceneImage *img, std::string *er
     if (l.type == MUON_LIGHT_QUAD) {
       quad_index[i] = static_cast<int32_t>(img->lights.size());
       img->lights.push_back(d);
+      img->all_lights.push_back(d);
     } else if (l.type == MUON_LIGHT_POINT || l.type == MUON_LIGHT_DIRECTIONAL) {
       d.edge0 = MakeF4(l.p1[0], l.p1[1], l.p1[2], 0.0f);  // attenuation for point lights
       img->other_lights.push_back(d);
+      img->all_lights.push_back(d);
     } else {
       *error = "light has an unknown type";
       return false;

@@ -43,6 +43,7 @@ struct SceneImage {
   std::vector<DevMaterial> materials;
   std::vector<DevLight> lights;           // quad lights only
   std::vector<DevLight> other_lights;     // point / directional lights
+  std::vector<DevLight> all_lights;       // every light, in scene order
   std::vector<int32_t> leaf_of_prim_id;   // parse-order id -> leaf slot (-1 = never hit)
   int64_t num_prims = 0;                  // primitives in the scene, including never-hit ones
   bool any_smooth = false;

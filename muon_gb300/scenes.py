@@ -264,6 +264,53 @@ def dense_mesh(width: int = 1024, height: int = 1024, spp: int = 256, max_depth:
     return "\n".join(L) + "\n"
 
 
+def whitted(width: int = 128, height: int = 128, spp: int = 1, max_depth: int = 5, seed: int = 1,
+            integrator: str = "raytracer", nee: str = "off") -> str:
+    """Scene for the ray tracer and analytic direct lighting: 24 seeded
+    spheres (every third one an ellipsoid under a push_transform), Phong
+    materials with and without specular colour (mirror chains up to
+    max_depth), a slightly specular ground quad, ambient terms, two attenuated
+    point lights, a directional light and one quad light (a quad light adds a
+    specular term in the ray tracer and is the only light analytic direct
+    lighting uses)."""
+    rng = np.random.default_rng(seed)
+    L = ["# spheres and lights for the ray tracer",
+         f"random_seed {seed}",
+         f"film_size {width} {height}",
+         f"integrator {integrator}",
+         f"pixel_samples {spp}",
+         f"max_depth {max_depth}",
+         f"next_event_estimation {nee}",
+         "camera 0 3 12  0 0.5 0  0 1 0  50",
+         "attenuation 1 0.05 0.01",
+         "point_light 4 6 4  12 11 10",
+         "point_light -5 3 2  4 5 7",
+         "directional_light 0.3 1 0.4  0.15 0.15 0.12",
+         "quad_light -1 5.5 -1  2 0 0  0 0 2  6 6 6",
+         "brdf phong",
+         "emission 0 0 0",
+         "ambient 0.03 0.03 0.03",
+         "diffuse 0.5 0.5 0.45",
+         "specular 0.2 0.2 0.2",
+         "shininess 40"]
+    _quad(L, (-12, 0, -12), (-12, 0, 12), (12, 0, 12), (12, 0, -12))
+    for k in range(24):
+        c = rng.uniform([-5.0, 0.3, -5.0], [5.0, 2.5, 3.0])
+        r = rng.uniform(0.3, 0.9)
+        kd = rng.uniform(0.05, 0.8, 3)
+        mirror = rng.uniform() < 0.4
+        ks = rng.uniform(0.3, 0.9, 3) if mirror else np.zeros(3)
+        L += ["diffuse " + _v(*kd), "specular " + _v(*ks), "shininess " + _f(10 ** rng.uniform(0.5, 2.5)),
+              "ambient " + _v(*(0.1 * kd))]
+        if k % 3 == 2:
+            sx, sy, sz = rng.uniform(0.5, 1.5, 3)
+            L += ["push_transform", "translate " + _v(*c), "rotate 0 1 0 " + _f(rng.uniform(0, 180)),
+                  "scale " + _v(sx, sy, sz), "sphere 0 0 0 " + _f(r), "pop_transform"]
+        else:
+            L.append("sphere " + _v(*c, r))
+    return "\n".join(L) + "\n"
+
+
 WORKLOADS = {
     "cornell": cornell,
     "sphere_field": sphere_field,

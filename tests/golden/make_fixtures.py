@@ -8,6 +8,8 @@ muon_gb300.scenes and stores small .npz files next to this script:
                    (linear structure: parse-order primitive ids; BVH: values)
   pt_<name>.npz    FP64 films of independent single-thread path-traced
                    renders (distinct seeds) for statistical parity tests
+  img_<name>.npz   1-spp films of the deterministic ray tracer and analytic
+                   direct integrators (FP32 values) and the ray counters
 
 Usage: python tests/golden/make_fixtures.py [--only NAME ...]
 Requires the reference sources (to build oracle/_ref); the GPU machine only reads
@@ -40,6 +42,14 @@ HIT_SCENES = {
     "feature_mix": lambda: scenes.feature_mix(128, 128, 1, "normals"),
     "dense_mesh": lambda: scenes.dense_mesh(128, 128, 1, 10, level=4, clutter=500).replace(
         "integrator pathtracer", "integrator normals"),
+}
+
+# deterministic integrators rendered at 1 spp (sample 0 = pixel centre)
+IMG_SCENES = {
+    "whitted_rt": lambda: scenes.whitted(128, 128, 1, 5, 1, "raytracer", "off"),
+    "whitted_rt_nee": lambda: scenes.whitted(128, 128, 1, 4, 2, "raytracer", "on"),
+    "whitted_analytic": lambda: scenes.whitted(128, 128, 1, 5, 3, "analyticdirect"),
+    "cornell_analytic": lambda: scenes.cornell(128, 128, 1, 5, 1, "analyticdirect"),
 }
 
 # (scene text, runs, spp per run)
@@ -102,6 +112,14 @@ def pt(name: str) -> None:
     print(f"pt_{name}: {runs} runs x {spp} spp, mean {sums.sum(0).mean() / (runs * spp):.4f}")
 
 
+def img(name: str) -> None:
+    text = IMG_SCENES[name]()
+    s, _, n, counters = _render((text, 1, 1))
+    np.savez_compressed(os.path.join(HERE, f"img_{name}.npz"), scene=np.array(text), film=s.astype(np.float32),
+                        counters=counters.astype(np.int64))
+    print(f"img_{name}: mean {s.mean():.5f}, counters {counters.tolist()}")
+
+
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--only", nargs="*")
@@ -113,6 +131,9 @@ def main() -> None:
     for name in PT_SCENES:
         if not a.only or ("pt_" + name) in a.only:
             pt(name)
+    for name in IMG_SCENES:
+        if not a.only or ("img_" + name) in a.only:
+            img(name)
 
 
 if __name__ == "__main__":

@@ -26,6 +26,7 @@
 #include <vector>
 
 #include "host_scene.h"
+#include "mesh_io.h"
 
 namespace muon_gpu {
 
@@ -61,7 +62,7 @@ struct Vertex {
 
 class Parser {
  public:
-  explicit Parser(ParsedScene *out) : s_(out) {
+  Parser(ParsedScene *out, const std::string &base_dir) : s_(out), base_dir_(base_dir) {
     std::random_device rd;
     seedgen_.seed(rd());
     material_ = DefaultMaterial();
@@ -109,7 +110,32 @@ class Parser {
   }
   int32_t NextPrimId() { return prim_counter_++; }
 
+  // Tri::Tri plus the vertex-normal accumulation of the `tri` command
+  // (muon/parser.cc:619-639) for global vertex ids g.
+  void AddTriangle(const int32_t g[3]) {
+    MuonTriangleDesc t{};
+    for (int k = 0; k < 3; ++k) {
+      t.v[k][0] = vertices_[g[k]].pos.x;
+      t.v[k][1] = vertices_[g[k]].pos.y;
+      t.v[k][2] = vertices_[g[k]].pos.z;
+      // Vertex ids are kept in the normal slots until Finish() resolves them.
+      std::memcpy(&t.n[k][0], &g[k], sizeof(int32_t));
+    }
+    t.transform = xform_stack_.back();
+    t.material = CurrentMaterial();
+    t.light = -1;
+    t.smooth = compute_vertex_normals_ ? 1 : 0;
+    t.prim_id = NextPrimId();
+    if (compute_vertex_normals_) {
+      mm::v3 a = vertices_[g[0]].pos, b = vertices_[g[1]].pos, c = vertices_[g[2]].pos;
+      mm::v3 face = mm::cross(b - a, c - a);
+      for (int k = 0; k < 3; ++k) vertices_[g[k]].normal = vertices_[g[k]].normal + face;
+    }
+    s_->triangles.push_back(t);
+  }
+
   ParsedScene *s_;
+  std::string base_dir_;
   std::mt19937 seedgen_;
   bool seed_drawn_ = false;
   MuonMaterialDesc material_;
@@ -238,9 +264,25 @@ void Parser::Line(const std::string &raw) {
   } else if (cmd == "load") {
     std::string v;
     if (!Read(iss, &v)) return Warn(line);
-    // Mesh import goes through assimp in the reference (muon/parser.cc:465-561);
-    // no importer is linked here, so the command loads nothing.
-    Warn(line);
+    // The reference imports through assimp relative to the scene file's
+    // directory (muon/parser.cc:465-561): new vertices, and triangles under
+    // the current material and transform. A file that cannot be read is
+    // skipped with a warning, as there.
+    std::string path = v;
+    if (!base_dir_.empty() && !v.empty() && v[0] != '/') path = base_dir_ + "/" + v;
+    MeshData mesh;
+    std::string err;
+    if (!LoadMesh(path, &mesh, &err)) {
+      if (std::getenv("MUON_PARSE_VERBOSE")) std::fprintf(stderr, "muon: load: %s\n", err.c_str());
+      return Warn(line);
+    }
+    const int32_t base = static_cast<int32_t>(vertices_.size());
+    for (const auto &p : mesh.positions)
+      vertices_.push_back(Vertex{mm::make3(p[0], p[1], p[2]), mm::splat3(0.0f)});
+    for (const auto &t : mesh.triangles) {
+      const int32_t g[3] = {base + t[0], base + t[1], base + t[2]};
+      AddTriangle(g);
+    }
   } else if (cmd == "compute_vertex_normals") {
     int32_t v = compute_vertex_normals_;
     std::string w;
@@ -281,26 +323,8 @@ void Parser::Line(const std::string &raw) {
     const std::vector<int32_t> &mesh = meshes_[cur_mesh_];
     int n = static_cast<int>(mesh.size());
     if (i0 < 0 || i1 < 0 || i2 < 0 || i0 >= n || i1 >= n || i2 >= n) return Warn(line);
-    int32_t g[3] = {mesh[i0], mesh[i1], mesh[i2]};
-    MuonTriangleDesc t{};
-    for (int k = 0; k < 3; ++k) {
-      t.v[k][0] = vertices_[g[k]].pos.x;
-      t.v[k][1] = vertices_[g[k]].pos.y;
-      t.v[k][2] = vertices_[g[k]].pos.z;
-      // Vertex ids are kept in the normal slots until Finish() resolves them.
-      std::memcpy(&t.n[k][0], &g[k], sizeof(int32_t));
-    }
-    t.transform = xform_stack_.back();
-    t.material = CurrentMaterial();
-    t.light = -1;
-    t.smooth = compute_vertex_normals_ ? 1 : 0;
-    t.prim_id = NextPrimId();
-    if (compute_vertex_normals_) {
-      mm::v3 a = vertices_[g[0]].pos, b = vertices_[g[1]].pos, c = vertices_[g[2]].pos;
-      mm::v3 face = mm::cross(b - a, c - a);
-      for (int k = 0; k < 3; ++k) vertices_[g[k]].normal = vertices_[g[k]].normal + face;
-    }
-    s_->triangles.push_back(t);
+    const int32_t g[3] = {mesh[i0], mesh[i1], mesh[i2]};
+    AddTriangle(g);
   } else if (cmd == "translate" || cmd == "scale") {
     mm::v3 v;
     if (!read3(&v)) return Warn(line);
@@ -420,8 +444,7 @@ MuonTransformDesc MakeTransformDesc(const mm::m4 &m) {
 
 bool ParseScene(const std::string &text, const std::string &base_dir, ParsedScene *out,
                 std::string *error) {
-  (void)base_dir;
-  Parser parser(out);
+  Parser parser(out, base_dir);
   std::istringstream in(text);
   std::string line;
   while (std::getline(in, line)) parser.Line(line);

@@ -46,6 +46,10 @@ WORKLOADS = {
     # traversal-bound: 1,310,720-triangle displaced icosphere (level 8) + 10k clutter triangles in the Cornell box
     "dense_mesh": {"workload": "dense_mesh", "triangles": 1320756, "width": 1024, "height": 1024, "spp": 256,
                    "max_depth": 10, "nee": "mis", "importance_sampling": "brdf", "seed": 1},
+    # 64 seeded scenes of uneven size in one batched wavefront
+    "batch64": {"workload": "batch64", "scenes": 64, "triangles": "log-uniform 1k-500k per scene",
+                "resolutions": [128, 256, 512, 1024], "spp": "uniform 4-64", "max_depth": "uniform 4-10",
+                "nee": "mis", "importance_sampling": "brdf", "seed": 1},
 }
 WORKLOAD = dict(WORKLOADS["sphere_field"])
 METRIC = "Mrays/s"
@@ -131,8 +135,122 @@ def algorithmic_bytes(st: dict, slots: int) -> dict:
     return {"extend": ext, "occlude": occ, "shade": shade, "fold": fold}
 
 
+def batch_texts() -> list[str]:
+    from muon_gb300 import scenes
+
+    return [scenes.batch_scene(i, WORKLOAD["seed"]) for i in range(WORKLOAD["scenes"])]
+
+
+def run_batch(args) -> None:
+    """One step = one batched render of all 64 scenes (muon_gpu_batch_render_device)."""
+    import torch
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    if world > 1:
+        torch.distributed.init_process_group("nccl", device_id=torch.device("cuda", local))
+    from muon_gb300 import build as native_build
+
+    native_build.build()
+    import muon_gb300 as m
+    from muon_gb300 import native
+
+    texts = batch_texts()
+    parsed = [m.parse_string(t) for t in texts]
+    sc = [m.Scene(p) for p in parsed]
+    batch = m.Batch(sc)
+    params = [s.params(intersect_mode=native.ISECT_EXACT, seed=1000 * rank + i) for i, s in enumerate(sc)]
+    t_tune = time.perf_counter()
+    tune = batch.autotune(params)
+    t_tune = time.perf_counter() - t_tune
+    films = [(torch.zeros((s.height, s.width, 3), dtype=torch.float64, device="cuda"),
+              torch.zeros((s.height, s.width, 3), dtype=torch.float64, device="cuda"),
+              torch.zeros((s.height, s.width), dtype=torch.int32, device="cuda")) for s in sc]
+    ptrs = [[f[k].data_ptr() for f in films] for k in range(3)]
+    render = lambda: batch.render_device(params, *ptrs)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    for _ in range(args.warmup):
+        render()
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    times, counted, lat = [], 0, []
+    with ClockSampler(local) as clocks:
+        for _ in range(args.steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            render()
+            total, per = batch.stats()
+            times.append(total["render_ms"])
+            counted += total["primary_rays"] + total["secondary_rays"]
+            lat += [p["done_ms"] for p in per]
+            launches = total["kernel_launches"]
+    dev_ms = sum(times)
+    t = torch.tensor([dev_ms, float(counted)], dtype=torch.float64, device="cuda")
+    if world > 1:
+        tmax, tsum = t.clone(), t.clone()
+        torch.distributed.all_reduce(tmax, op=torch.distributed.ReduceOp.MAX)
+        torch.distributed.all_reduce(tsum, op=torch.distributed.ReduceOp.SUM)
+        dev_ms, counted = float(tmax[0]), float(tsum[1])
+    value = counted / (dev_ms * 1e3)
+    # end to end: scene uploads (BVH builds), batch merge, render, host films back
+    e2e_steps = 2
+    h2d = sum(p.desc.num_triangles * 80 + p.desc.num_spheres * 32 + p.desc.num_materials * 56 +
+              p.desc.num_lights * 52 + p.desc.num_transforms * 192 for p in parsed)
+    d2h = sum(s.width * s.height * (3 * 8 * 2 + 4) for s in sc)
+    t0 = time.perf_counter()
+    e2e_counted = 0
+    for _ in range(e2e_steps):
+        scs = [m.Scene(p) for p in parsed]
+        b2 = m.Batch(scs)
+        b2.render(params)
+        tot, _ = b2.stats()
+        e2e_counted += tot["primary_rays"] + tot["secondary_rays"]
+        b2.close()
+        for s in scs:
+            s.close()
+    e2e_value = e2e_counted / (time.perf_counter() - t0) / 1e6
+    if rank != 0:
+        return
+    lat_sorted = sorted(lat)
+    pct = lambda q: lat_sorted[min(len(lat_sorted) - 1, int(q * len(lat_sorted)))]
+    cpu = None
+    if world == 1:
+        threads = os.cpu_count() or 1
+        rates = [reference_rate(texts[i], 1, threads) for i in range(4)]
+        rays = sum(r[0] * r[1] for r in rates)
+        secs = sum(r[1] for r in rates)
+        cpu = {"value": round(rays / secs, 3), "unit": METRIC, "cores": threads, "kind": rates[0][2],
+               "sample": f"scenes 0-3 of the batch at 1 spp, {secs:.1f} s on {threads} threads"}
+    line = {
+        "metric": METRIC, "value": round(value, 2), "unit": METRIC, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(dev_ms / args.steps, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (64 seeded scenes)",
+        "config": dict(WORKLOAD, parallelism=f"replicas{world}", intersect_mode="exact",
+                       total_triangles=int(sum(p.desc.num_triangles for p in parsed)),
+                       paths_per_step=int(total["paths"]),
+                       l2="flushed between steps (256 MiB write)"),
+        "latency_ms": {"p50": round(pct(0.50), 3), "p99": round(pct(0.99), 3), "max": round(lat_sorted[-1], 3),
+                       "note": "per scene: batch start to its film complete"},
+        "autotune": dict(tune, seconds=round(t_tune, 2)),
+        "e2e": {"value": round(e2e_value, 2), "unit": METRIC, "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h),
+                "note": "64 scene uploads (BVH builds) + batch merge + render + host films back per step"},
+        "gpu_launches": int(launches) * args.steps,
+        "clocks": clocks.summary(),
+    }
+    if cpu:
+        line["cpu_baseline"] = cpu
+    print(json.dumps(line), flush=True)
+
+
 def run_ours(args) -> None:
     import torch
+
+    if WORKLOAD["workload"] == "batch64":
+        return run_batch(args)
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -313,10 +431,17 @@ def run_reference(args) -> None:
     from oracle import build as oracle_build
 
     oracle_build.build()
-    text = scene_text()
     threads = os.cpu_count() or 1
-    rate1, el1, kind = reference_rate(text, 1, threads)
-    spp = max(1, min(WORKLOAD["spp"], int(5.0 / max(el1, 1e-3))))
+    if WORKLOAD["workload"] == "batch64":
+        # a bounded sample of the batch: its first scene at 1 spp per step
+        text = batch_texts()[0]
+        spp = 1
+        sample = "scene 0 of the batch at 1 spp per step"
+    else:
+        text = scene_text()
+        rate1, el1, kind = reference_rate(text, 1, threads)
+        spp = max(1, min(WORKLOAD["spp"], int(5.0 / max(el1, 1e-3))))
+        sample = f"full {WORKLOAD['width']}x{WORKLOAD['height']} frame at {spp} spp (of {WORKLOAD['spp']}) per step"
     for _ in range(args.warmup):
         reference_rate(text, 1, threads)
     rates, times = [], []
@@ -331,8 +456,7 @@ def run_reference(args) -> None:
             "data": f"synthetic (seeded {WORKLOAD['workload'].replace('_', ' ')})",
             "config": dict(WORKLOAD, parallelism=f"host threads {threads}"),
             "cpu_baseline": {"value": round(value, 3), "unit": METRIC, "cores": threads, "kind": kind,
-                             "sample": f"full {WORKLOAD['width']}x{WORKLOAD['height']} frame at {spp} spp "
-                                       f"(of {WORKLOAD['spp']}) per step"},
+                             "sample": sample},
             "e2e": {"value": round(value, 3), "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 

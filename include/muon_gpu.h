@@ -315,6 +315,51 @@ int muon_gpu_render_noalloc(MuonScene *scene, const MuonRenderParams *params, do
 /* Counters and device timings of the last render (muon/stats.h:11-44). */
 int muon_gpu_stats(const MuonScene *scene, MuonStats *stats);
 
+/* ---- batched rendering -------------------------------------------------
+ * Many scenes of uneven size, resolution and sample count rendered by one
+ * wavefront: every kernel launch covers paths of all the scenes at once, and
+ * the whole batch is replayed as one CUDA graph. This generalises the thread
+ * pool of Renderer::Render (muon/renderer.cc:31-77) from one scene to many;
+ * the reference itself renders one scene per process. Path tracer only. */
+typedef struct MuonBatch MuonBatch;
+
+typedef struct MuonBatchSceneStats {
+  uint64_t primary_rays;
+  double done_ms; /* from the start of the batch until this scene's film was complete */
+} MuonBatchSceneStats;
+
+/* Launch configuration chosen by muon_gpu_batch_autotune. */
+typedef struct MuonBatchTuning {
+  int32_t wave_paths;              /* paths per wavefront                        */
+  int32_t traversal_blocks_per_sm; /* resident blocks of the traversal kernels   */
+  int32_t candidates;              /* configurations timed                       */
+  int32_t pad;
+  double best_ms;                  /* time of the chosen configuration's trial   */
+} MuonBatchTuning;
+
+/* Copies the scenes (created on the current device by muon_gpu_scene_create;
+ * they stay usable and unchanged) into one device image: their BVHs side by
+ * side under separate roots, their materials, transforms and lights
+ * concatenated. Scenes are scheduled shortest first. */
+int muon_gpu_batch_create(MuonScene *const *scenes, int32_t n, MuonBatch **out);
+void muon_gpu_batch_destroy(MuonBatch *batch);
+/* Renders scene i with params[i] into film i (n entries each), like
+ * muon_gpu_render_device / muon_gpu_render per scene. params[i].wave_paths is
+ * ignored: the wavefront size is the batch's (autotuned or default). Every
+ * max_depth must be >= 0. */
+int muon_gpu_batch_render_device(MuonBatch *batch, const MuonRenderParams *params, double *const *d_sum,
+                                 double *const *d_sum_sq, uint32_t *const *d_count);
+int muon_gpu_batch_render(MuonBatch *batch, const MuonRenderParams *params, MuonFilm *films);
+/* Times candidate launch configurations (wavefront size x traversal grid) on
+ * a reduced-sample pass of the batch with these params, keeps the fastest for
+ * later renders of this batch and reports it. */
+int muon_gpu_batch_autotune(MuonBatch *batch, const MuonRenderParams *params, MuonBatchTuning *out);
+/* Totals of the last batched render and, if per_scene is not NULL, one entry
+ * per scene (in the order given to muon_gpu_batch_create). */
+int muon_gpu_batch_stats(const MuonBatch *batch, MuonStats *total, MuonBatchSceneStats *per_scene);
+/* One-shot form: create, render into host films, destroy. */
+int muon_gpu_render_batch(MuonScene *const *scenes, const MuonRenderParams *params, int32_t n, MuonFilm *films);
+
 /* The CUDA stream (cudaStream_t) all of this scene's work is launched on, for
  * callers that time or order work around it with CUDA events. */
 int muon_gpu_scene_stream(const MuonScene *scene, void **stream);

@@ -226,6 +226,60 @@ class Scene:
             pass
 
 
+class Batch:
+    """Several GPU scenes rendered by one wavefront (muon_gpu_batch_*)."""
+
+    def __init__(self, scenes: list[Scene]):
+        self.scenes = list(scenes)
+        hs = (C.c_void_p * len(self.scenes))(*[s._h for s in self.scenes])
+        h = C.c_void_p()
+        check(load().muon_gpu_batch_create(hs, len(self.scenes), C.byref(h)))
+        self._h = h
+
+    def _params(self, params):
+        arr = (native.RenderParams * len(self.scenes))()
+        for i, p in enumerate(params):
+            arr[i] = p
+        return arr
+
+    def render(self, params: list[native.RenderParams]) -> list[FilmResult]:
+        films = [FilmResult(np.zeros((s.height, s.width, 3)), np.zeros((s.height, s.width, 3)),
+                            np.zeros((s.height, s.width), dtype=np.uint32)) for s in self.scenes]
+        cf = (native.Film * len(films))(*[f._cfilm() for f in films])
+        check(load().muon_gpu_batch_render(self._h, self._params(params), cf))
+        return films
+
+    def render_device(self, params: list[native.RenderParams], d_sum: list[int], d_sum_sq: list[int],
+                      d_count: list[int]) -> None:
+        n = len(self.scenes)
+        arr = lambda xs: (C.c_void_p * n)(*[C.c_void_p(x) for x in xs])
+        check(load().muon_gpu_batch_render_device(self._h, self._params(params), arr(d_sum), arr(d_sum_sq),
+                                                  arr(d_count)))
+
+    def autotune(self, params: list[native.RenderParams]) -> dict:
+        t = native.BatchTuning()
+        check(load().muon_gpu_batch_autotune(self._h, self._params(params), C.byref(t)))
+        return {name: getattr(t, name) for name, _ in native.BatchTuning._fields_ if name != "pad"}
+
+    def stats(self) -> tuple[dict, list[dict]]:
+        s = native.Stats()
+        per = (native.BatchSceneStats * len(self.scenes))()
+        check(load().muon_gpu_batch_stats(self._h, C.byref(s), per))
+        total = {name: getattr(s, name) for name, _ in native.Stats._fields_}
+        return total, [{"primary_rays": x.primary_rays, "done_ms": x.done_ms} for x in per]
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            load().muon_gpu_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 def render_file(path: str, **overrides) -> tuple[FilmResult, float]:
     """Parses and renders a scene file; returns the film and the file's gamma."""
     scene = Scene.from_file(path)

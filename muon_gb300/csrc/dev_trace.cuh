@@ -320,8 +320,8 @@ struct TravState {
   int stack[kStackSize];
 };
 
-__device__ __forceinline__ void TravBegin(TravState &t, float tmax) {
-  t.node = 0;
+__device__ __forceinline__ void TravBegin(TravState &t, float tmax, int root) {
+  t.node = root;
   t.sp = 0;
   t.hit = -1;
   t.tmax = tmax;

@@ -1,0 +1,441 @@
+// Learned path guiding: network initialisation and packing, tensor-core
+// forward pass for given features, and the training step.
+//
+// Training is a hand-written FP32 pipeline over a batch of samples: the
+// forward pass layer by layer (inputs of every layer kept), the mixture loss
+// gradient per sample, the backward pass layer by layer, and weight gradients
+// as per-chunk partial sums reduced in a fixed order, so a step's gradients do
+// not depend on scheduling. Adam then updates the FP32 master weights, which
+// are repacked as the BF16 tensor-core operand layout for inference.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdint>
+
+#include "dev_common.cuh"
+#include "guide.h"
+#include "guide_mlp.cuh"
+
+namespace muon_gpu {
+
+namespace {
+
+using namespace guide;
+
+constexpr int kThreads = 256;
+constexpr int kChunk = 2048;  // samples per weight-gradient partial
+
+// ---- packing and initialisation ------------------------------------------------
+__global__ void PackKernel(const float *params, __nv_bfloat16 *wt, float *bias) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < kWtElems) {
+    int l = 0;
+    while (l + 1 < kLayers && i >= WtOffset(l + 1)) ++l;
+    const int local = i - WtOffset(l);
+    const int o = local / Stride(l), k = local % Stride(l);
+    float v = 0.0f;
+    if (k < In(l)) v = params[MasterOffset(l) + k * Out(l) + o];
+    wt[i] = __float2bfloat16_rn(v);
+  }
+  if (i < kBiasFloats) {
+    const int l = i < 4 * kWidth ? i / kWidth : kLayers - 1;
+    const int o = i - BiasOffset(l);
+    bias[i] = params[MasterOffset(l) + In(l) * Out(l) + o];
+  }
+}
+
+// He-uniform weights U(-sqrt(6 / fan_in), sqrt(6 / fan_in)), zero biases.
+__global__ void InitKernel(float *params, uint64_t seed) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= kParams) return;
+  int l = 0;
+  while (l + 1 < kLayers && i >= MasterOffset(l + 1)) ++l;
+  const int local = i - MasterOffset(l);
+  if (local >= In(l) * Out(l)) {
+    params[i] = 0.0f;
+    return;
+  }
+  Rng r(seed, 0, 0);
+  r.ctr = make_uint4(static_cast<uint32_t>(i), 0x6d6c70u, 0u, 0u);
+  const float lim = sqrtf(6.0f / static_cast<float>(In(l)));
+  params[i] = (2.0f * r.Next() - 1.0f) * lim;
+}
+
+// ---- tensor-core forward for given features ------------------------------------
+__global__ void __launch_bounds__(128) ForwardKernel(const __nv_bfloat16 *wt, const float *bias,
+                                                     const float *features, int n, float *out) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  LoadNetwork(wt, bias, smem);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  float *sfeat = reinterpret_cast<float *>(smem + kSmemBytes) + warp * (32 * kFeatures + 32 * kOut);
+  float *sout = sfeat + 32 * kFeatures;
+  __syncthreads();
+  const int base = (blockIdx.x * 4 + warp) * 32;
+  if (base >= n) return;  // whole warp leaves together
+  for (int d = 0; d < kFeatures; ++d) {
+    const int r = base + lane;
+    sfeat[lane * kFeatures + d] = r < n ? features[static_cast<int64_t>(r) * kFeatures + d] : 0.0f;
+  }
+  __syncwarp();
+  ForwardWarp(smem, [&](int r, int d) { return sfeat[r * kFeatures + d]; }, sout);
+  __syncwarp();
+  for (int k = lane; k < 32 * kOut; k += 32) {
+    const int r = base + k / kOut;
+    if (r < n) out[static_cast<int64_t>(r) * kOut + k % kOut] = sout[k];
+  }
+}
+
+// ---- training: forward ----------------------------------------------------------
+// y[b][n] = act(sum_k x[b][k] w[k][n] + bias[n]) for a tile of 64 samples;
+// with kBlob, x is the one-blob encoding of features (batch x 8).
+template <bool kBlob, bool kRelu>
+__global__ void __launch_bounds__(kThreads) FwdLayerKernel(const float *x, const float *w, const float *bias, int K,
+                                                           int N, float *y, int batch) {
+  __shared__ float xs[64][33];
+  __shared__ float ws[32][65];
+  const int tid = threadIdx.x, ty = tid >> 4, tx = tid & 15;
+  const int b0 = blockIdx.x * 64;
+  float acc[4][4] = {};
+  for (int k0 = 0; k0 < K; k0 += 32) {
+    for (int i = tid; i < 64 * 32; i += kThreads) {
+      const int r = i >> 5, c = i & 31, b = b0 + r, k = k0 + c;
+      float v = 0.0f;
+      if (b < batch) {
+        if (kBlob) v = Blob(x[static_cast<int64_t>(b) * kFeatures + k / kBins], k % kBins);
+        else v = x[static_cast<int64_t>(b) * K + k];
+      }
+      xs[r][c] = v;
+    }
+    for (int i = tid; i < 32 * 64; i += kThreads) {
+      const int r = i >> 6, c = i & 63;
+      ws[r][c] = c < N ? w[(k0 + r) * N + c] : 0.0f;
+    }
+    __syncthreads();
+#pragma unroll 8
+    for (int kk = 0; kk < 32; ++kk) {
+      float a[4], bb[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) a[i] = xs[ty * 4 + i][kk], bb[i] = ws[kk][tx * 4 + i];
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc[i][j] += a[i] * bb[j];
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const int b = b0 + ty * 4 + i;
+    if (b >= batch) continue;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int c = tx * 4 + j;
+      if (c >= N) continue;
+      float v = acc[i][j] + bias[c];
+      y[static_cast<int64_t>(b) * N + c] = kRelu ? fmaxf(v, 0.0f) : v;
+    }
+  }
+}
+
+// ---- training: loss ---------------------------------------------------------------
+// Replaces z (raw outputs) by d(mean loss)/dz and writes per-block loss sums.
+__global__ void __launch_bounds__(kThreads) LossKernel(float *z, const float *dirs, const float *weights, int batch,
+                                                       double *loss_out) {
+  __shared__ double red[kThreads];
+  const int b = blockIdx.x * kThreads + threadIdx.x;
+  double loss = 0.0;
+  if (b < batch) {
+    float *r = z + static_cast<int64_t>(b) * kOut;
+    const float wx = dirs[3 * b], wy = dirs[3 * b + 1], wz = dirs[3 * b + 2];
+    const float wt = weights[b];
+    float pi[kLobes], kap[kLobes], mu[kLobes][3], nrm[kLobes], cosw[kLobes], lpf[kLobes];
+    float amax = -INFINITY;
+    for (int i = 0; i < kLobes; ++i) amax = fmaxf(amax, r[5 * i]);
+    float s = 0.0f;
+    for (int i = 0; i < kLobes; ++i) s += expf(r[5 * i] - amax);
+    const float lse = amax + logf(s);
+    float lmax = -INFINITY;
+    for (int i = 0; i < kLobes; ++i) {
+      const float la = r[5 * i] - lse;  // log pi
+      pi[i] = expf(la);
+      float mx = r[5 * i + 1], my = r[5 * i + 2], mz = r[5 * i + 3];
+      float n2 = mx * mx + my * my + mz * mz;
+      nrm[i] = sqrtf(n2);
+      if (n2 > 1e-24f) {
+        mu[i][0] = mx / nrm[i], mu[i][1] = my / nrm[i], mu[i][2] = mz / nrm[i];
+      } else {
+        mu[i][0] = 0.0f, mu[i][1] = 0.0f, mu[i][2] = 1.0f;
+      }
+      const float bb = fminf(fmaxf(r[5 * i + 4], kBMin), kBMax);
+      kap[i] = expf(bb);
+      cosw[i] = mu[i][0] * wx + mu[i][1] * wy + mu[i][2] * wz;
+      const float logf_i = logf(kap[i]) - logf(2.0f * 3.14159265358979f) - logf(-expm1f(-2.0f * kap[i])) +
+                           kap[i] * (cosw[i] - 1.0f);
+      lpf[i] = la + logf_i;
+      lmax = fmaxf(lmax, lpf[i]);
+    }
+    float qs = 0.0f;
+    for (int i = 0; i < kLobes; ++i) qs += expf(lpf[i] - lmax);
+    const float logq = lmax + logf(qs);
+    loss = -static_cast<double>(wt) * logq;
+    const float coef = -wt / static_cast<float>(batch);
+    for (int i = 0; i < kLobes; ++i) {
+      const float resp = expf(lpf[i] - logq);
+      const float cr = coef * resp;
+      float g[5];
+      g[0] = coef * (resp - pi[i]);
+      if (nrm[i] * nrm[i] > 1e-24f) {
+        for (int c = 0; c < 3; ++c) {
+          const float w_c = c == 0 ? wx : (c == 1 ? wy : wz);
+          g[1 + c] = cr * kap[i] * (w_c - cosw[i] * mu[i][c]) / nrm[i];
+        }
+      } else {
+        g[1] = g[2] = g[3] = 0.0f;
+      }
+      const float e2 = expf(-2.0f * kap[i]);
+      const float dk = 1.0f / kap[i] - 2.0f * e2 / (-expm1f(-2.0f * kap[i])) + (cosw[i] - 1.0f);
+      const float braw = r[5 * i + 4];
+      g[4] = (braw > kBMin && braw < kBMax) ? cr * dk * kap[i] : 0.0f;
+      for (int c = 0; c < 5; ++c) r[5 * i + c] = g[c];
+    }
+  }
+  red[threadIdx.x] = loss;
+  __syncthreads();
+  for (int o = kThreads / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) loss_out[blockIdx.x] = red[0];
+}
+
+// ---- training: backward -------------------------------------------------------------
+// dx[b][k] = (sum_n dz[b][n] w[k][n]) * (h[b][k] > 0), K = 64, N <= 64.
+__global__ void __launch_bounds__(kThreads) BwdDataKernel(const float *dz, const float *w, const float *h, int N,
+                                                          float *dx, int batch) {
+  __shared__ float ds[64][65];
+  __shared__ float ws[64][65];
+  const int tid = threadIdx.x, ty = tid >> 4, tx = tid & 15;
+  const int b0 = blockIdx.x * 64;
+  for (int i = tid; i < 64 * 64; i += kThreads) {
+    const int r = i >> 6, c = i & 63, b = b0 + r;
+    ds[r][c] = (b < batch && c < N) ? dz[static_cast<int64_t>(b) * N + c] : 0.0f;
+    ws[r][c] = c < N ? w[r * N + c] : 0.0f;  // row k, column n
+  }
+  __syncthreads();
+  float acc[4][4] = {};
+  for (int n = 0; n < N; ++n) {
+    float a[4], bb[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) a[i] = ds[ty * 4 + i][n], bb[i] = ws[tx * 4 + i][n];
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+      for (int j = 0; j < 4; ++j) acc[i][j] += a[i] * bb[j];
+  }
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const int b = b0 + ty * 4 + i;
+    if (b >= batch) continue;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int k = tx * 4 + j;
+      const int64_t o = static_cast<int64_t>(b) * kWidth + k;
+      dx[o] = h[o] > 0.0f ? acc[i][j] : 0.0f;
+    }
+  }
+}
+
+// Per chunk of samples: partial[k * N + n] = sum_b x[b][k] dz[b][n] and the
+// bias part partial[K * N + n] = sum_b dz[b][n]. Each thread owns a TK x TN
+// block of outputs.
+template <bool kBlob, int K, int N, int TK, int TN>
+__global__ void __launch_bounds__(kThreads) WgradKernel(const float *x, const float *dz, int batch, float *partial,
+                                                        int stride, int layer_off) {
+  static_assert((K / TK) * (N / TN) == kThreads, "thread tiling");
+  __shared__ float xs[32][K + 1];
+  __shared__ float ds[32][N + 1];
+  const int tid = threadIdx.x;
+  const int kg = tid / (N / TN), ng = tid % (N / TN);
+  const int b0 = blockIdx.x * kChunk;
+  float acc[TK][TN] = {};
+  float bacc = 0.0f;
+  for (int s0 = b0; s0 < b0 + kChunk && s0 < batch; s0 += 32) {
+    for (int i = tid; i < 32 * K; i += kThreads) {
+      const int r = i / K, k = i % K, b = s0 + r;
+      float v = 0.0f;
+      if (b < batch) {
+        if (kBlob) v = Blob(x[static_cast<int64_t>(b) * kFeatures + k / kBins], k % kBins);
+        else v = x[static_cast<int64_t>(b) * K + k];
+      }
+      xs[r][k] = v;
+    }
+    for (int i = tid; i < 32 * N; i += kThreads) {
+      const int r = i / N, n = i % N, b = s0 + r;
+      ds[r][n] = b < batch ? dz[static_cast<int64_t>(b) * N + n] : 0.0f;
+    }
+    __syncthreads();
+    for (int r = 0; r < 32; ++r) {
+      float a[TK], d[TN];
+#pragma unroll
+      for (int i = 0; i < TK; ++i) a[i] = xs[r][kg * TK + i];
+#pragma unroll
+      for (int j = 0; j < TN; ++j) d[j] = ds[r][ng * TN + j];
+#pragma unroll
+      for (int i = 0; i < TK; ++i)
+#pragma unroll
+        for (int j = 0; j < TN; ++j) acc[i][j] += a[i] * d[j];
+    }
+    if (tid < N)
+      for (int r = 0; r < 32; ++r) bacc += ds[r][tid];
+    __syncthreads();
+  }
+  float *p = partial + static_cast<int64_t>(blockIdx.x) * stride + layer_off;
+#pragma unroll
+  for (int i = 0; i < TK; ++i)
+#pragma unroll
+    for (int j = 0; j < TN; ++j) p[(kg * TK + i) * N + ng * TN + j] = acc[i][j];
+  if (tid < N) p[K * N + tid] = bacc;
+}
+
+__global__ void ReduceKernel(const float *partial, int chunks, float *grad) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= kParams) return;
+  float s = 0.0f;
+  for (int c = 0; c < chunks; ++c) s += partial[static_cast<int64_t>(c) * kParams + i];
+  grad[i] = s;
+}
+
+// Adam (Kingma and Ba, 2015) with bias correction.
+__global__ void AdamKernel(float *params, float *m, float *v, const float *grad, float lr, float c1, float c2) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= kParams) return;
+  const float g = grad[i];
+  const float mi = 0.9f * m[i] + 0.1f * g;
+  const float vi = 0.999f * v[i] + 0.001f * g * g;
+  m[i] = mi;
+  v[i] = vi;
+  params[i] -= lr * (mi / c1) / (sqrtf(vi / c2) + 1e-8f);
+}
+
+// ---- sample gathering -----------------------------------------------------------------
+__global__ void GatherKernel(const GuideSample *pool, uint64_t available, uint32_t cap, int batch, uint64_t seed,
+                             float *features, float *dirs, float *weights) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= batch) return;
+  const uint64_t valid = available < cap ? available : cap;
+  Rng r(seed, 0, 0);
+  r.ctr = make_uint4(static_cast<uint32_t>(i), 0x67617468u, static_cast<uint32_t>(seed >> 32), 0u);
+  const uint64_t j = static_cast<uint64_t>(r.Next() * static_cast<float>(valid)) % (valid ? valid : 1);
+  const GuideSample s = pool[j];
+  float *f = features + static_cast<int64_t>(i) * kFeatures;
+  f[0] = s.f0.x, f[1] = s.f0.y, f[2] = s.f0.z, f[3] = s.f0.w;
+  f[4] = s.f1.x, f[5] = s.f1.y, f[6] = s.f1.z, f[7] = s.f1.w;
+  dirs[3 * i] = s.dir_w.x, dirs[3 * i + 1] = s.dir_w.y, dirs[3 * i + 2] = s.dir_w.z;
+  weights[i] = s.dir_w.w;
+}
+
+// Divides the weights by their mean (one block; fixed summation order).
+__global__ void __launch_bounds__(1024) NormaliseKernel(float *weights, int batch) {
+  __shared__ double red[1024];
+  double s = 0.0;
+  for (int i = threadIdx.x; i < batch; i += 1024) s += weights[i];
+  red[threadIdx.x] = s;
+  __syncthreads();
+  for (int o = 512; o > 0; o >>= 1) {
+    if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+    __syncthreads();
+  }
+  const double mean = red[0] / static_cast<double>(batch);
+  const float inv = mean > 0.0 ? static_cast<float>(1.0 / mean) : 0.0f;
+  for (int i = threadIdx.x; i < batch; i += 1024) weights[i] *= inv;
+}
+
+inline unsigned Grid(int64_t n, int block) { return static_cast<unsigned>((n + block - 1) / block); }
+
+}  // namespace
+
+void LaunchGuidePack(const float *params, void *wt, float *bias, cudaStream_t st) {
+  PackKernel<<<Grid(std::max(kWtElems, kBiasFloats), 256), 256, 0, st>>>(params, static_cast<__nv_bfloat16 *>(wt),
+                                                                        bias);
+}
+
+void LaunchGuideInit(float *params, uint64_t seed, cudaStream_t st) {
+  InitKernel<<<Grid(kParams, 256), 256, 0, st>>>(params, seed);
+}
+
+void LaunchGuideForward(const void *wt, const float *bias, const float *features, int n, float *out,
+                        cudaStream_t st) {
+  if (n <= 0) return;
+  const int smem = kSmemBytes + 4 * (32 * kFeatures + 32 * kOut) * 4;
+  cudaFuncSetAttribute(ForwardKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  ForwardKernel<<<Grid(n, 128), 128, smem, st>>>(static_cast<const __nv_bfloat16 *>(wt), bias, features, n, out);
+}
+
+size_t GuideTrainBytes(int batch) {
+  const size_t chunks = (batch + kChunk - 1) / kChunk;
+  return sizeof(float) * (4ull * batch * kWidth + static_cast<size_t>(batch) * kOut + 2ull * batch * kWidth +
+                          chunks * kParams + kParams) +
+         sizeof(double) * (batch / kThreads + 2) + 256 * 8;
+}
+
+void GuideTrainCarve(void *base, int batch, GuideTrainBuffers *out) {
+  char *p = static_cast<char *>(base);
+  auto take = [&](size_t bytes) {
+    char *r = p;
+    p += (bytes + 255) / 256 * 256;
+    return r;
+  };
+  out->h[0] = nullptr;
+  for (int l = 1; l < 5; ++l) out->h[l] = reinterpret_cast<float *>(take(sizeof(float) * batch * kWidth));
+  out->z = reinterpret_cast<float *>(take(sizeof(float) * batch * kOut));
+  out->dz[0] = reinterpret_cast<float *>(take(sizeof(float) * batch * kWidth));
+  out->dz[1] = reinterpret_cast<float *>(take(sizeof(float) * batch * kWidth));
+  out->chunks = (batch + kChunk - 1) / kChunk;
+  out->partial = reinterpret_cast<float *>(take(sizeof(float) * out->chunks * kParams));
+  out->grad = reinterpret_cast<float *>(take(sizeof(float) * kParams));
+  out->loss = reinterpret_cast<double *>(take(sizeof(double) * (batch / kThreads + 2)));
+}
+
+void LaunchGuideGradients(const float *params, const float *features, const float *dirs, const float *weights,
+                          int batch, const GuideTrainBuffers &tb, cudaStream_t st) {
+  const unsigned tiles = Grid(batch, 64);
+  auto W = [&](int l) { return params + MasterOffset(l); };
+  auto B = [&](int l) { return params + MasterOffset(l) + In(l) * Out(l); };
+  FwdLayerKernel<true, true><<<tiles, kThreads, 0, st>>>(features, W(0), B(0), kIn, kWidth, tb.h[1], batch);
+  for (int l = 1; l < 4; ++l)
+    FwdLayerKernel<false, true><<<tiles, kThreads, 0, st>>>(tb.h[l], W(l), B(l), kWidth, kWidth, tb.h[l + 1], batch);
+  FwdLayerKernel<false, false><<<tiles, kThreads, 0, st>>>(tb.h[4], W(4), B(4), kWidth, kOut, tb.z, batch);
+  LossKernel<<<Grid(batch, kThreads), kThreads, 0, st>>>(tb.z, dirs, weights, batch, tb.loss);
+  const unsigned chunks = static_cast<unsigned>(tb.chunks);
+  // layer 4: 64 x 40
+  WgradKernel<false, kWidth, kOut, 2, 5><<<chunks, kThreads, 0, st>>>(tb.h[4], tb.z, batch, tb.partial, kParams,
+                                                                       MasterOffset(4));
+  BwdDataKernel<<<tiles, kThreads, 0, st>>>(tb.z, W(4), tb.h[4], kOut, tb.dz[0], batch);
+  // layers 3..1: 64 x 64
+  int cur = 0;
+  for (int l = 3; l >= 1; --l) {
+    WgradKernel<false, kWidth, kWidth, 4, 4><<<chunks, kThreads, 0, st>>>(tb.h[l], tb.dz[cur], batch, tb.partial,
+                                                                         kParams, MasterOffset(l));
+    BwdDataKernel<<<tiles, kThreads, 0, st>>>(tb.dz[cur], W(l), tb.h[l], kWidth, tb.dz[cur ^ 1], batch);
+    cur ^= 1;
+  }
+  // layer 0: one-blob input, 256 x 64
+  WgradKernel<true, kIn, kWidth, 8, 8><<<chunks, kThreads, 0, st>>>(features, tb.dz[cur], batch, tb.partial,
+                                                                    kParams, MasterOffset(0));
+  ReduceKernel<<<Grid(kParams, 256), 256, 0, st>>>(tb.partial, tb.chunks, tb.grad);
+}
+
+void LaunchGuideGather(const GuideSample *pool, uint64_t available, uint32_t cap, int batch, uint64_t seed,
+                       float *features, float *dirs, float *weights, cudaStream_t st) {
+  GatherKernel<<<Grid(batch, 256), 256, 0, st>>>(pool, available, cap, batch, seed, features, dirs, weights);
+  NormaliseKernel<<<1, 1024, 0, st>>>(weights, batch);
+}
+
+void LaunchGuideAdam(float *params, float *m, float *v, const float *grad, float lr, int step, cudaStream_t st) {
+  const float c1 = 1.0f - powf(0.9f, static_cast<float>(step));
+  const float c2 = 1.0f - powf(0.999f, static_cast<float>(step));
+  AdamKernel<<<Grid(kParams, 256), 256, 0, st>>>(params, m, v, grad, lr, c1, c2);
+}
+
+}  // namespace muon_gpu

@@ -1,0 +1,86 @@
+// Learned path guiding: structures shared by the host code and the kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "kernels.cuh"
+
+namespace muon_gpu {
+
+// What a guided render leaves behind for one path vertex whose path
+// continued: its features, the sampled direction, the throughput before the
+// vertex and the radiance the path had collected once the vertex's direct
+// light was added. Together with the path's final radiance this gives the
+// training target of the direction (see GuideCollect).
+struct GuideRec {
+  float4 f0, f1;   // features 0-3, 4-7
+  float4 dir;      // xyz, w = path id word
+  float4 tp;       // throughput before the vertex; w = 1 when recorded
+  float4 after;    // radiance after the vertex's direct light
+};
+
+// One training sample: features, direction and weight (target / density).
+struct GuideSample {
+  float4 f0, f1;
+  float4 dir_w;
+};
+
+// Device view of a guide for the render kernels.
+struct GuideDev {
+  const void *wt;        // BF16 transposed network weights (guide::WtOffset layout)
+  const float *bias;     // FP32 biases (guide::BiasOffset layout)
+  float4 *mix;           // 10 per queue entry: the processed mixture
+  float4 *feat;          // 2 per queue entry: the features
+  GuideRec *rec;         // rec_bounces x rec_cap
+  int32_t rec_cap;       // entries per bounce (the wave's capacity)
+  int32_t rec_bounces;   // bounces recorded for training
+  float alpha;           // probability of sampling the mixture instead of the BRDF
+  float lo[3], inv_ext[3];  // scene box: feature = (p - lo) * inv_ext
+  GuideSample *pool;     // training samples (ring buffer)
+  unsigned long long *pool_count;  // samples ever appended
+  uint32_t pool_cap;
+  int32_t pad;
+};
+
+// Kernels of the guided render (kernels.cu).
+void LaunchGuideInfer(const DevScene &s, const PathBuffers &b, WaveCounters wc, int bounce, int bound, int isect,
+                      const GuideDev &g, cudaStream_t st);
+void LaunchShadePathGuided(const DevScene &s, const WaveInfo &w, const ShadeParams &sp, const PathBuffers &b,
+                           WaveCounters wc, int bounce, int bound, const GuideDev &g, cudaStream_t st);
+void LaunchFoldGuided(const PathBuffers &b, WaveCounters wc, int bounce, int slots, int bound, const GuideDev &g,
+                      cudaStream_t st);
+void LaunchGuideCollect(const PathBuffers &b, WaveCounters wc, int bounces, int bound, const GuideDev &g,
+                        cudaStream_t st);
+
+// Training and network kernels (guide.cu). `params` is the FP32 master copy
+// (guide::MasterOffset layout).
+void LaunchGuidePack(const float *params, void *wt, float *bias, cudaStream_t st);
+void LaunchGuideInit(float *params, uint64_t seed, cudaStream_t st);
+// Network outputs (n x 40) for features (n x 8) on the tensor-core path.
+void LaunchGuideForward(const void *wt, const float *bias, const float *features, int n, float *out,
+                        cudaStream_t st);
+
+// Working memory of one training step over `batch` samples.
+struct GuideTrainBuffers {
+  float *h[5];      // inputs of layers 1..4 (h[0] unused: the one-blob input is recomputed), batch x 64
+  float *z;         // batch x 40 outputs, then their gradients
+  float *dz[2];     // batch x 64 gradients (ping-pong)
+  float *partial;   // per chunk: all weight and bias gradients
+  float *grad;      // guide::kParams
+  double *loss;     // one value per chunk
+  int32_t chunks;
+};
+size_t GuideTrainBytes(int batch);
+void GuideTrainCarve(void *base, int batch, GuideTrainBuffers *out);
+// Gradients of the mean loss over the batch into tb.grad; loss into *loss_out
+// (device double) when not null.
+void LaunchGuideGradients(const float *params, const float *features, const float *dirs, const float *weights,
+                          int batch, const GuideTrainBuffers &tb, cudaStream_t st);
+// Gathers `batch` samples from the pool at random positions (seeded) into
+// features / dirs / weights (weights normalised by their batch mean).
+void LaunchGuideGather(const GuideSample *pool, uint64_t available, uint32_t cap, int batch, uint64_t seed,
+                       float *features, float *dirs, float *weights, cudaStream_t st);
+void LaunchGuideAdam(float *params, float *m, float *v, const float *grad, float lr, int step, cudaStream_t st);
+
+}  // namespace muon_gpu

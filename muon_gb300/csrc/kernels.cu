@@ -22,6 +22,8 @@
 #include "dev_shade.cuh"
 #include "dev_trace.cuh"
 #include "kernels.cuh"
+#include "guide.h"
+#include "guide_mlp.cuh"
 
 namespace muon_gpu {
 
@@ -194,23 +196,35 @@ __device__ __forceinline__ T *Pick(T *const (&a)[2], int i) {
   return i ? a[1] : a[0];
 }
 
+__device__ __forceinline__ int PathOf(float id) { return static_cast<int>(__float_as_uint(id) & kPathMask); }
+__device__ __forceinline__ int SegOf(float id) { return static_cast<int>(__float_as_uint(id) >> kPathBits); }
+
+// Index of the last segment whose `field` start is <= i (segments are in
+// ascending order of both path0 and pix0).
+template <int32_t BatchSeg::*kField>
+__device__ __forceinline__ int FindSeg(const BatchSeg *segs, int nseg, int i) {
+  int lo = 0, hi = nseg - 1;
+  while (lo < hi) {
+    int mid = (lo + hi + 1) >> 1;
+    if (__ldg(&(segs[mid].*kField)) <= i) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
 // ---- camera ------------------------------------------------------------
 // Sampler::NextSample (muon/sampling.cc:80-121): sample 0 at the pixel centre,
 // later samples jittered uniformly inside the pixel. Fills bounce 0's queue in
 // path order and clears each path's final radiance.
-__global__ void __launch_bounds__(kBlock) CameraKernel(DevCamera cam, WaveInfo w, PathBuffers b, WaveCounters wc) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i == 0) *wc.count(0) = static_cast<uint32_t>(w.n);
-  if (i >= w.n) return;
-  int pixel = w.p0 + i / w.ns;
-  uint32_t sample = w.sample_offset + static_cast<uint32_t>(w.s0 + i % w.ns);
-  int px = pixel % w.width, py = pixel / w.width;
+__device__ __forceinline__ void CameraSample(const DevCamera &cam, int width, uint64_t seed, int pixel,
+                                             uint32_t sample, float3 *o, float3 *d) {
+  int px = pixel % width, py = pixel / width;
   float x, y;
   if (sample == 0) {
     x = mm::add(static_cast<float>(px), 0.5f);
     y = mm::add(static_cast<float>(py), 0.5f);
   } else {
-    Rng rng(w.seed, 0, 0xffffffffu);
+    Rng rng(seed, 0, 0xffffffffu);
     rng.ctr = make_uint4(sample, static_cast<uint32_t>(pixel), 0xffffffffu, 0u);
     float u = rng.Next(), v = rng.Next();
     float fx = static_cast<float>(px), fy = static_cast<float>(py);
@@ -219,13 +233,43 @@ __global__ void __launch_bounds__(kBlock) CameraKernel(DevCamera cam, WaveInfo w
     if (x == mm::add(fx, 1.0f)) x = nextafterf(x, -INFINITY);
     if (y == mm::add(fy, 1.0f)) y = nextafterf(y, -INFINITY);
   }
-  float3 o, d;
-  CastRay(cam, x, y, &o, &d);
-  b.ray_o[0][i] = make_float4(o.x, o.y, o.z, __int_as_float(i));
-  b.ray_d[0][i] = make_float4(d.x, d.y, d.z, INFINITY);
+  CastRay(cam, x, y, o, d);
+}
+
+// Writes bounce 0's queue entry i: the ray, its id word and its BVH root.
+__device__ __forceinline__ void StartPath(const PathBuffers &b, int i, uint32_t id, int root, float3 o, float3 d) {
+  b.ray_o[0][i] = make_float4(o.x, o.y, o.z, __uint_as_float(id));
+  b.ray_d[0][i] = make_float4(d.x, d.y, d.z, __int_as_float(root));
   b.tp[0][i] = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
   b.rad[0][i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
   b.final_rad[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+}
+
+__global__ void __launch_bounds__(kBlock) CameraKernel(DevCamera cam, WaveInfo w, PathBuffers b, WaveCounters wc) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i == 0) *wc.count(0) = static_cast<uint32_t>(w.n);
+  if (i >= w.n) return;
+  int pixel = w.p0 + i / w.ns;
+  uint32_t sample = w.sample_offset + static_cast<uint32_t>(w.s0 + i % w.ns);
+  float3 o, d;
+  CameraSample(cam, w.width, w.seed, pixel, sample, &o, &d);
+  StartPath(b, i, static_cast<uint32_t>(i), 0, o, d);
+}
+
+__global__ void __launch_bounds__(kBlock) CameraBatchKernel(const BatchScene *scenes, const BatchSeg *segs, int nseg,
+                                                            int paths, PathBuffers b, WaveCounters wc) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i == 0) *wc.count(0) = static_cast<uint32_t>(paths);
+  if (i >= paths) return;
+  const int k = FindSeg<&BatchSeg::path0>(segs, nseg, i);
+  const BatchSeg sg = segs[k];
+  const BatchScene &sc = scenes[sg.scene];
+  const int local = i - sg.path0;
+  int pixel = sg.p0 + local / sg.ns;
+  uint32_t sample = sc.sample_offset + static_cast<uint32_t>(sg.s0 + local % sg.ns);
+  float3 o, d;
+  CameraSample(sc.cam, sc.width, sc.seed, pixel, sample, &o, &d);
+  StartPath(b, i, static_cast<uint32_t>(i) | (static_cast<uint32_t>(k) << kPathBits), sg.root, o, d);
 }
 
 // ---- extend / occlude ------------------------------------------------------
@@ -257,9 +301,10 @@ __device__ __forceinline__ void PersistentTraverse(const DevScene &s, int n, uin
           ray = static_cast<int>(mine);
           float3 o, d;
           float tmax;
-          load(ray, &o, &d, &tmax);
+          int root;
+          load(ray, &o, &d, &tmax, &root);
           r = Prepare<kMode>(o, d);
-          TravBegin(t, tmax);
+          TravBegin(t, tmax, root);
         } else {
           exhausted = true;
         }
@@ -282,11 +327,12 @@ __global__ void __launch_bounds__(kBlock) ExtendKernel(DevScene s, PathBuffers b
   bool overflow = false;
   PersistentTraverse<false, kStats, kTri>(
       s, n, wc.fetch_extend(bounce),
-      [&](int j, float3 *o, float3 *d, float *tmax) {
+      [&](int j, float3 *o, float3 *d, float *tmax, int *root) {
         float4 o4 = ray_o[j], d4 = ray_d[j];
         *o = f3(o4.x, o4.y, o4.z);
         *d = f3(d4.x, d4.y, d4.z);
-        *tmax = d4.w;
+        *tmax = INFINITY;
+        *root = __float_as_int(d4.w);
       },
       [&](int j, const TravState &t) {
         b.hits[j] = make_int2(__float_as_int(kTri == MUON_ISECT_EXACT ? t.t_obj : t.tmax), t.hit);
@@ -327,12 +373,13 @@ __global__ void __launch_bounds__(kBlock) OccludeKernel(DevScene s, PathBuffers 
   bool overflow = false;
   PersistentTraverse<true, kStats, kTri>(
       s, n, wc.fetch_occlude(bounce),
-      [&](int j, float3 *o, float3 *d, float *tmax) {
+      [&](int j, float3 *o, float3 *d, float *tmax, int *root) {
         uint32_t slot = b.shq[j];
         float4 o4 = b.org[slot / slots], d4 = b.slot_dir[slot];
         *o = f3(o4.x, o4.y, o4.z);
         *d = f3(d4.x, d4.y, d4.z);
         *tmax = d4.w;
+        *root = __float_as_int(o4.w);
       },
       [&](int j, const TravState &t) {
         if (t.hit >= 0) b.contrib[b.shq[j]] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
@@ -355,7 +402,7 @@ __global__ void __launch_bounds__(kBlock) ShadeDebugKernel(DevScene s, PathBuffe
   const int n = static_cast<int>(*wc.count(0));
   for (int j = blockIdx.x * kBlock + threadIdx.x; j < n; j += gridDim.x * kBlock) {
     float4 o4 = b.ray_o[0][j], d4 = b.ray_d[0][j];
-    int path = __float_as_int(o4.w);
+    int path = PathOf(o4.w);
     int2 h = b.hits[j];
     float4 out = make_float4(0, 0, 0, 0);
     if (h.y >= 0) {
@@ -491,7 +538,10 @@ __global__ void __launch_bounds__(kBlock) WhittedKernel(DevScene s, PathBuffers 
           }
           v3 dc = kd * GlmMax(dot(n, info.dir), 0.0f);
           v3 half = normalize(info.dir - rd);
-          v3 sc = kspec * powf(GlmMax(dot(n, half), 0.0f), kd4.w);
+          // pow in double rounded to float: the correctly rounded value,
+          // which the host libm's powf also returns on all but rare inputs.
+          v3 sc = kspec * static_cast<float>(pow(static_cast<double>(GlmMax(dot(n, half), 0.0f)),
+                                                 static_cast<double>(kd4.w)));
           color = color + info.color * (dc + sc);
         }
         if (kspec.x > 0.0f || kspec.y > 0.0f || kspec.z > 0.0f) {
@@ -542,9 +592,215 @@ constexpr int kMaskSlots = 64;
 #define MUON_SHADE_MIN_BLOCKS 2
 #endif
 
+// ---- guided sampling ----------------------------------------------------------------
+// Direction sampling of a guided render: with probability alpha from the
+// learned mixture of the vertex, else from the render's own sampler
+// (hemisphere, cosine or BRDF); the sample is weighted by the density of the
+// combination (one-sample MIS, balance heuristic), so the estimator stays
+// unbiased whatever the network predicts. Light-sample MIS weights use the
+// same combined density.
+__device__ __forceinline__ float GuidedPdf(const GuideDev *g, const float *mx, float base_pdf, float3 w) {
+  return g->alpha * guide::MixturePdf(mx, w.x, w.y, w.z) + (1.0f - g->alpha) * base_pdf;
+}
+
+__device__ __forceinline__ bool SampleGuided(const GuideDev *g, const float *mx, int mode, const Mat &m, float3 n,
+                                             float3 ray_dir, float3 tp, Rng &rng, float3 *dir, float *pdf,
+                                             float3 *next_tp) {
+  float3 w;
+  if (rng.Next() < g->alpha) {
+    const float u0 = rng.Next(), u1 = rng.Next(), u2 = rng.Next();
+    guide::SampleMixture(mx, u0, u1, u2, &w.x, &w.y, &w.z);
+  } else if (mode == MUON_IS_HEMISPHERE) {
+    w = SampleHemisphere(n, rng);
+  } else if (mode == MUON_IS_COSINE) {
+    w = SampleCosine(n, rng);
+  } else {
+    w = BrdfSample(m, ray_dir, n, rng);
+  }
+  const float cosn = dot3(w, n);
+  if (cosn <= 0.0f) return false;
+  const float p = GuidedPdf(g, mx, IsPdf(mode, m, w, ray_dir, n), w);
+  if (!(p > 0.0f)) return false;
+  *next_tp = tp * BrdfEval(m, w, ray_dir, n) * (cosn / p);
+  *dir = w;
+  *pdf = p;
+  return true;
+}
+
+// Shading of one queued hit (PathTracer::Shade); `local` is the path's index
+// in its wave (or batch segment), which seeds its random numbers.
+struct ShadeOut {
+  uint32_t want_cont = 0, nshadow = 0;
+  unsigned long long mask = 0;  // nonzero slots (first 64)
+  float3 cont_o, cont_d, cont_tp;
+};
+
 template <int kMode>
-__global__ void __launch_bounds__(kBlock, MUON_SHADE_MIN_BLOCKS) ShadePathKernel(DevScene s, WaveInfo w, ShadeParams sp, PathBuffers b,
-                                                          WaveCounters wc, int bounce) {
+__device__ __forceinline__ void ShadeEntry(const DevScene &s, const WaveInfo &w, const ShadeParams &sp,
+                                           const PathBuffers &b, int cur, int bounce, int S, int jj, float4 o4,
+                                           float4 d4, int local, unsigned long long &counted, ShadeOut &out,
+                                           const GuideDev *gd) {
+    // the vertex's learned mixture when guided
+    const float *mx = gd ? reinterpret_cast<const float *>(gd->mix + 10 * static_cast<int64_t>(jj)) : nullptr;
+    const float3 o = f3(o4.x, o4.y, o4.z), d = f3(d4.x, d4.y, d4.z);
+    const int2 h = b.hits[jj];
+    float4 *contrib = b.contrib + static_cast<int64_t>(jj) * S;
+    float4 *sdir = b.slot_dir + static_cast<int64_t>(jj) * S;
+    for (int k = 0; k < S; ++k) contrib[k] = make_float4(0, 0, 0, 0);
+    float3 L = f3(Pick(b.rad, cur)[jj]);
+    const float3 tp = f3(Pick(b.tp, cur)[jj]);
+
+    if (h.y >= 0) {
+      float3 p, nrm;
+      float hit_dist;
+      int mat_id, light_id, pid;
+      Surface<kMode>(s, h.y, o, d, __int_as_float(h.x), &p, &nrm, &hit_dist, &mat_id, &light_id, &pid);
+      const Mat m = LoadMat(s.materials, mat_id);
+      const float3 shift = p + kEps * nrm;
+      Rng rng = MakeRng(w, local, static_cast<uint32_t>(bounce));
+      const bool direct = bounce >= sp.min_depth;
+      const bool mis = direct && sp.nee == MUON_NEE_MIS;
+
+      if (direct) {
+        // Emission: only at the first vertex when lights are sampled, and
+        // only from the front face (muon/integration.cc:257-264).
+        if ((sp.nee == MUON_NEE_OFF || bounce == 0) && !(dot3(nrm, -d) < 0.0f)) L = L + tp * m.ke;
+        if (sp.nee != MUON_NEE_OFF) {
+          int slot = 0;
+          // Area lights: ShadeDirectNEE (muon/integration.cc:371-462).
+#pragma unroll 1
+          for (int li = 0; li < s.num_lights; ++li) {
+            const DevLight &l = s.lights[li];
+            const float3 corner = f3(l.corner), e0 = f3(l.edge0), e1 = f3(l.edge1), rev = f3(l.rev_normal);
+            const float3 lcol = f3(l.color) * (l.color.w / static_cast<float>(sp.light_samples));
+            const float inv_strata = 1.0f / static_cast<float>(sp.strata);
+#pragma unroll 1
+            for (int q = 0; q < sp.per_light; ++q, ++slot) {
+              const int si = (q / sp.per_section) / sp.strata, sj = (q / sp.per_section) % sp.strata;
+              float u = rng.Next(), v = rng.Next();
+              float fu = (static_cast<float>(si) + u) * inv_strata;
+              float fv = (static_cast<float>(sj) + v) * inv_strata;
+              float3 ptl = corner + fu * e0 + fv * e1 - kEps * rev - shift;
+              float dist = sqrtf(dot3(ptl, ptl));
+              float3 ldir = ptl * (1.0f / dist);
+              float ci = fmaxf(dot3(nrm, ldir), 0.0f);
+              float cl = fmaxf(dot3(rev, ldir), 0.0f);
+              if (ci == 0.0f || cl == 0.0f) continue;
+              float3 c = BrdfEval(m, ldir, d, nrm) * (ci * cl / (dist * dist));
+              if (mis) {
+                float bp = IsPdf(sp.is_mode, m, ldir, d, nrm);
+                if (gd) bp = GuidedPdf(gd, mx, bp, ldir);
+                c = c * PowerHeuristic(NeePdf(s, shift, ldir), bp);
+              }
+              c = tp * lcol * c;
+              if (!nonzero3(c)) continue;
+              contrib[slot] = make_float4(c.x, c.y, c.z, 0.0f);
+              sdir[slot] = make_float4(ldir.x, ldir.y, ldir.z, dist);
+              ++out.nshadow;
+              if (slot < kMaskSlots) out.mask |= 1ull << slot;
+            }
+          }
+          // Point and directional lights (muon/integration.cc:350-369,
+          // muon/lighting.cc:38-64).
+#pragma unroll 1
+          for (int li = 0; li < s.num_other_lights; ++li, ++slot) {
+            const DevLight &l = s.other_lights[li];
+            float3 lcol = f3(l.color);
+            float3 ldir;
+            float dist;
+            if (__float_as_int(l.corner.w) == MUON_LIGHT_POINT) {
+              float3 ptl = f3(l.corner) - p;
+              ldir = normalize3(ptl);
+              dist = length3(ptl);
+              float att = l.edge0.x + l.edge0.y * dist + l.edge0.z * dist * dist;
+              lcol = lcol / att;
+              lcol = lcol / (dist * dist);
+            } else {
+              ldir = f3(l.corner);
+              dist = INFINITY;
+            }
+            float ci = fmaxf(dot3(nrm, ldir), 0.0f);
+            float3 c = tp * lcol * BrdfEval(m, ldir, d, nrm) * ci;
+            if (!nonzero3(c)) continue;
+            contrib[slot] = make_float4(c.x, c.y, c.z, 0.0f);
+            sdir[slot] = make_float4(ldir.x, ldir.y, ldir.z, dist);
+            ++out.nshadow;
+            if (slot < kMaskSlots) out.mask |= 1ull << slot;
+          }
+        }
+      }
+      // Two BRDF samples share one code path: first the MIS light-hit ray
+      // (ShadeDirectImportanceSampling, muon/integration.cc:468-501), then
+      // the continuation (ShadeIndirect, muon/integration.cc:294-328).
+#pragma unroll 1
+      for (int pass = mis ? 0 : 1; pass < 2; ++pass) {
+        float3 dir, ntp;
+        float pdf;
+        if (!(gd ? SampleGuided(gd, mx, sp.is_mode, m, nrm, d, tp, rng, &dir, &pdf, &ntp)
+                 : SampleReflection(sp.is_mode, m, nrm, d, tp, rng, &dir, &pdf, &ntp)))
+          continue;
+        if (pass == 0) {
+          ++counted;
+          // The sampled ray's closest hit is a light triangle exactly when
+          // some light triangle is hit at t_L and nothing is hit before
+          // t_L: an any-hit query up to t_L, none if no light is met. Same
+          // triangle test and ray preparation as the traversal, so t_L is
+          // bit-identical to what the query compares against.
+          float best = INFINITY;
+          int best_light = -1;
+          RayPre rp = Prepare<kMode>(shift, dir);
+          const PrimRecord *lts = kMode == MUON_ISECT_EXACT ? s.light_tris_obj : s.light_tris;
+#pragma unroll 1
+          for (int lt = 0; lt < 2 * s.num_lights; ++lt) {
+            if (!s.light_tri_ok[lt]) continue;
+            PrimRecord lp = LoadPrim(lts, lt);
+            float t_obj;
+            float t = PrimTest<kMode>(s, rp, lp, __float_as_uint(lp.p3.w), &t_obj);
+            if (t > 0.0f && t < best) best = t, best_light = lt >> 1;
+          }
+          if (best_light < 0) continue;
+          float3 c = ntp * f3(s.lights[best_light].color) * PowerHeuristic(pdf, NeePdf(s, shift, dir));
+          if (!nonzero3(c)) continue;
+          const int slot = sp.mis_slot;
+          contrib[slot] = make_float4(c.x, c.y, c.z, 0.0f);
+          sdir[slot] = make_float4(dir.x, dir.y, dir.z, best);
+          ++out.nshadow;
+          if (slot < kMaskSlots) out.mask |= 1ull << slot;
+        } else {
+          bool survive = true;
+          if (sp.rr) {
+            float q = fminf(max3c(ntp), 1.0f);
+            if (q < rng.Next()) survive = false;
+            else ntp = ntp / q;
+          }
+          const int next_depth = bounce + 1;
+          const bool depth_ok = sp.max_trace_depth < 0 || next_depth <= sp.max_trace_depth;
+          if (survive && depth_ok && next_depth < sp.max_bounces) {
+            out.want_cont = 1;
+            ++counted;
+            out.cont_o = shift;
+            out.cont_d = dir;
+            out.cont_tp = ntp;
+            if (gd && bounce < gd->rec_bounces) {
+              // training record; the fold adds the radiance after this vertex
+              GuideRec &r = gd->rec[static_cast<int64_t>(bounce) * gd->rec_cap + jj];
+              r.f0 = gd->feat[2 * static_cast<int64_t>(jj)];
+              r.f1 = gd->feat[2 * static_cast<int64_t>(jj) + 1];
+              r.dir = make_float4(dir.x, dir.y, dir.z, o4.w);
+              r.tp = make_float4(tp.x, tp.y, tp.z, 1.0f);
+            }
+          }
+        }
+      }
+      if (out.nshadow) b.org[jj] = make_float4(shift.x, shift.y, shift.z, d4.w);  // w: BVH root
+    }
+    Pick(b.rad, cur)[jj] = make_float4(L.x, L.y, L.z, 0.0f);
+}
+
+template <int kMode, bool kBatch, bool kGuide>
+__global__ void __launch_bounds__(kBlock, MUON_SHADE_MIN_BLOCKS)
+    ShadePathKernel(DevScene s, WaveInfo w, ShadeParams sp, PathBuffers b, WaveCounters wc, int bounce,
+                    const BatchScene *bscenes, const BatchSeg *segs, int slot_stride, GuideDev gdev) {
   // Hits of this bounce, grouped by shading class: position i of the
   // concatenated class lists is entry order[c * cap + (i - start[c])].
   __shared__ uint32_t class_start[kNumClasses + 1];
@@ -559,7 +815,7 @@ __global__ void __launch_bounds__(kBlock, MUON_SHADE_MIN_BLOCKS) ShadePathKernel
   __syncthreads();
   const int n = static_cast<int>(class_start[kNumClasses]);
   const int cur = bounce & 1, nxt = cur ^ 1;
-  const int S = sp.slots;
+  const int S = slot_stride;
   unsigned long long counted = 0;  // secondary rays in the reference's sense
   QUEUE_LOOP(j, n) {
     const int ii = j_base + threadIdx.x;
@@ -570,169 +826,53 @@ __global__ void __launch_bounds__(kBlock, MUON_SHADE_MIN_BLOCKS) ShadePathKernel
       while (c + 1 < kNumClasses && static_cast<uint32_t>(ii) >= class_start[c + 1]) ++c;
       jj = b.order[static_cast<int64_t>(c) * b.order_cap + (ii - static_cast<int>(class_start[c]))];
     }
-    uint32_t want_cont = 0, nshadow = 0;
-    unsigned long long mask = 0;  // nonzero slots (first 64)
-    int path = 0;
-    float3 cont_o = f3(0, 0, 0), cont_d = f3(0, 0, 0), cont_tp = f3(0, 0, 0);
+    ShadeOut so;
+    float id = 0.0f, root = 0.0f;
     if (active) {
       const float4 o4 = Pick(b.ray_o, cur)[jj], d4 = Pick(b.ray_d, cur)[jj];
-      path = __float_as_int(o4.w);
-      const float3 o = f3(o4.x, o4.y, o4.z), d = f3(d4.x, d4.y, d4.z);
-      const int2 h = b.hits[jj];
-      float4 *contrib = b.contrib + static_cast<int64_t>(jj) * S;
-      float4 *sdir = b.slot_dir + static_cast<int64_t>(jj) * S;
-      for (int k = 0; k < S; ++k) contrib[k] = make_float4(0, 0, 0, 0);
-      float3 L = f3(Pick(b.rad, cur)[jj]);
-      const float3 tp = f3(Pick(b.tp, cur)[jj]);
-
-      if (h.y >= 0) {
-        float3 p, nrm;
-        float hit_dist;
-        int mat_id, light_id, pid;
-        Surface<kMode>(s, h.y, o, d, __int_as_float(h.x), &p, &nrm, &hit_dist, &mat_id, &light_id, &pid);
-        const Mat m = LoadMat(s.materials, mat_id);
-        const float3 shift = p + kEps * nrm;
-        Rng rng = MakeRng(w, path, static_cast<uint32_t>(bounce));
-        const bool direct = bounce >= sp.min_depth;
-        const bool mis = direct && sp.nee == MUON_NEE_MIS;
-
-        if (direct) {
-          // Emission: only at the first vertex when lights are sampled, and
-          // only from the front face (muon/integration.cc:257-264).
-          if ((sp.nee == MUON_NEE_OFF || bounce == 0) && !(dot3(nrm, -d) < 0.0f)) L = L + tp * m.ke;
-          if (sp.nee != MUON_NEE_OFF) {
-            int slot = 0;
-            // Area lights: ShadeDirectNEE (muon/integration.cc:371-462).
-#pragma unroll 1
-            for (int li = 0; li < s.num_lights; ++li) {
-              const DevLight &l = s.lights[li];
-              const float3 corner = f3(l.corner), e0 = f3(l.edge0), e1 = f3(l.edge1), rev = f3(l.rev_normal);
-              const float3 lcol = f3(l.color) * (l.color.w / static_cast<float>(sp.light_samples));
-              const float inv_strata = 1.0f / static_cast<float>(sp.strata);
-#pragma unroll 1
-              for (int q = 0; q < sp.per_light; ++q, ++slot) {
-                const int si = (q / sp.per_section) / sp.strata, sj = (q / sp.per_section) % sp.strata;
-                float u = rng.Next(), v = rng.Next();
-                float fu = (static_cast<float>(si) + u) * inv_strata;
-                float fv = (static_cast<float>(sj) + v) * inv_strata;
-                float3 ptl = corner + fu * e0 + fv * e1 - kEps * rev - shift;
-                float dist = sqrtf(dot3(ptl, ptl));
-                float3 ldir = ptl * (1.0f / dist);
-                float ci = fmaxf(dot3(nrm, ldir), 0.0f);
-                float cl = fmaxf(dot3(rev, ldir), 0.0f);
-                if (ci == 0.0f || cl == 0.0f) continue;
-                float3 c = BrdfEval(m, ldir, d, nrm) * (ci * cl / (dist * dist));
-                if (mis) c = c * PowerHeuristic(NeePdf(s, shift, ldir), IsPdf(sp.is_mode, m, ldir, d, nrm));
-                c = tp * lcol * c;
-                if (!nonzero3(c)) continue;
-                contrib[slot] = make_float4(c.x, c.y, c.z, 0.0f);
-                sdir[slot] = make_float4(ldir.x, ldir.y, ldir.z, dist);
-                ++nshadow;
-                if (slot < kMaskSlots) mask |= 1ull << slot;
-              }
-            }
-            // Point and directional lights (muon/integration.cc:350-369,
-            // muon/lighting.cc:38-64).
-#pragma unroll 1
-            for (int li = 0; li < s.num_other_lights; ++li, ++slot) {
-              const DevLight &l = s.other_lights[li];
-              float3 lcol = f3(l.color);
-              float3 ldir;
-              float dist;
-              if (__float_as_int(l.corner.w) == MUON_LIGHT_POINT) {
-                float3 ptl = f3(l.corner) - p;
-                ldir = normalize3(ptl);
-                dist = length3(ptl);
-                float att = l.edge0.x + l.edge0.y * dist + l.edge0.z * dist * dist;
-                lcol = lcol / att;
-                lcol = lcol / (dist * dist);
-              } else {
-                ldir = f3(l.corner);
-                dist = INFINITY;
-              }
-              float ci = fmaxf(dot3(nrm, ldir), 0.0f);
-              float3 c = tp * lcol * BrdfEval(m, ldir, d, nrm) * ci;
-              if (!nonzero3(c)) continue;
-              contrib[slot] = make_float4(c.x, c.y, c.z, 0.0f);
-              sdir[slot] = make_float4(ldir.x, ldir.y, ldir.z, dist);
-              ++nshadow;
-              if (slot < kMaskSlots) mask |= 1ull << slot;
-            }
-          }
-        }
-        // Two BRDF samples share one code path: first the MIS light-hit ray
-        // (ShadeDirectImportanceSampling, muon/integration.cc:468-501), then
-        // the continuation (ShadeIndirect, muon/integration.cc:294-328).
-#pragma unroll 1
-        for (int pass = mis ? 0 : 1; pass < 2; ++pass) {
-          float3 dir, ntp;
-          float pdf;
-          if (!SampleReflection(sp.is_mode, m, nrm, d, tp, rng, &dir, &pdf, &ntp)) continue;
-          if (pass == 0) {
-            ++counted;
-            // The sampled ray's closest hit is a light triangle exactly when
-            // some light triangle is hit at t_L and nothing is hit before
-            // t_L: an any-hit query up to t_L, none if no light is met. Same
-            // triangle test and ray preparation as the traversal, so t_L is
-            // bit-identical to what the query compares against.
-            float best = INFINITY;
-            int best_light = -1;
-            RayPre rp = Prepare<kMode>(shift, dir);
-            const PrimRecord *lts = kMode == MUON_ISECT_EXACT ? s.light_tris_obj : s.light_tris;
-#pragma unroll 1
-            for (int lt = 0; lt < 2 * s.num_lights; ++lt) {
-              if (!s.light_tri_ok[lt]) continue;
-              PrimRecord lp = LoadPrim(lts, lt);
-              float t_obj;
-              float t = PrimTest<kMode>(s, rp, lp, __float_as_uint(lp.p3.w), &t_obj);
-              if (t > 0.0f && t < best) best = t, best_light = lt >> 1;
-            }
-            if (best_light < 0) continue;
-            float3 c = ntp * f3(s.lights[best_light].color) * PowerHeuristic(pdf, NeePdf(s, shift, dir));
-            if (!nonzero3(c)) continue;
-            const int slot = sp.mis_slot;
-            contrib[slot] = make_float4(c.x, c.y, c.z, 0.0f);
-            sdir[slot] = make_float4(dir.x, dir.y, dir.z, best);
-            ++nshadow;
-            if (slot < kMaskSlots) mask |= 1ull << slot;
-          } else {
-            bool survive = true;
-            if (sp.rr) {
-              float q = fminf(max3c(ntp), 1.0f);
-              if (q < rng.Next()) survive = false;
-              else ntp = ntp / q;
-            }
-            const int next_depth = bounce + 1;
-            const bool depth_ok = sp.max_trace_depth < 0 || next_depth <= sp.max_trace_depth;
-            if (survive && depth_ok && next_depth < sp.max_bounces) {
-              want_cont = 1;
-              ++counted;
-              cont_o = shift;
-              cont_d = dir;
-              cont_tp = ntp;
-            }
-          }
-        }
-        if (nshadow) b.org[jj] = make_float4(shift.x, shift.y, shift.z, 0.0f);
+      id = o4.w;
+      root = d4.w;
+      if (kBatch) {
+        // This path's scene: its lights, settings and sample numbering.
+        const BatchSeg &sg = segs[SegOf(o4.w)];
+        const BatchScene &bs = bscenes[sg.scene];
+        DevScene sv = s;
+        sv.lights = s.lights + bs.light_off;
+        sv.light_tris = s.light_tris + 2 * bs.light_off;
+        sv.light_tris_obj = s.light_tris_obj + 2 * bs.light_off;
+        sv.light_tri_ok = s.light_tri_ok + 2 * bs.light_off;
+        sv.num_lights = bs.num_lights;
+        sv.other_lights = s.other_lights + bs.other_off;
+        sv.num_other_lights = bs.num_other;
+        WaveInfo wv = w;
+        wv.p0 = sg.p0;
+        wv.s0 = sg.s0;
+        wv.ns = sg.ns;
+        wv.seed = bs.seed;
+        wv.sample_offset = bs.sample_offset;
+        ShadeEntry<kMode>(sv, wv, bs.sp, b, cur, bounce, S, jj, o4, d4, PathOf(o4.w) - sg.path0, counted, so,
+                          nullptr);
+      } else {
+        ShadeEntry<kMode>(s, w, sp, b, cur, bounce, S, jj, o4, d4, PathOf(o4.w), counted, so,
+                          kGuide ? &gdev : nullptr);
       }
-      Pick(b.rad, cur)[jj] = make_float4(L.x, L.y, L.z, 0.0f);
     }
 
     uint32_t off_c, off_s;
-    BlockReserve(want_cont, nshadow, wc.count(bounce + 1), wc.shadow(bounce), &off_c, &off_s);
-    if (active) b.link[jj] = want_cont ? static_cast<int32_t>(off_c) : -1;
-    if (want_cont) {
-      Pick(b.ray_o, nxt)[off_c] = make_float4(cont_o.x, cont_o.y, cont_o.z, __int_as_float(path));
-      Pick(b.ray_d, nxt)[off_c] = make_float4(cont_d.x, cont_d.y, cont_d.z, INFINITY);
-      Pick(b.tp, nxt)[off_c] = make_float4(cont_tp.x, cont_tp.y, cont_tp.z, 0.0f);
+    BlockReserve(so.want_cont, so.nshadow, wc.count(bounce + 1), wc.shadow(bounce), &off_c, &off_s);
+    if (active) b.link[jj] = so.want_cont ? static_cast<int32_t>(off_c) : -1;
+    if (so.want_cont) {
+      Pick(b.ray_o, nxt)[off_c] = make_float4(so.cont_o.x, so.cont_o.y, so.cont_o.z, id);
+      Pick(b.ray_d, nxt)[off_c] = make_float4(so.cont_d.x, so.cont_d.y, so.cont_d.z, root);
+      Pick(b.tp, nxt)[off_c] = make_float4(so.cont_tp.x, so.cont_tp.y, so.cont_tp.z, 0.0f);
     }
-    if (nshadow) {
+    if (so.nshadow) {
       const uint32_t base = static_cast<uint32_t>(jj) * static_cast<uint32_t>(S);
       uint32_t k = off_s;
       if (S <= kMaskSlots) {
-        while (mask) {
-          int slot = __ffsll(static_cast<long long>(mask)) - 1;
-          mask &= mask - 1;
+        while (so.mask) {
+          int slot = __ffsll(static_cast<long long>(so.mask)) - 1;
+          so.mask &= so.mask - 1;
           b.shq[k++] = base + slot;
         }
       } else {
@@ -751,7 +891,9 @@ __global__ void __launch_bounds__(kBlock, MUON_SHADE_MIN_BLOCKS) ShadePathKernel
 // After the occlusion pass of a bounce: each entry's radiance plus its
 // unblocked shadow slots moves to its next-bounce entry, or to the path's
 // final radiance when the path ends here.
-__global__ void __launch_bounds__(kBlock) FoldKernel(PathBuffers b, WaveCounters wc, int bounce, int slots) {
+template <bool kGuide>
+__global__ void __launch_bounds__(kBlock) FoldKernel(PathBuffers b, WaveCounters wc, int bounce, int slots,
+                                                     GuideDev g) {
   const int n = static_cast<int>(*wc.count(bounce));
   const int cur = bounce & 1, nxt = cur ^ 1;
   for (int j = blockIdx.x * kBlock + threadIdx.x; j < n; j += gridDim.x * kBlock) {
@@ -765,8 +907,13 @@ __global__ void __launch_bounds__(kBlock) FoldKernel(PathBuffers b, WaveCounters
       }
     }
     int next = b.link[j];
+    if (kGuide && bounce < g.rec_bounces) {
+      GuideRec &rc = g.rec[static_cast<int64_t>(bounce) * g.rec_cap + j];
+      if (next >= 0) rc.after = r;
+      else rc.tp.w = 0.0f;  // no continuation: nothing to learn from this vertex
+    }
     if (next >= 0) Pick(b.rad, nxt)[next] = r;
-    else b.final_rad[__float_as_int(Pick(b.ray_o, cur)[j].w)] = r;
+    else b.final_rad[PathOf(Pick(b.ray_o, cur)[j].w)] = r;
   }
 }
 
@@ -791,6 +938,139 @@ __global__ void __launch_bounds__(kBlock) FilmKernel(WaveInfo w, PathBuffers b, 
   sum_sq[3 * pixel + 1] += q1;
   sum_sq[3 * pixel + 2] += q2;
   count[pixel] += static_cast<uint32_t>(w.ns);
+}
+
+// ---- learned guiding: features, inference, training records -----------------------
+// Spherical coordinates of a unit vector scaled to [0, 1]^2.
+__device__ __forceinline__ void Spherical01(float3 v, float *a, float *b) {
+  *a = acosf(fminf(fmaxf(v.z, -1.0f), 1.0f)) * kInvPi;
+  *b = atan2f(v.y, v.x) * (0.5f * kInvPi) + 0.5f;
+}
+
+// The 8 guiding features of a shading point.
+__device__ __forceinline__ void GuideFeatures(const GuideDev &g, float3 p, float3 n, float3 d, const Mat &m,
+                                              float *f) {
+  f[0] = fminf(fmaxf((p.x - g.lo[0]) * g.inv_ext[0], 0.0f), 1.0f);
+  f[1] = fminf(fmaxf((p.y - g.lo[1]) * g.inv_ext[1], 0.0f), 1.0f);
+  f[2] = fminf(fmaxf((p.z - g.lo[2]) * g.inv_ext[2], 0.0f), 1.0f);
+  Spherical01(n, &f[3], &f[4]);
+  Spherical01(-d, &f[5], &f[6]);
+  // GGX alpha; for Phong the Beckmann-equivalent sqrt(2 / (s + 2)); Lambertian 1
+  float r = 1.0f;
+  if (m.brdf == MUON_BRDF_GGX) r = m.roughness;
+  else if (m.brdf == MUON_BRDF_PHONG) r = sqrtf(2.0f / (m.shininess + 2.0f));
+  f[7] = fminf(fmaxf(r, 0.0f), 1.0f);
+}
+
+// For every hit of the bounce's queue: its features and the network's mixture
+// (one warp per 32 queue entries, network in shared memory).
+template <int kMode>
+__global__ void __launch_bounds__(128) GuideInferKernel(DevScene s, PathBuffers b, WaveCounters wc, int bounce,
+                                                        GuideDev g) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  guide::LoadNetwork(static_cast<const __nv_bfloat16 *>(g.wt), g.bias, smem);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  float *sfeat = reinterpret_cast<float *>(smem + guide::kSmemBytes) + warp * (32 * guide::kFeatures + 32 * guide::kOut);
+  float *sout = sfeat + 32 * guide::kFeatures;
+  __syncthreads();
+  const int n = static_cast<int>(*wc.count(bounce));
+  const int cur = bounce & 1;
+  for (int base = (blockIdx.x * 4 + warp) * 32; base < n; base += gridDim.x * 4 * 32) {
+    const int j = base + lane;
+    float f[guide::kFeatures] = {0, 0, 0, 0, 0, 0, 0, 0};
+    bool hit = false;
+    if (j < n) {
+      const int2 h = b.hits[j];
+      if (h.y >= 0) {
+        hit = true;
+        const float4 o4 = Pick(b.ray_o, cur)[j], d4 = Pick(b.ray_d, cur)[j];
+        float3 p, nrm;
+        float dist;
+        int mat, light, pid;
+        const float3 d = f3(d4.x, d4.y, d4.z);
+        Surface<kMode>(s, h.y, f3(o4.x, o4.y, o4.z), d, __int_as_float(h.x), &p, &nrm, &dist, &mat, &light, &pid);
+        GuideFeatures(g, p, nrm, d, LoadMat(s.materials, mat), f);
+        g.feat[2 * static_cast<int64_t>(j)] = make_float4(f[0], f[1], f[2], f[3]);
+        g.feat[2 * static_cast<int64_t>(j) + 1] = make_float4(f[4], f[5], f[6], f[7]);
+      }
+    }
+#pragma unroll
+    for (int d = 0; d < guide::kFeatures; ++d) sfeat[lane * guide::kFeatures + d] = f[d];
+    __syncwarp();
+    guide::ForwardWarp(smem, [&](int r, int d) { return sfeat[r * guide::kFeatures + d]; }, sout);
+    __syncwarp();
+    if (hit) guide::MakeMixture(sout + lane * guide::kOut, reinterpret_cast<float *>(g.mix + 10 * static_cast<int64_t>(j)));
+    __syncwarp();
+  }
+}
+
+// After a guided wave: every recorded vertex becomes a training sample whose
+// weight is the luminance of (final radiance - radiance after the vertex) /
+// throughput before it, i.e. f cos L_i / density of the sampled direction.
+__global__ void __launch_bounds__(kBlock) GuideCollectKernel(PathBuffers b, WaveCounters wc, int bounces, GuideDev g) {
+  for (int k = 0; k < bounces; ++k) {
+    const int n = static_cast<int>(*wc.count(k));
+    for (int base = blockIdx.x * kBlock; base < n; base += gridDim.x * kBlock) {
+      const int j = base + threadIdx.x;
+      bool keep = false;
+      GuideSample smp;
+      if (j < n) {
+        const GuideRec rc = g.rec[static_cast<int64_t>(k) * g.rec_cap + j];
+        if (rc.tp.w == 1.0f) {
+          const float4 L = b.final_rad[PathOf(rc.dir.w)];
+          const float dl[3] = {L.x - rc.after.x, L.y - rc.after.y, L.z - rc.after.z};
+          const float tp[3] = {rc.tp.x, rc.tp.y, rc.tp.z};
+          const float lum[3] = {0.2126f, 0.7152f, 0.0722f};
+          float wgt = 0.0f;
+          for (int c = 0; c < 3; ++c)
+            if (tp[c] > 0.0f) wgt += lum[c] * fmaxf(dl[c], 0.0f) / tp[c];
+          if (wgt > 0.0f && isfinite(wgt)) {
+            keep = true;
+            smp.f0 = rc.f0;
+            smp.f1 = rc.f1;
+            smp.dir_w = make_float4(rc.dir.x, rc.dir.y, rc.dir.z, wgt);
+          }
+        }
+      }
+      const unsigned mask = __ballot_sync(0xffffffffu, keep);
+      if (mask) {
+        const int lane = threadIdx.x & 31, leader = __ffs(mask) - 1;
+        unsigned long long base_idx = 0;
+        if (lane == leader) base_idx = atomicAdd(g.pool_count, static_cast<unsigned long long>(__popc(mask)));
+        base_idx = __shfl_sync(0xffffffffu, base_idx, leader);
+        if (keep) {
+          const unsigned long long idx = base_idx + __popc(mask & ((1u << lane) - 1u));
+          g.pool[idx % g.pool_cap] = smp;
+        }
+      }
+    }
+  }
+}
+
+// Batched film: one thread per pixel of the wave's segments.
+__global__ void __launch_bounds__(kBlock) FilmBatchKernel(const BatchScene *scenes, const BatchSeg *segs, int nseg,
+                                                          int pixels, PathBuffers b) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= pixels) return;
+  const BatchSeg sg = segs[FindSeg<&BatchSeg::pix0>(segs, nseg, i)];
+  const BatchScene &sc = scenes[sg.scene];
+  const int local = i - sg.pix0;
+  const int pixel = sg.p0 + local;
+  double s0 = 0, s1 = 0, s2 = 0, q0 = 0, q1 = 0, q2 = 0;
+  const float4 *fr = b.final_rad + sg.path0 + static_cast<int64_t>(local) * sg.ns;
+  for (int k = 0; k < sg.ns; ++k) {
+    float4 r = fr[k];
+    s0 += r.x, s1 += r.y, s2 += r.z;
+    q0 += static_cast<double>(r.x) * r.x, q1 += static_cast<double>(r.y) * r.y, q2 += static_cast<double>(r.z) * r.z;
+  }
+  double *sum = sc.sum, *sum_sq = sc.sum_sq;
+  sum[3 * pixel + 0] += s0;
+  sum[3 * pixel + 1] += s1;
+  sum[3 * pixel + 2] += s2;
+  sum_sq[3 * pixel + 0] += q0;
+  sum_sq[3 * pixel + 1] += q1;
+  sum_sq[3 * pixel + 2] += q2;
+  sc.count[pixel] += static_cast<uint32_t>(sg.ns);
 }
 
 // ---- ray-level queries -----------------------------------------------------------
@@ -846,8 +1126,11 @@ inline unsigned CountedBlocks(int64_t bound) {
   return static_cast<unsigned>(std::max<int64_t>(1, std::min<int64_t>(Blocks(bound), g_persistent_blocks)));
 }
 
+int g_traversal_override = 0;
+
 inline unsigned TraversalBlocks(int64_t bound) {
-  return static_cast<unsigned>(std::max<int64_t>(1, std::min<int64_t>(Blocks(bound), g_traversal_blocks)));
+  const int grid = g_traversal_override > 0 ? g_traversal_override : g_traversal_blocks;
+  return static_cast<unsigned>(std::max<int64_t>(1, std::min<int64_t>(Blocks(bound), grid)));
 }
 
 // Calls f(std::integral_constant<int, mode>) for a runtime intersection mode.
@@ -861,6 +1144,8 @@ void WithMode(int mode, F &&f) {
 }  // namespace
 
 void SetPersistentGrid(int blocks) { g_persistent_blocks = std::max(1, blocks); }
+
+void SetTraversalBlocksOverride(int blocks) { g_traversal_override = std::max(0, blocks); }
 
 void SetTraversalGrid(int sms) {
   // Enough resident blocks to fill every SM once; the persistent traversal
@@ -910,7 +1195,8 @@ void LaunchShadePath(const DevScene &s, const WaveInfo &w, const ShadeParams &sp
                      WaveCounters wc, int bounce, int bound, cudaStream_t st) {
   if (bound <= 0) return;
   WithMode(sp.isect, [&](auto m) {
-    ShadePathKernel<decltype(m)::value><<<CountedBlocks(bound), kBlock, 0, st>>>(s, w, sp, b, wc, bounce);
+    ShadePathKernel<decltype(m)::value, false, false>
+        <<<CountedBlocks(bound), kBlock, 0, st>>>(s, w, sp, b, wc, bounce, nullptr, nullptr, sp.slots, GuideDev{});
   });
 }
 
@@ -927,12 +1213,66 @@ void LaunchOcclude(const DevScene &s, const PathBuffers &b, WaveCounters wc, int
 
 void LaunchFold(const PathBuffers &b, WaveCounters wc, int bounce, int slots, int bound, cudaStream_t st) {
   if (bound <= 0) return;
-  FoldKernel<<<CountedBlocks(bound), kBlock, 0, st>>>(b, wc, bounce, slots);
+  FoldKernel<false><<<CountedBlocks(bound), kBlock, 0, st>>>(b, wc, bounce, slots, GuideDev{});
 }
 
 void LaunchFilm(const WaveInfo &w, const PathBuffers &b, double *sum, double *sum_sq, uint32_t *count,
                 cudaStream_t st) {
   if (w.npix > 0) FilmKernel<<<Blocks(w.npix), kBlock, 0, st>>>(w, b, sum, sum_sq, count);
+}
+
+void LaunchCameraBatch(const BatchScene *scenes, const BatchSeg *segs, int nseg, int paths, const PathBuffers &b,
+                       WaveCounters wc, cudaStream_t st) {
+  CameraBatchKernel<<<Blocks(std::max(paths, 1)), kBlock, 0, st>>>(scenes, segs, nseg, paths, b, wc);
+}
+
+void LaunchShadePathBatch(const DevScene &s, const BatchScene *scenes, const BatchSeg *segs, int slot_stride,
+                          int isect, const PathBuffers &b, WaveCounters wc, int bounce, int bound, cudaStream_t st) {
+  if (bound <= 0) return;
+  WaveInfo w{};
+  ShadeParams sp{};
+  WithMode(isect, [&](auto m) {
+    ShadePathKernel<decltype(m)::value, true, false>
+        <<<CountedBlocks(bound), kBlock, 0, st>>>(s, w, sp, b, wc, bounce, scenes, segs, slot_stride, GuideDev{});
+  });
+}
+
+void LaunchFilmBatch(const BatchScene *scenes, const BatchSeg *segs, int nseg, int pixels, const PathBuffers &b,
+                     cudaStream_t st) {
+  if (pixels > 0) FilmBatchKernel<<<Blocks(pixels), kBlock, 0, st>>>(scenes, segs, nseg, pixels, b);
+}
+
+void LaunchGuideInfer(const DevScene &s, const PathBuffers &b, WaveCounters wc, int bounce, int bound, int isect,
+                      const GuideDev &g, cudaStream_t st) {
+  if (bound <= 0) return;
+  const int smem = guide::kSmemBytes + 4 * (32 * guide::kFeatures + 32 * guide::kOut) * 4;
+  const unsigned grid = static_cast<unsigned>(std::max<int64_t>(1, std::min<int64_t>((bound + 127) / 128, 2 * g_traversal_blocks)));
+  WithMode(isect, [&](auto m) {
+    constexpr int M = decltype(m)::value;
+    cudaFuncSetAttribute(GuideInferKernel<M>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    GuideInferKernel<M><<<grid, 128, smem, st>>>(s, b, wc, bounce, g);
+  });
+}
+
+void LaunchShadePathGuided(const DevScene &s, const WaveInfo &w, const ShadeParams &sp, const PathBuffers &b,
+                           WaveCounters wc, int bounce, int bound, const GuideDev &g, cudaStream_t st) {
+  if (bound <= 0) return;
+  WithMode(sp.isect, [&](auto m) {
+    ShadePathKernel<decltype(m)::value, false, true>
+        <<<CountedBlocks(bound), kBlock, 0, st>>>(s, w, sp, b, wc, bounce, nullptr, nullptr, sp.slots, g);
+  });
+}
+
+void LaunchFoldGuided(const PathBuffers &b, WaveCounters wc, int bounce, int slots, int bound, const GuideDev &g,
+                      cudaStream_t st) {
+  if (bound <= 0) return;
+  FoldKernel<true><<<CountedBlocks(bound), kBlock, 0, st>>>(b, wc, bounce, slots, g);
+}
+
+void LaunchGuideCollect(const PathBuffers &b, WaveCounters wc, int bounces, int bound, const GuideDev &g,
+                        cudaStream_t st) {
+  if (bound <= 0 || bounces <= 0) return;
+  GuideCollectKernel<<<CountedBlocks(bound), kBlock, 0, st>>>(b, wc, bounces, g);
 }
 
 void LaunchIntersectRays(const DevScene &s, const float *rays, int64_t n, int isect, float *out_hit, cudaStream_t st) {

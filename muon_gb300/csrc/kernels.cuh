@@ -39,6 +39,14 @@ struct WaveInfo {
   uint64_t seed;
 };
 
+// A path record's id word (ray_o.w) holds the wave-local path index in its low
+// kPathBits bits and, in a batched wave, the segment index above them; a
+// wave holds at most 2^kPathBits paths and kMaxSegments segments.
+constexpr int kPathBits = 24;
+constexpr uint32_t kPathMask = (1u << kPathBits) - 1u;
+constexpr int kMaxWavePaths = 1 << kPathBits;
+constexpr int kMaxSegments = 256;
+
 // Queue counters of one wavefront, all on the device so that a wavefront is a
 // fixed launch sequence: count(k) = paths queued at bounce k (count(0) = n),
 // shadow(k) = shadow rays emitted at bounce k.
@@ -90,6 +98,29 @@ struct ShadeParams {
   int32_t max_bounces;
 };
 
+// Batched rendering: several scenes share one wavefront. Their device arrays
+// are concatenated into one DevScene (each scene's BVH under its own root
+// node, its lights a contiguous range); a wave is a list of segments, each a
+// block of one scene's pixels and samples.
+struct BatchScene {
+  DevCamera cam;
+  ShadeParams sp;      // slots/mis_slot of this scene; the wave's slot stride may be larger
+  int32_t light_off, num_lights;   // quad lights (and their triangles at 2x)
+  int32_t other_off, num_other;    // point / directional lights
+  int32_t width;
+  uint32_t sample_offset;
+  uint64_t seed;
+  double *sum, *sum_sq;
+  uint32_t *count;
+};
+struct BatchSeg {
+  int32_t scene;
+  int32_t path0;  // first wave-local path of the segment
+  int32_t pix0;   // first wave-local pixel of the segment
+  int32_t p0, npix, s0, ns;  // film pixels [p0, p0 + npix), samples [s0, s0 + ns)
+  int32_t root;   // BVH root node of the scene
+};
+
 // Upper bound on the blocks of the device-counted launches (they loop over
 // their queue with a grid stride), and the block count of the persistent
 // traversal kernels; set from the SM count at scene creation.
@@ -112,6 +143,18 @@ void LaunchOcclude(const DevScene &s, const PathBuffers &b, WaveCounters wc, int
 void LaunchFold(const PathBuffers &b, WaveCounters wc, int bounce, int slots, int bound, cudaStream_t st);
 void LaunchFilm(const WaveInfo &w, const PathBuffers &b, double *sum, double *sum_sq, uint32_t *count,
                 cudaStream_t st);
+// Batched counterparts: `segs` (nseg entries) and `scenes` are device tables;
+// `paths` and `pixels` are the wave's totals, `slot_stride` the wave's shadow
+// slots per entry (the largest of its scenes').
+void LaunchCameraBatch(const BatchScene *scenes, const BatchSeg *segs, int nseg, int paths, const PathBuffers &b,
+                       WaveCounters wc, cudaStream_t st);
+void LaunchShadePathBatch(const DevScene &s, const BatchScene *scenes, const BatchSeg *segs, int slot_stride,
+                          int isect, const PathBuffers &b, WaveCounters wc, int bounce, int bound, cudaStream_t st);
+void LaunchFilmBatch(const BatchScene *scenes, const BatchSeg *segs, int nseg, int pixels, const PathBuffers &b,
+                     cudaStream_t st);
+// Grid of the persistent traversal kernels for the launches that follow
+// (0 restores the default of filling every SM once).
+void SetTraversalBlocksOverride(int blocks);
 // Ray-level queries for the batched Intersect/HasIntersection seams.
 void LaunchIntersectRays(const DevScene &s, const float *rays, int64_t n, int isect, float *out_hit,
                          cudaStream_t st);

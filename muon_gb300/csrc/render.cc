@@ -15,6 +15,7 @@
 #include <string>
 #include <vector>
 
+#include "host_cuda.h"
 #include "host_scene.h"
 #include "kernels.cuh"
 #include "scene_access.h"
@@ -27,50 +28,6 @@ namespace {
 constexpr int kDefaultWavePaths = 1 << 24;
 constexpr int kMaxBounces = 256;  // hard cap for unbounded depth without Russian roulette
 constexpr int kMaxEventPairs = 16384;
-
-struct CudaError {
-  cudaError_t code;
-  const char *where;
-};
-
-#define CUDA_TRY(expr)                                                              \
-  do {                                                                              \
-    cudaError_t _e = (expr);                                                        \
-    if (_e != cudaSuccess) throw CudaError{_e, #expr};                              \
-  } while (0)
-
-struct DeviceBuffer {
-  void *ptr = nullptr;
-  size_t bytes = 0;
-  ~DeviceBuffer() {
-    if (ptr) cudaFree(ptr);
-  }
-  void Ensure(size_t want) {
-    if (want <= bytes && ptr) return;
-    if (ptr) cudaFree(ptr);
-    ptr = nullptr;
-    bytes = 0;
-    if (want == 0) return;
-    cudaError_t e = cudaMalloc(&ptr, want);
-    if (e != cudaSuccess) throw CudaError{e, "cudaMalloc"};
-    bytes = want;
-  }
-  template <typename T>
-  T *as() const {
-    return static_cast<T *>(ptr);
-  }
-};
-
-template <typename T>
-void Upload(DeviceBuffer &buf, const std::vector<T> &v, cudaStream_t st) {
-  buf.Ensure(std::max<size_t>(v.size() * sizeof(T), 16));
-  if (!v.empty()) CUDA_TRY(cudaMemcpyAsync(buf.ptr, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, st));
-}
-
-struct EventPair {
-  cudaEvent_t a = nullptr, b = nullptr;
-  int kind = 0;  // 0 extend, 1 occlude, 2 other
-};
 
 }  // namespace
 
@@ -197,7 +154,7 @@ void SetLastError(const std::string &msg) { g_last_error = msg; }
 const char *LastError() { return g_last_error.c_str(); }
 }  // namespace muon_gpu
 
-namespace {
+namespace muon_gpu {
 
 int Fail(int code, const std::string &msg) {
   SetLastError(msg);
@@ -230,38 +187,10 @@ void ComputeCamera(const MuonCameraDesc &c, DevCamera *out) {
   out->height = c.height;
 }
 
-int ValidateParams(const MuonRenderParams &p) {
-  if (p.integrator < MUON_INTEGRATOR_NORMALS || p.integrator > MUON_INTEGRATOR_PATHTRACER)
-    return Fail(MUON_ERR_INVALID_ARG, "unknown integrator");
-  if (p.pixel_samples < 1) return Fail(MUON_ERR_INVALID_ARG, "pixel_samples must be >= 1");
-  if (p.next_event_estimation < MUON_NEE_OFF || p.next_event_estimation > MUON_NEE_MIS)
-    return Fail(MUON_ERR_INVALID_ARG, "unknown next_event_estimation mode");
-  if (p.importance_sampling < MUON_IS_HEMISPHERE || p.importance_sampling > MUON_IS_BRDF)
-    return Fail(MUON_ERR_INVALID_ARG, "unknown importance_sampling mode");
-  if (p.intersect_mode < MUON_ISECT_FAST || p.intersect_mode > MUON_ISECT_EXACT)
-    return Fail(MUON_ERR_INVALID_ARG, "unknown intersect_mode");
-  if (p.integrator == MUON_INTEGRATOR_PATHTRACER && p.next_event_estimation != MUON_NEE_OFF && p.light_samples < 1)
-    return Fail(MUON_ERR_INVALID_ARG, "light_samples must be >= 1");
-  if (p.max_depth < -1) return Fail(MUON_ERR_INVALID_ARG, "max_depth must be >= -1");
-  if (p.wave_paths < 0) return Fail(MUON_ERR_INVALID_ARG, "wave_paths must be >= 0");
-  return MUON_OK;
-}
-
-// Renders into a device film. Throws CudaError.
-//
-// Bounded depth: every wavefront is a fixed launch sequence (camera; per
-// bounce extend, shade, occlude, fold; film) whose kernels read their queue
-// lengths from device counters, so the whole frame is captured once into a
-// CUDA graph and replayed; the host synchronises once per frame. Unbounded
-// depth (max_depth -1): the host reads the queue length after every bounce and
-// stops when no path continues.
-void RenderDevice(MuonScene *sc, const MuonRenderParams &p, double *d_sum, double *d_sq, uint32_t *d_cnt) {
-  cudaStream_t st = sc->stream;
+// ShadeParams of a render (PathTracer settings and the shadow-slot layout of
+// a path vertex); returns the number of shadow slots.
+int SetupShade(const MuonRenderParams &p, int num_quad_lights, int num_other_lights, ShadeParams *out) {
   const bool pt = p.integrator == MUON_INTEGRATOR_PATHTRACER;
-  // Raytracer / AnalyticDirect: one kernel follows each path to its end.
-  const bool whitted = p.integrator == MUON_INTEGRATOR_RAYTRACER || p.integrator == MUON_INTEGRATOR_ANALYTIC_DIRECT;
-  const bool stats_on = (p.flags & MUON_RENDER_STATS) != 0;
-  const bool timing = (p.flags & MUON_RENDER_TIMING) != 0;
   ShadeParams sp{};
   sp.integrator = p.integrator;
   sp.nee = p.next_event_estimation;
@@ -280,10 +209,87 @@ void RenderDevice(MuonScene *sc, const MuonRenderParams &p, double *d_sum, doubl
   int slots = 0;
   sp.mis_slot = -1;
   if (pt && p.next_event_estimation != MUON_NEE_OFF) {
-    slots = sc->dev.num_lights * sp.per_light + sc->dev.num_other_lights;
+    slots = num_quad_lights * sp.per_light + num_other_lights;
     if (p.next_event_estimation == MUON_NEE_MIS) sp.mis_slot = slots++;
   }
   sp.slots = slots;
+  *out = sp;
+  return slots;
+}
+
+// The two triangles of each quad light (muon/parser.cc:735-747), in the same
+// record format as the BVH's, for the MIS light-hit test.
+void BuildLightTris(const std::vector<DevLight> &lights, std::vector<PrimRecord> *lt_out,
+                    std::vector<PrimRecord> *lt_obj_out, std::vector<int32_t> *lt_ok_out) {
+  std::vector<PrimRecord> &lt = *lt_out, &lt_obj = *lt_obj_out;
+  std::vector<int32_t> &lt_ok = *lt_ok_out;
+  lt.assign(2 * lights.size(), PrimRecord{});
+  lt_obj.assign(2 * lights.size(), PrimRecord{});
+  lt_ok.assign(2 * lights.size(), 0);
+  for (size_t i = 0; i < lights.size(); ++i) {
+    const DevLight &l = lights[i];
+    mm::v3 c = mm::make3(l.corner.x, l.corner.y, l.corner.z);
+    mm::v3 e0 = mm::make3(l.edge0.x, l.edge0.y, l.edge0.z), e1 = mm::make3(l.edge1.x, l.edge1.y, l.edge1.z);
+    mm::v3 va = c, vb = c + e0, vc = c + e1, vd = c + e0 + e1;
+    const mm::v3 tri[2][3] = {{va, vc, vb}, {vb, vc, vd}};
+    for (int t = 0; t < 2; ++t) {
+      mm::v3 n = mm::cross(tri[t][1] - tri[t][0], tri[t][2] - tri[t][0]);
+      PrimRecord &r = lt[2 * i + t];
+      r.p0 = F4{tri[t][0].x, tri[t][0].y, tri[t][0].z, mm::dot(tri[t][0], n)};
+      r.p1 = F4{tri[t][1].x, tri[t][1].y, tri[t][1].z, 1e-4f};
+      r.p2 = F4{tri[t][2].x, tri[t][2].y, tri[t][2].z, 0.0f};
+      r.p3 = F4{n.x, n.y, n.z, 0.0f};
+      lt_ok[2 * i + t] = mm::length(n) >= 1e-4f ? 1 : 0;
+      PrimRecord &ro = lt_obj[2 * i + t];
+      int32_t identity = -1;
+      float xf_bits;
+      std::memcpy(&xf_bits, &identity, 4);
+      ro.p0 = F4{tri[t][0].x, tri[t][0].y, tri[t][0].z, 0.0f};
+      ro.p1 = F4{tri[t][1].x, tri[t][1].y, tri[t][1].z, xf_bits};
+      ro.p2 = F4{tri[t][2].x, tri[t][2].y, tri[t][2].z, mm::dot(n, n)};
+      ro.p3 = F4{n.x, n.y, n.z, 0.0f};
+    }
+  }
+}
+
+int ValidateParams(const MuonRenderParams &p) {
+  if (p.integrator < MUON_INTEGRATOR_NORMALS || p.integrator > MUON_INTEGRATOR_PATHTRACER)
+    return Fail(MUON_ERR_INVALID_ARG, "unknown integrator");
+  if (p.pixel_samples < 1) return Fail(MUON_ERR_INVALID_ARG, "pixel_samples must be >= 1");
+  if (p.next_event_estimation < MUON_NEE_OFF || p.next_event_estimation > MUON_NEE_MIS)
+    return Fail(MUON_ERR_INVALID_ARG, "unknown next_event_estimation mode");
+  if (p.importance_sampling < MUON_IS_HEMISPHERE || p.importance_sampling > MUON_IS_BRDF)
+    return Fail(MUON_ERR_INVALID_ARG, "unknown importance_sampling mode");
+  if (p.intersect_mode < MUON_ISECT_FAST || p.intersect_mode > MUON_ISECT_EXACT)
+    return Fail(MUON_ERR_INVALID_ARG, "unknown intersect_mode");
+  if (p.integrator == MUON_INTEGRATOR_PATHTRACER && p.next_event_estimation != MUON_NEE_OFF && p.light_samples < 1)
+    return Fail(MUON_ERR_INVALID_ARG, "light_samples must be >= 1");
+  if (p.max_depth < -1) return Fail(MUON_ERR_INVALID_ARG, "max_depth must be >= -1");
+  if (p.wave_paths < 0) return Fail(MUON_ERR_INVALID_ARG, "wave_paths must be >= 0");
+  return MUON_OK;
+}
+
+}  // namespace muon_gpu
+
+namespace {
+
+// Renders into a device film. Throws CudaError.
+//
+// Bounded depth: every wavefront is a fixed launch sequence (camera; per
+// bounce extend, shade, occlude, fold; film) whose kernels read their queue
+// lengths from device counters, so the whole frame is captured once into a
+// CUDA graph and replayed; the host synchronises once per frame. Unbounded
+// depth (max_depth -1): the host reads the queue length after every bounce and
+// stops when no path continues.
+void RenderDevice(MuonScene *sc, const MuonRenderParams &p, double *d_sum, double *d_sq, uint32_t *d_cnt) {
+  cudaStream_t st = sc->stream;
+  const bool pt = p.integrator == MUON_INTEGRATOR_PATHTRACER;
+  // Raytracer / AnalyticDirect: one kernel follows each path to its end.
+  const bool whitted = p.integrator == MUON_INTEGRATOR_RAYTRACER || p.integrator == MUON_INTEGRATOR_ANALYTIC_DIRECT;
+  const bool stats_on = (p.flags & MUON_RENDER_STATS) != 0;
+  const bool timing = (p.flags & MUON_RENDER_TIMING) != 0;
+  ShadeParams sp;
+  const int slots = SetupShade(p, sc->dev.num_lights, sc->dev.num_other_lights, &sp);
 
   const int W = sc->img.width, H = sc->img.height;
   const int64_t npix_total = static_cast<int64_t>(W) * H;
@@ -292,6 +298,7 @@ void RenderDevice(MuonScene *sc, const MuonRenderParams &p, double *d_sum, doubl
   // Keep per-wave path state within ~8 GiB.
   const int64_t per_path = 200 + 36 * static_cast<int64_t>(std::max(slots, 1));
   budget = std::max<int64_t>(1, std::min<int64_t>(budget, (int64_t(8) << 30) / per_path));
+  budget = std::min<int64_t>(budget, kMaxWavePaths);
   const int ns = static_cast<int>(std::min<int64_t>(spp, budget));
   const int64_t pix_per_wave = std::max<int64_t>(1, budget / ns);
   std::vector<WaveInfo> waves;
@@ -506,34 +513,9 @@ int muon_gpu_scene_create(const MuonSceneDesc *desc, MuonScene **out) {
     Upload(sc->lights, im.lights, st);
     Upload(sc->other_lights, im.other_lights, st);
     Upload(sc->all_lights, im.all_lights, st);
-    // The two triangles of each quad light (muon/parser.cc:735-747), in the
-    // same record format as the BVH's, for the MIS light-hit test.
-    std::vector<PrimRecord> lt(2 * im.lights.size()), lt_obj(2 * im.lights.size());
-    std::vector<int32_t> lt_ok(2 * im.lights.size(), 0);
-    for (size_t i = 0; i < im.lights.size(); ++i) {
-      const DevLight &l = im.lights[i];
-      mm::v3 c = mm::make3(l.corner.x, l.corner.y, l.corner.z);
-      mm::v3 e0 = mm::make3(l.edge0.x, l.edge0.y, l.edge0.z), e1 = mm::make3(l.edge1.x, l.edge1.y, l.edge1.z);
-      mm::v3 va = c, vb = c + e0, vc = c + e1, vd = c + e0 + e1;
-      const mm::v3 tri[2][3] = {{va, vc, vb}, {vb, vc, vd}};
-      for (int t = 0; t < 2; ++t) {
-        mm::v3 n = mm::cross(tri[t][1] - tri[t][0], tri[t][2] - tri[t][0]);
-        PrimRecord &r = lt[2 * i + t];
-        r.p0 = F4{tri[t][0].x, tri[t][0].y, tri[t][0].z, mm::dot(tri[t][0], n)};
-        r.p1 = F4{tri[t][1].x, tri[t][1].y, tri[t][1].z, 1e-4f};
-        r.p2 = F4{tri[t][2].x, tri[t][2].y, tri[t][2].z, 0.0f};
-        r.p3 = F4{n.x, n.y, n.z, 0.0f};
-        lt_ok[2 * i + t] = mm::length(n) >= 1e-4f ? 1 : 0;
-        PrimRecord &ro = lt_obj[2 * i + t];
-        int32_t identity = -1;
-        float xf_bits;
-        std::memcpy(&xf_bits, &identity, 4);
-        ro.p0 = F4{tri[t][0].x, tri[t][0].y, tri[t][0].z, 0.0f};
-        ro.p1 = F4{tri[t][1].x, tri[t][1].y, tri[t][1].z, xf_bits};
-        ro.p2 = F4{tri[t][2].x, tri[t][2].y, tri[t][2].z, mm::dot(n, n)};
-        ro.p3 = F4{n.x, n.y, n.z, 0.0f};
-      }
-    }
+    std::vector<PrimRecord> lt, lt_obj;
+    std::vector<int32_t> lt_ok;
+    BuildLightTris(im.lights, &lt, &lt_obj, &lt_ok);
     Upload(sc->light_tris, lt, st);
     Upload(sc->light_tris_obj, lt_obj, st);
     Upload(sc->light_tri_ok, lt_ok, st);
@@ -700,6 +682,7 @@ bool GetSceneView(const MuonScene *scene, SceneView *out) {
   out->device = scene->device;
   out->width = scene->img.width;
   out->height = scene->img.height;
+  out->img = &scene->img;
   return true;
 }
 

@@ -6,6 +6,7 @@
 
 #include "../../include/muon_gpu.h"
 #include "dev_layout.h"
+#include "scene_build.h"
 
 namespace muon_gpu {
 
@@ -15,6 +16,7 @@ struct SceneView {
   cudaStream_t stream;
   int device;
   int width, height;
+  const SceneImage *img;  // host copy of the scene's device arrays
 };
 
 // Fills `out` from a scene created by muon_gpu_scene_create; false if null.

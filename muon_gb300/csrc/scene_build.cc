@@ -320,9 +320,12 @@ void BuildBvh(const std::vector<Aabb> &boxes, int accel, int strategy, int max_l
   double sah = 0.0;
   float root_area = std::max(Area(bn[root].box), 1e-30f);
   if (bn[root].left < 0) {
+    // The root is a leaf: both child slots refer to it. (An inverted box in
+    // the second slot would pass the slab test, and an empty link ends the
+    // traversal.) Testing the leaf twice cannot change a closest hit.
     BvhNode n{};
     SetChild(n, 0, bn[root].box, ~bn[root].start);
-    SetChild(n, 1, EmptyBox(), kEmptyLink);
+    SetChild(n, 1, bn[root].box, ~bn[root].start);
     nodes->push_back(n);
   } else {
     // Explicit stack of (build node, output slot).

@@ -103,6 +103,15 @@ class Stats(C.Structure):
                 ("occlude_box_tests", C.c_uint64), ("occlude_prim_tests", C.c_uint64)]
 
 
+class BatchSceneStats(C.Structure):
+    _fields_ = [("primary_rays", C.c_uint64), ("done_ms", C.c_double)]
+
+
+class BatchTuning(C.Structure):
+    _fields_ = [("wave_paths", C.c_int32), ("traversal_blocks_per_sm", C.c_int32), ("candidates", C.c_int32),
+                ("pad", C.c_int32), ("best_ms", C.c_double)]
+
+
 # Every entry point declared in include/muon_gpu.h: name -> (restype, argtypes)
 SIGNATURES = {
     "muon_parse_scene_file": (C.c_int, [C.c_char_p, C.POINTER(C.c_void_p)]),
@@ -127,6 +136,15 @@ SIGNATURES = {
     "muon_gpu_stats": (C.c_int, [C.c_void_p, C.POINTER(Stats)]),
     "muon_gpu_scene_stream": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p)]),
     "muon_gpu_last_error": (C.c_char_p, []),
+    "muon_gpu_batch_create": (C.c_int, [C.POINTER(C.c_void_p), C.c_int32, C.POINTER(C.c_void_p)]),
+    "muon_gpu_batch_destroy": (None, [C.c_void_p]),
+    "muon_gpu_batch_render_device": (C.c_int, [C.c_void_p, C.POINTER(RenderParams), C.POINTER(C.c_void_p),
+                                               C.POINTER(C.c_void_p), C.POINTER(C.c_void_p)]),
+    "muon_gpu_batch_render": (C.c_int, [C.c_void_p, C.POINTER(RenderParams), C.POINTER(Film)]),
+    "muon_gpu_batch_autotune": (C.c_int, [C.c_void_p, C.POINTER(RenderParams), C.POINTER(BatchTuning)]),
+    "muon_gpu_batch_stats": (C.c_int, [C.c_void_p, C.POINTER(Stats), C.POINTER(BatchSceneStats)]),
+    "muon_gpu_render_batch": (C.c_int, [C.POINTER(C.c_void_p), C.POINTER(RenderParams), C.c_int32,
+                                        C.POINTER(Film)]),
 }
 
 _lib = None

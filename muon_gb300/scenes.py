@@ -311,6 +311,55 @@ def whitted(width: int = 128, height: int = 128, spp: int = 1, max_depth: int = 
     return "\n".join(L) + "\n"
 
 
+def batch_scene(index: int, seed: int = 1, max_tris: int = 500_000, resolutions=(128, 256, 512, 1024),
+                spp_range=(4, 64), depth_range=(4, 10)) -> str:
+    """Scene `index` of the batched workload: the Cornell box with a displaced
+    icosphere of a log-uniform triangle count in [1000, max_tris] (the nearest
+    icosphere level at or below the count, the rest as small clutter
+    triangles), one material drawn from Lambertian / Phong / GGX, resolution
+    drawn from `resolutions` (square), spp uniform in spp_range, max depth
+    uniform in depth_range, NEE with MIS. Seeded by (seed, index)."""
+    rng = np.random.default_rng([seed, index])
+    target = int(round(np.exp(rng.uniform(np.log(1000), np.log(max_tris)))))
+    level = 0
+    while 20 * 4 ** (level + 1) <= target:
+        level += 1
+    clutter = max(0, target - 20 * 4 ** level)
+    res = int(rng.choice(resolutions))
+    spp = int(rng.integers(spp_range[0], spp_range[1] + 1))
+    depth = int(rng.integers(depth_range[0], depth_range[1] + 1))
+    L = cornell(res, res, spp, depth, int(rng.integers(1, 1 << 30)), "pathtracer", "mis").splitlines()
+    kind = int(rng.integers(0, 3))
+    if kind == 0:
+        L += ["brdf lambertian", "diffuse " + _v(*rng.uniform(0.2, 0.8, 3)), "specular 0 0 0"]
+    elif kind == 1:
+        L += ["brdf phong", "diffuse " + _v(*rng.uniform(0.1, 0.5, 3)), "specular " + _v(*rng.uniform(0.1, 0.5, 3)),
+              "shininess " + _f(10 ** rng.uniform(0.5, 2.5))]
+    else:
+        L += ["brdf ggx", "diffuse " + _v(*rng.uniform(0.0, 0.3, 3)), "specular " + _v(*rng.uniform(0.2, 0.9, 3)),
+              "roughness " + _f(rng.uniform(0.05, 0.5))]
+    V, F = icosphere(level)
+    V = V * (1.0 + 0.1 * value_noise(V, seed * 1000 + index, freq=3.0))[:, None]
+    c = rng.uniform([-0.4, 0.5, -0.4], [0.4, 1.1, 0.4])
+    r = rng.uniform(0.25, 0.45)
+    L += ["push_transform", "translate " + _v(*c), "scale " + _v(r / 1000, r / 1000, r / 1000)]
+    _mesh_fast(L, V * 1000.0, F)
+    L.append("pop_transform")
+    if clutter:
+        L += ["push_transform", "scale 0.001 0.001 0.001"]
+        centres = rng.uniform([-0.95, 0.05, -0.95], [0.95, 1.95, 0.95], size=(clutter, 3))
+        edge = rng.uniform(0.01, 0.05, size=clutter)
+        d1 = rng.normal(size=(clutter, 3))
+        d1 /= np.linalg.norm(d1, axis=1, keepdims=True)
+        d2 = rng.normal(size=(clutter, 3))
+        d2 -= (d2 * d1).sum(1, keepdims=True) * d1
+        d2 /= np.linalg.norm(d2, axis=1, keepdims=True)
+        tri = np.stack([centres, centres + d1 * edge[:, None], centres + (0.5 * d1 + 0.866 * d2) * edge[:, None]], 1)
+        _mesh_fast(L, tri.reshape(-1, 3) * 1000.0, np.arange(3 * clutter, dtype=np.int64).reshape(-1, 3))
+        L.append("pop_transform")
+    return "\n".join(L) + "\n"
+
+
 WORKLOADS = {
     "cornell": cornell,
     "sphere_field": sphere_field,

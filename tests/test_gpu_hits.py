@@ -112,3 +112,28 @@ def test_debug_integrators_are_bitwise_equal(lib, name, integrator):
     print(f"{name}/{integrator}: {int(differ.sum())} of {len(differ)} pixels differ in 8-bit output "
           f"({int((differ & ~same).sum())} of them at exact ties)")
     assert not (differ & same).any()
+
+
+TINY = {
+    "one_sphere": "film_size 16 16\ncamera 0 0 5  0 0 0  0 1 0  45\nsphere 0 0 0 1\n",
+    "one_quad": ("film_size 16 16\ncamera 0 0 5  0 0 0  0 1 0  45\nstart_mesh\nvertex -1 -1 0\nvertex 1 -1 0\n"
+                 "vertex 1 1 0\nvertex -1 1 0\ntri 0 1 2\ntri 0 2 3\nend_mesh\n"),
+}
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", sorted(TINY))
+def test_scene_whose_bvh_root_is_a_leaf(lib, name):
+    """With at most four primitives the whole BVH is one leaf; rays from
+    outside its box must still find it."""
+    from oracle import port
+
+    text = TINY[name]
+    rays = port.camera_rays(text)
+    scene = m.Scene.from_string(text)
+    dist, pid, _, _ = scene.intersect(rays[:, :3], rays[:, 3:], native.ISECT_EXACT)
+    d_ref, id_ref, _, _ = port.intersect(text, rays, precision=32, linear=True)
+    assert (id_ref >= 0).sum() > 0
+    assert np.array_equal(pid >= 0, id_ref >= 0)
+    hit = id_ref >= 0
+    assert np.array_equal(dist[hit], d_ref[hit].astype(np.float32))

@@ -364,6 +364,55 @@ int muon_gpu_render_batch(MuonScene *const *scenes, const MuonRenderParams *para
  * callers that time or order work around it with CUDA events. */
 int muon_gpu_scene_stream(const MuonScene *scene, void **stream);
 
+/* ---- learned path guiding --------------------------------------------
+ * No counterpart in the reference (which has no learned component): a small
+ * MLP predicts, per shading point, a mixture of 8 von Mises-Fisher lobes over
+ * directions; the path tracer samples it with probability mixture_fraction
+ * and its own sampler otherwise, weighting every sample by the combined
+ * density, so the estimate stays unbiased whatever the network predicts. The
+ * network (one-blob encoded position, normal, outgoing direction and
+ * roughness -> 5 layers of 64 -> 40 outputs; BF16 tensor-core inference,
+ * FP32 training with Adam) learns online from the radiance samples of the
+ * guide's own renders. */
+typedef struct MuonGuide MuonGuide;
+
+typedef struct MuonGuideConfig {
+  int32_t batch;            /* training batch (0: 2^18)                            */
+  int32_t wave_paths;       /* paths per wavefront of guided renders (0: 2^22)     */
+  int32_t record_bounces;   /* vertices per path kept as training samples (0: 4)   */
+  int32_t pool_capacity;    /* training samples kept, newest first (0: 2^22)       */
+  float learning_rate;      /* Adam step size (0: 1e-3)                            */
+  float mixture_fraction;   /* probability of sampling the mixture (0: 0.5)        */
+  uint64_t seed;            /* network initialisation and batch selection          */
+} MuonGuideConfig;
+
+/* Number of FP32 network parameters (weights [in][out] then biases, per layer). */
+#define MUON_GUIDE_PARAMS 31528
+
+int muon_gpu_guide_create(MuonScene *scene, const MuonGuideConfig *config, MuonGuide **out);
+void muon_gpu_guide_destroy(MuonGuide *guide);
+/* Path-traced render of the guide's scene (device film, as
+ * muon_gpu_render_device) sampling with the current network; its path
+ * vertices become training samples. params->integrator must be the path
+ * tracer; params->wave_paths is the guide's. */
+int muon_gpu_guide_render_device(MuonGuide *guide, const MuonRenderParams *params, double *d_sum, double *d_sum_sq,
+                                 uint32_t *d_count);
+/* `steps` Adam steps on batches drawn from the collected samples; the mean
+ * loss of the last step goes to *loss when not NULL. */
+int muon_gpu_guide_train(MuonGuide *guide, int32_t steps, double *loss);
+/* Network outputs (n x 40 raw values) for features (n x 8), on the
+ * tensor-core inference path; host arrays. */
+int muon_gpu_guide_forward(MuonGuide *guide, const float *features, int64_t n, float *out);
+/* Gradients (MUON_GUIDE_PARAMS values) of the mean loss over one batch of n
+ * samples (features n x 8, unit directions n x 3, weights n) and the loss;
+ * host arrays. */
+int muon_gpu_guide_gradients(MuonGuide *guide, const float *features, const float *dirs, const float *weights,
+                             int32_t n, float *grad, double *loss);
+int muon_gpu_guide_get_params(const MuonGuide *guide, float *params);
+int muon_gpu_guide_set_params(MuonGuide *guide, const float *params);
+/* Training samples collected so far. */
+int muon_gpu_guide_samples(const MuonGuide *guide, uint64_t *count);
+
 /* Thread-local description of the last failure on this thread. */
 const char *muon_gpu_last_error(void);
 

@@ -280,6 +280,70 @@ class Batch:
             pass
 
 
+class Guide:
+    """Learned path guiding for one scene (muon_gpu_guide_*)."""
+
+    def __init__(self, scene: Scene, **config):
+        self.scene = scene
+        cfg = native.GuideConfig()
+        for k, v in config.items():
+            setattr(cfg, k, v)
+        h = C.c_void_p()
+        check(load().muon_gpu_guide_create(scene._h, C.byref(cfg), C.byref(h)))
+        self._h = h
+
+    def render_device(self, params: native.RenderParams, d_sum: int, d_sum_sq: int, d_count: int) -> None:
+        check(load().muon_gpu_guide_render_device(self._h, C.byref(params), C.c_void_p(d_sum), C.c_void_p(d_sum_sq),
+                                                  C.c_void_p(d_count)))
+
+    def train(self, steps: int) -> float:
+        loss = C.c_double()
+        check(load().muon_gpu_guide_train(self._h, steps, C.byref(loss)))
+        return loss.value
+
+    def forward(self, features: np.ndarray) -> np.ndarray:
+        f = np.ascontiguousarray(features, dtype=np.float32)
+        out = np.zeros((len(f), 40), dtype=np.float32)
+        check(load().muon_gpu_guide_forward(self._h, f.ctypes.data_as(C.POINTER(C.c_float)), len(f),
+                                            out.ctypes.data_as(C.POINTER(C.c_float))))
+        return out
+
+    def gradients(self, features: np.ndarray, dirs: np.ndarray, weights: np.ndarray) -> tuple[np.ndarray, float]:
+        f = np.ascontiguousarray(features, dtype=np.float32)
+        d = np.ascontiguousarray(dirs, dtype=np.float32)
+        w = np.ascontiguousarray(weights, dtype=np.float32)
+        g = np.zeros(native.GUIDE_PARAMS, dtype=np.float32)
+        loss = C.c_double()
+        fp = lambda a: a.ctypes.data_as(C.POINTER(C.c_float))
+        check(load().muon_gpu_guide_gradients(self._h, fp(f), fp(d), fp(w), len(f), fp(g), C.byref(loss)))
+        return g, loss.value
+
+    def params(self) -> np.ndarray:
+        out = np.zeros(native.GUIDE_PARAMS, dtype=np.float32)
+        check(load().muon_gpu_guide_get_params(self._h, out.ctypes.data_as(C.POINTER(C.c_float))))
+        return out
+
+    def set_params(self, values: np.ndarray) -> None:
+        v = np.ascontiguousarray(values, dtype=np.float32)
+        check(load().muon_gpu_guide_set_params(self._h, v.ctypes.data_as(C.POINTER(C.c_float))))
+
+    def samples(self) -> int:
+        n = C.c_uint64()
+        check(load().muon_gpu_guide_samples(self._h, C.byref(n)))
+        return n.value
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            load().muon_gpu_guide_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 def render_file(path: str, **overrides) -> tuple[FilmResult, float]:
     """Parses and renders a scene file; returns the film and the file's gamma."""
     scene = Scene.from_file(path)

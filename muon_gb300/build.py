@@ -21,8 +21,9 @@ OBJ = os.path.join(LIB, "obj")
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
-CUDA_UNITS = ["kernels.cu", "noalloc.cu"]
-HOST_UNITS = ["scene_parser.cc", "mesh_io.cc", "scene_build.cc", "host_api.cc", "render.cc", "batch.cc"]
+CUDA_UNITS = ["kernels.cu", "noalloc.cu", "guide.cu"]
+HOST_UNITS = ["scene_parser.cc", "mesh_io.cc", "scene_build.cc", "host_api.cc", "render.cc", "batch.cc",
+              "guide_host.cc"]
 CXXFLAGS = ["-std=c++17", "-O2", "-fPIC", "-ffp-contract=off", "-Wall", "-Wno-unused-function"]
 NVFLAGS = [ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off",
            "--extended-lambda"] + os.environ.get("MUON_NVCC_EXTRA", "").split()

@@ -43,6 +43,12 @@ struct GuideDev {
   int32_t pad;
 };
 
+// A path-traced render with guiding (render.cc): the single-scene wavefront
+// loop with the guide's inference before shading, guided sampling, and
+// training records collected after each wave. Throws CudaError.
+void RenderGuided(MuonScene *sc, const MuonRenderParams &p, double *d_sum, double *d_sq, uint32_t *d_cnt,
+                  const GuideDev &g);
+
 // Kernels of the guided render (kernels.cu).
 void LaunchGuideInfer(const DevScene &s, const PathBuffers &b, WaveCounters wc, int bounce, int bound, int isect,
                       const GuideDev &g, cudaStream_t st);
@@ -68,13 +74,13 @@ struct GuideTrainBuffers {
   float *dz[2];     // batch x 64 gradients (ping-pong)
   float *partial;   // per chunk: all weight and bias gradients
   float *grad;      // guide::kParams
-  double *loss;     // one value per chunk
+  double *loss;     // loss sum of every 256 consecutive samples
   int32_t chunks;
 };
 size_t GuideTrainBytes(int batch);
 void GuideTrainCarve(void *base, int batch, GuideTrainBuffers *out);
-// Gradients of the mean loss over the batch into tb.grad; loss into *loss_out
-// (device double) when not null.
+// Gradients of the mean loss over the batch into tb.grad and the loss sums
+// into tb.loss.
 void LaunchGuideGradients(const float *params, const float *features, const float *dirs, const float *weights,
                           int batch, const GuideTrainBuffers &tb, cudaStream_t st);
 // Gathers `batch` samples from the pool at random positions (seeded) into

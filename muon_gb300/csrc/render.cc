@@ -15,6 +15,7 @@
 #include <string>
 #include <vector>
 
+#include "guide.h"
 #include "host_cuda.h"
 #include "host_scene.h"
 #include "kernels.cuh"
@@ -281,7 +282,8 @@ namespace {
 // CUDA graph and replayed; the host synchronises once per frame. Unbounded
 // depth (max_depth -1): the host reads the queue length after every bounce and
 // stops when no path continues.
-void RenderDevice(MuonScene *sc, const MuonRenderParams &p, double *d_sum, double *d_sq, uint32_t *d_cnt) {
+void RenderDevice(MuonScene *sc, const MuonRenderParams &p, double *d_sum, double *d_sq, uint32_t *d_cnt,
+                  const GuideDev *guide = nullptr) {
   cudaStream_t st = sc->stream;
   const bool pt = p.integrator == MUON_INTEGRATOR_PATHTRACER;
   // Raytracer / AnalyticDirect: one kernel follows each path to its end.
@@ -357,18 +359,25 @@ void RenderDevice(MuonScene *sc, const MuonRenderParams &p, double *d_sum, doubl
       }
       for (int k = 0; k < (whitted ? 0 : bounces); ++k) {
         timed(0, [&] { LaunchExtend(sc->dev, b, wc, k, w.n, p.intersect_mode, stats_on, st); });
+        if (guide) timed(2, [&] { LaunchGuideInfer(sc->dev, b, wc, k, w.n, p.intersect_mode, *guide, st); });
         if (!pt) {
           timed(2, [&] { LaunchShadeDebug(sc->dev, b, wc, p.integrator, w.n, p.intersect_mode, st); });
           break;
         }
-        timed(2, [&] { LaunchShadePath(sc->dev, w, sp, b, wc, k, w.n, st); });
+        timed(2, [&] {
+          if (guide) LaunchShadePathGuided(sc->dev, w, sp, b, wc, k, w.n, *guide, st);
+          else LaunchShadePath(sc->dev, w, sp, b, wc, k, w.n, st);
+        });
         if (slots > 0) {
           timed(1, [&] {
             LaunchOcclude(sc->dev, b, wc, k, slots, static_cast<int>(std::min<int64_t>(int64_t(w.n) * slots, INT32_MAX)),
                           p.intersect_mode, stats_on, st);
           });
         }
-        timed(3, [&] { LaunchFold(b, wc, k, slots, w.n, st); });
+        timed(3, [&] {
+          if (guide) LaunchFoldGuided(b, wc, k, slots, w.n, *guide, st);
+          else LaunchFold(b, wc, k, slots, w.n, st);
+        });
         if (host_loop) {
           CUDA_TRY(cudaMemcpyAsync(sc->h_counters, wc.count(k + 1), sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
           CUDA_TRY(cudaStreamSynchronize(st));
@@ -377,18 +386,26 @@ void RenderDevice(MuonScene *sc, const MuonRenderParams &p, double *d_sum, doubl
       }
       LaunchFilm(w, b, d_sum, d_sq, d_cnt, st);
       ++launches;
+      if (guide) {
+        LaunchGuideCollect(b, wc, std::min(bounces, guide->rec_bounces), w.n, *guide, st);
+        ++launches;
+      }
     }
     timed_pairs = sc->events_used;
   };
 
   cudaEvent_t t0 = sc->NextEvent(2)->a;
   cudaEvent_t t1 = sc->events[0].b;
-  char keybuf[512];
-  std::snprintf(keybuf, sizeof(keybuf), "%d %d %d %d %d %d %d %d %d %d %llu %d %d %u %p %p %p %zu %d", p.integrator,
-                p.pixel_samples, p.light_samples, p.light_stratify, p.next_event_estimation, p.russian_roulette,
-                p.importance_sampling, p.min_depth, p.max_depth, p.sample_offset, (unsigned long long)p.seed,
-                p.intersect_mode, p.wave_paths, p.flags, (void *)d_sum, (void *)d_sq, (void *)d_cnt, waves.size(),
-                bounces);
+  char keybuf[640];
+  int klen = std::snprintf(keybuf, sizeof(keybuf), "%d %d %d %d %d %d %d %d %d %d %llu %d %d %u %p %p %p %zu %d",
+                           p.integrator, p.pixel_samples, p.light_samples, p.light_stratify, p.next_event_estimation,
+                           p.russian_roulette, p.importance_sampling, p.min_depth, p.max_depth, p.sample_offset,
+                           (unsigned long long)p.seed, p.intersect_mode, p.wave_paths, p.flags, (void *)d_sum,
+                           (void *)d_sq, (void *)d_cnt, waves.size(), bounces);
+  if (guide && klen > 0 && klen < static_cast<int>(sizeof(keybuf)))
+    std::snprintf(keybuf + klen, sizeof(keybuf) - klen, " guide %p %p %p %p %d %d %.9g %.9g %.9g %.9g", guide->wt,
+                  (void *)guide->mix, (void *)guide->rec, (void *)guide->pool, guide->rec_cap, guide->rec_bounces,
+                  guide->alpha, guide->lo[0], guide->lo[1], guide->inv_ext[0]);
   const bool use_graph = bounded && !(p.flags & MUON_RENDER_NO_GRAPH);
   if (moved) sc->DropGraph();
   CUDA_TRY(cudaEventRecord(t0, st));
@@ -477,6 +494,15 @@ void RenderDevice(MuonScene *sc, const MuonRenderParams &p, double *d_sum, doubl
 }
 
 }  // namespace
+
+namespace muon_gpu {
+
+void RenderGuided(MuonScene *sc, const MuonRenderParams &p, double *d_sum, double *d_sq, uint32_t *d_cnt,
+                  const GuideDev &g) {
+  RenderDevice(sc, p, d_sum, d_sq, d_cnt, &g);
+}
+
+}  // namespace muon_gpu
 
 
 extern "C" {

@@ -112,6 +112,14 @@ class BatchTuning(C.Structure):
                 ("pad", C.c_int32), ("best_ms", C.c_double)]
 
 
+class GuideConfig(C.Structure):
+    _fields_ = [("batch", C.c_int32), ("wave_paths", C.c_int32), ("record_bounces", C.c_int32),
+                ("pool_capacity", C.c_int32), ("learning_rate", C.c_float), ("mixture_fraction", C.c_float),
+                ("seed", C.c_uint64)]
+
+
+GUIDE_PARAMS = 31528
+
 # Every entry point declared in include/muon_gpu.h: name -> (restype, argtypes)
 SIGNATURES = {
     "muon_parse_scene_file": (C.c_int, [C.c_char_p, C.POINTER(C.c_void_p)]),
@@ -145,6 +153,18 @@ SIGNATURES = {
     "muon_gpu_batch_stats": (C.c_int, [C.c_void_p, C.POINTER(Stats), C.POINTER(BatchSceneStats)]),
     "muon_gpu_render_batch": (C.c_int, [C.POINTER(C.c_void_p), C.POINTER(RenderParams), C.c_int32,
                                         C.POINTER(Film)]),
+    "muon_gpu_guide_create": (C.c_int, [C.c_void_p, C.POINTER(GuideConfig), C.POINTER(C.c_void_p)]),
+    "muon_gpu_guide_destroy": (None, [C.c_void_p]),
+    "muon_gpu_guide_render_device": (C.c_int, [C.c_void_p, C.POINTER(RenderParams), C.c_void_p, C.c_void_p,
+                                               C.c_void_p]),
+    "muon_gpu_guide_train": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_double)]),
+    "muon_gpu_guide_forward": (C.c_int, [C.c_void_p, C.POINTER(C.c_float), C.c_int64, C.POINTER(C.c_float)]),
+    "muon_gpu_guide_gradients": (C.c_int, [C.c_void_p, C.POINTER(C.c_float), C.POINTER(C.c_float),
+                                           C.POINTER(C.c_float), C.c_int32, C.POINTER(C.c_float),
+                                           C.POINTER(C.c_double)]),
+    "muon_gpu_guide_get_params": (C.c_int, [C.c_void_p, C.POINTER(C.c_float)]),
+    "muon_gpu_guide_set_params": (C.c_int, [C.c_void_p, C.POINTER(C.c_float)]),
+    "muon_gpu_guide_samples": (C.c_int, [C.c_void_p, C.POINTER(C.c_uint64)]),
 }
 
 _lib = None

@@ -360,9 +360,73 @@ def batch_scene(index: int, seed: int = 1, max_tris: int = 500_000, resolutions=
     return "\n".join(L) + "\n"
 
 
+def slit_room(width: int = 1024, height: int = 1024, spp: int = 16, max_depth: int = 10, level: int = 8,
+              clutter: int = 10000, seed: int = 1) -> str:
+    """Guiding workload: the dense-mesh icosphere and clutter inside a closed
+    room [-1,1]x[0,2]x[-1,1] whose only opening is a 0.05-wide slit across the
+    ceiling (x in [-0.025, 0.025]); a 1x1 quad light of emission 50 outside,
+    0.5 above the slit, lights the room through it. Every object (each wall,
+    the icosphere, the clutter) has its own GGX material with alpha
+    U[0.05, 0.5]. Camera inside the room. NEE with MIS, BRDF sampling."""
+    rng = np.random.default_rng(seed)
+    L = ["# closed room lit through a ceiling slit",
+         f"random_seed {seed}",
+         f"film_size {width} {height}",
+         "integrator pathtracer",
+         f"pixel_samples {spp}",
+         f"max_depth {max_depth}",
+         "next_event_estimation mis",
+         "importance_sampling brdf",
+         "russian_roulette off",
+         "camera 0 1.1 0.95  0 0.7 -1  0 1 0  60",
+         "quad_light -0.5 2.5 -0.5  0 0 1  1 0 0  50 50 50",
+         "emission 0 0 0",
+         "ambient 0 0 0"]
+
+    def ggx(kd):
+        return ["brdf ggx", "diffuse " + _v(*kd), "specular 0.04 0.04 0.04",
+                "roughness " + _f(rng.uniform(0.05, 0.5))]
+
+    h = 0.025
+    walls = [
+        ((0.6, 0.6, 0.6), [((-1, 0, -1), (-1, 0, 1), (1, 0, 1), (1, 0, -1))]),                       # floor
+        ((0.6, 0.6, 0.6), [((-1, 2, -1), (-h, 2, -1), (-h, 2, 1), (-1, 2, 1)),                       # ceiling
+                           ((h, 2, -1), (1, 2, -1), (1, 2, 1), (h, 2, 1))]),
+        ((0.6, 0.6, 0.6), [((-1, 0, -1), (1, 0, -1), (1, 2, -1), (-1, 2, -1))]),                     # back
+        ((0.6, 0.6, 0.6), [((-1, 0, 1), (-1, 2, 1), (1, 2, 1), (1, 0, 1))]),                         # front
+        ((0.63, 0.065, 0.05), [((-1, 0, -1), (-1, 2, -1), (-1, 2, 1), (-1, 0, 1))]),                 # left
+        ((0.14, 0.45, 0.09), [((1, 0, -1), (1, 0, 1), (1, 2, 1), (1, 2, -1))]),                      # right
+    ]
+    for kd, quads in walls:
+        L += ggx(kd)
+        for a, b, c, d in quads:
+            _quad(L, a, b, c, d)
+    V, F = icosphere(level)
+    V = V * (1.0 + 0.1 * value_noise(V, seed, freq=3.0))[:, None]
+    L += ggx((0.5, 0.45, 0.4))
+    L += ["push_transform", "translate 0 0.6 -0.2", "scale 0.0005 0.0005 0.0005"]
+    _mesh_fast(L, V * 1000.0, F)
+    L.append("pop_transform")
+    if clutter:
+        L += ggx((0.3, 0.4, 0.6))
+        L += ["push_transform", "scale 0.001 0.001 0.001"]
+        centres = rng.uniform([-0.95, 0.05, -0.95], [0.95, 1.95, 0.95], size=(clutter, 3))
+        edge = rng.uniform(0.01, 0.05, size=clutter)
+        d1 = rng.normal(size=(clutter, 3))
+        d1 /= np.linalg.norm(d1, axis=1, keepdims=True)
+        d2 = rng.normal(size=(clutter, 3))
+        d2 -= (d2 * d1).sum(1, keepdims=True) * d1
+        d2 /= np.linalg.norm(d2, axis=1, keepdims=True)
+        tri = np.stack([centres, centres + d1 * edge[:, None], centres + (0.5 * d1 + 0.866 * d2) * edge[:, None]], 1)
+        _mesh_fast(L, tri.reshape(-1, 3) * 1000.0, np.arange(3 * clutter, dtype=np.int64).reshape(-1, 3))
+        L.append("pop_transform")
+    return "\n".join(L) + "\n"
+
+
 WORKLOADS = {
     "cornell": cornell,
     "sphere_field": sphere_field,
     "feature_mix": feature_mix,
     "dense_mesh": dense_mesh,
+    "slit_room": slit_room,
 }

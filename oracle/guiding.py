@@ -185,3 +185,22 @@ def features_of(pos, normal, wo, roughness, lo, hi):
 
     p = (np.asarray(pos, dtype=np.float64) - lo) / np.maximum(np.asarray(hi) - lo, 1e-30)
     return np.concatenate([np.clip(p, 0, 1), sph(normal), sph(wo), np.asarray(roughness)[..., None]], axis=-1)
+
+
+def flatten(params) -> np.ndarray:
+    """(W, b) per layer -> the library's flat FP32 layout (W [in][out], then b)."""
+    return np.concatenate([np.concatenate([w.ravel(), b.ravel()]) for w, b in params]).astype(np.float32)
+
+
+def unflatten(flat: np.ndarray):
+    out, off = [], 0
+    for fan_in, fan_out in LAYERS:
+        w = np.asarray(flat[off:off + fan_in * fan_out], dtype=np.float64).reshape(fan_in, fan_out)
+        off += fan_in * fan_out
+        b = np.asarray(flat[off:off + fan_out], dtype=np.float64)
+        off += fan_out
+        out.append((w, b))
+    return out
+
+
+N_PARAMS = sum(a * b + b for a, b in LAYERS)

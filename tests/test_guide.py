@@ -1,0 +1,129 @@
+"""Learned path guiding: the network, its training and the guided estimator.
+
+The oracle (oracle/guiding.py, FP64 numpy) is pinned first by finite
+differences. The GPU's tensor-core forward pass must match the oracle's
+forward pass with the same BF16 rounding of weights and activations to the
+accuracy BF16 allows; its FP32 training gradients must match the oracle's
+FP64 gradients for the same parameters; training must lower the loss on a
+known target; guided renders must converge to the same image as plain ones
+(the estimator is unbiased whatever the network predicts).
+"""
+import numpy as np
+import pytest
+
+import muon_gb300 as m
+from muon_gb300 import native, scenes
+from oracle import guiding as G
+
+
+def test_oracle_gradients_match_finite_differences():
+    rng = np.random.default_rng(0)
+    n = 12
+    feat = rng.uniform(0, 1, (n, 8))
+    w = rng.normal(size=(n, 3))
+    w /= np.linalg.norm(w, axis=1, keepdims=True)
+    wt = rng.uniform(0.1, 2.0, n)
+    params = G.init_params(3)
+    out, acts, zs = G.forward(params, feat, bf16_round=False)
+    loss, dout = G.loss_grad(out, w, wt)
+    grads = G.backward(params, acts, zs, dout)
+    eps = 1e-6
+    for j in range(G.N_OUT):
+        o2 = out.copy()
+        o2[5, j] += eps
+        fd = (G.loss_grad(o2, w, wt)[0] - loss) / eps
+        assert abs(fd - dout[5, j]) <= 1e-5 * max(1.0, abs(fd))
+    for li, (a, b) in [(0, (17, 3)), (1, (5, 60)), (3, (40, 2)), (4, (63, 39))]:
+        p2 = [(x.copy(), y.copy()) for x, y in params]
+        p2[li][0][a, b] += eps
+        o3, _, _ = G.forward(p2, feat, bf16_round=False)
+        fd = (G.loss_grad(o3, w, wt)[0] - loss) / eps
+        assert abs(fd - grads[li][0][a, b]) <= 1e-5 * max(1.0, abs(fd))
+
+
+def test_flat_layout_round_trip():
+    p = G.init_params(5)
+    flat = G.flatten(p)
+    assert flat.size == G.N_PARAMS == native.GUIDE_PARAMS
+    q = G.unflatten(flat)
+    assert all(np.allclose(a[0], b[0], atol=1e-7) and np.allclose(a[1], b[1]) for a, b in zip(p, q))
+
+
+def tiny_scene():
+    return m.Scene.from_string(scenes.cornell(32, 32, 4, 5, 1))
+
+
+def random_batch(n, seed):
+    rng = np.random.default_rng(seed)
+    feat = rng.uniform(0, 1, (n, 8)).astype(np.float32)
+    d = rng.normal(size=(n, 3))
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    w = rng.uniform(0.05, 3.0, n).astype(np.float32)
+    return feat, d.astype(np.float32), w
+
+
+@pytest.mark.gpu
+def test_tensor_core_forward_matches_oracle(lib):
+    guide = m.Guide(tiny_scene(), seed=11)
+    params = G.unflatten(guide.params())
+    # non-zero biases so that they are exercised too
+    rng = np.random.default_rng(1)
+    params = [(w, rng.normal(0, 0.1, b.shape)) for w, b in params]
+    guide.set_params(G.flatten(params))
+    params = G.unflatten(G.flatten(params))
+    feat, _, _ = random_batch(1000, 2)
+    got = guide.forward(feat)
+    ref, _, _ = G.forward(params, feat.astype(np.float64), bf16_round=True)
+    scale = np.abs(ref).max()
+    err = np.abs(got - ref).max() / scale
+    print(f"forward: max error {err:.3g} of the output scale {scale:.3g}")
+    assert err < 2e-2
+    assert np.corrcoef(got.ravel(), ref.ravel())[0, 1] > 0.9995
+
+
+@pytest.mark.gpu
+def test_training_gradients_match_oracle(lib):
+    guide = m.Guide(tiny_scene(), seed=12)
+    params = G.unflatten(guide.params())
+    feat, d, w = random_batch(3000, 3)
+    grad, loss = guide.gradients(feat, d, w)
+    out, acts, zs = G.forward(params, feat.astype(np.float64), bf16_round=False)
+    ref_loss, dout = G.loss_grad(out, d.astype(np.float64), w.astype(np.float64))
+    ref = G.flatten(G.backward(params, acts, zs, dout)).astype(np.float64)
+    rel = np.abs(grad - ref).max() / np.abs(ref).max()
+    print(f"gradients: max error {rel:.3g} of the largest gradient; loss {loss:.6f} vs {ref_loss:.6f}")
+    assert abs(loss - ref_loss) <= 1e-4 * abs(ref_loss)
+    assert rel < 1e-3
+
+
+@pytest.mark.gpu
+def test_guided_render_is_unbiased(lib):
+    """Plain and guided renders of the Cornell box converge to the same
+    image, before and after training (mixture sampled with probability 0.5)."""
+    import torch
+
+    scene = m.Scene.from_string(scenes.cornell(32, 32, 4096, 5, 1))
+    plain = scene.render(pixel_samples=4096, seed=5)
+    guide = m.Guide(scene, seed=3, wave_paths=1 << 20, batch=1 << 14)
+    h, w = scene.height, scene.width
+    s = torch.zeros((h, w, 3), dtype=torch.float64, device="cuda")
+    q = torch.zeros_like(s)
+    c = torch.zeros((h, w), dtype=torch.int32, device="cuda")
+    for it in range(4):
+        p = scene.params(pixel_samples=1024, seed=100 + it, sample_offset=1024 * it,
+                         flags=native.RENDER_ACCUMULATE if it else 0)
+        guide.render_device(p, s.data_ptr(), q.data_ptr(), c.data_ptr())
+        guide.train(8)
+    torch.cuda.synchronize()
+    assert guide.samples() > 0
+    gs, gq, gc = s.cpu().numpy(), q.cpu().numpy(), c.cpu().numpy()
+    assert np.all(gc == 4096)
+    mean_g = gs / gc[..., None]
+    var_g = np.maximum(gq / gc[..., None] - mean_g ** 2, 0) / gc[..., None]
+    mean_p, var_p = plain.mean(), plain.variance_of_mean()
+    img_se = np.sqrt(var_g.sum() + var_p.sum()) / mean_g.size
+    diff = mean_g.mean() - mean_p.mean()
+    print(f"image mean guided {mean_g.mean():.5f} plain {mean_p.mean():.5f} ({diff / img_se:+.2f} se)")
+    assert abs(diff) <= 4 * img_se
+    z = (mean_g - mean_p) / np.sqrt(var_g + var_p + 1e-30)
+    assert (np.abs(z) > 4).mean() <= 0.01

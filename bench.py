@@ -46,6 +46,12 @@ WORKLOADS = {
     # traversal-bound: 1,310,720-triangle displaced icosphere (level 8) + 10k clutter triangles in the Cornell box
     "dense_mesh": {"workload": "dense_mesh", "triangles": 1320756, "width": 1024, "height": 1024, "spp": 256,
                    "max_depth": 10, "nee": "mis", "importance_sampling": "brdf", "seed": 1},
+    # learned path guiding: time to RMSE 1e-2 against a converged plain render, guided vs plain
+    "guiding": {"workload": "slit_room", "triangles": 1320756 + 10000 + 14, "width": 1024, "height": 1024,
+                "max_depth": 10, "nee": "mis", "importance_sampling": "brdf", "seed": 1, "target_rmse": 1e-2,
+                "reference_spp": 8192, "pass_spp": 16, "train_steps_per_pass": 8, "train_passes": 24,
+                "batch": 1 << 18,
+                "mixture_fraction": 0.5},
     # 64 seeded scenes of uneven size in one batched wavefront
     "batch64": {"workload": "batch64", "scenes": 64, "triangles": "log-uniform 1k-500k per scene",
                 "resolutions": [128, 256, 512, 1024], "spp": "uniform 4-64", "max_depth": "uniform 4-10",
@@ -246,11 +252,124 @@ def run_batch(args) -> None:
     print(json.dumps(line), flush=True)
 
 
+def run_guiding(args) -> None:
+    """Time to reach RMSE 1e-2 against a converged plain render of the slit
+    room: the plain GPU tracer and the guided one (training time included),
+    both rendering progressive passes of `pass_spp` samples; device time with
+    CUDA events, the RMSE evaluations between passes excluded."""
+    import torch
+
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    rank = int(os.environ.get("RANK", "0"))
+    torch.cuda.set_device(local)
+    from muon_gb300 import build as native_build
+
+    native_build.build()
+    import muon_gb300 as m
+    from muon_gb300 import native, scenes
+
+    w = WORKLOAD
+    text = scenes.slit_room(w["width"], w["height"], w["pass_spp"], w["max_depth"], seed=w["seed"])
+    scene = m.Scene.from_string(text)
+    H, W = scene.height, scene.width
+    stream = torch.cuda.ExternalStream(scene.stream())
+
+    def film():
+        return (torch.zeros((H, W, 3), dtype=torch.float64, device="cuda"),
+                torch.zeros((H, W, 3), dtype=torch.float64, device="cuda"),
+                torch.zeros((H, W), dtype=torch.int32, device="cuda"))
+
+    ptr = lambda f: [x.data_ptr() for x in f]
+    # converged reference, plain tracer, in passes of at most 256 spp
+    ref = film()
+    t0 = time.perf_counter()
+    done = 0
+    while done < w["reference_spp"]:
+        n = min(256, w["reference_spp"] - done)
+        scene.render_device(scene.params(pixel_samples=n, seed=7777, sample_offset=done,
+                                         flags=native.RENDER_ACCUMULATE if done else 0), *ptr(ref))
+        done += n
+    torch.cuda.synchronize()
+    ref_s = time.perf_counter() - t0
+    ref_img = ref[0] / ref[2][..., None].double()
+
+    def rmse(f):
+        img = f[0] / f[2].clamp(min=1)[..., None].double()
+        return float(torch.sqrt(((img - ref_img) ** 2).mean()))
+
+    def progressive(render_pass, train=None, max_passes=4096):
+        f = film()
+        dev_ms, spp, passes, counted = 0.0, 0, 0, 0
+        trace = []
+        while passes < max_passes:
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            stream.wait_stream(torch.cuda.current_stream())
+            e0.record(stream)
+            counted += render_pass(f, spp)
+            if train is not None:
+                train()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            dev_ms += e0.elapsed_time(e1)
+            spp += w["pass_spp"]
+            passes += 1
+            err = rmse(f)
+            trace.append((spp, round(dev_ms, 2), round(err, 5)))
+            if err <= w["target_rmse"]:
+                break
+        return dev_ms, spp, err, counted, trace
+
+    # passes launch kernel by kernel: a graph would be captured again for
+    # every pass (its sample offset changes)
+    def plain_pass(f, spp):
+        scene.render_device(scene.params(pixel_samples=w["pass_spp"], seed=11, sample_offset=spp,
+                                         flags=native.RENDER_NO_GRAPH | (native.RENDER_ACCUMULATE if spp else 0)),
+                            *ptr(f))
+        st = scene.stats()
+        return st["primary_rays"] + st["secondary_rays"]
+
+    guide = m.Guide(scene, seed=w["seed"], batch=w["batch"], mixture_fraction=w["mixture_fraction"])
+
+    def guided_pass(f, spp):
+        guide.render_device(scene.params(pixel_samples=w["pass_spp"], seed=12, sample_offset=spp,
+                                         flags=native.RENDER_NO_GRAPH | (native.RENDER_ACCUMULATE if spp else 0)),
+                            *ptr(f))
+        st = scene.stats()
+        return st["primary_rays"] + st["secondary_rays"]
+
+    passes_trained = [0]
+
+    def train():
+        # online training during the first passes, then the network is frozen
+        if passes_trained[0] < w["train_passes"]:
+            guide.train(w["train_steps_per_pass"])
+            passes_trained[0] += 1
+
+    plain_ms, plain_spp, plain_err, plain_rays, plain_trace = progressive(plain_pass)
+    guided_ms, guided_spp, guided_err, guided_rays, guided_trace = progressive(guided_pass, train=train)
+    if rank != 0:
+        return
+    line = {
+        "metric": "time-to-RMSE 1e-2 (guided / plain)", "value": round(guided_ms / plain_ms, 4), "unit": "ratio",
+        "n_gpus": 1, "steps": 1, "warmup": 0, "higher_is_better": False, "scaling": "none", "vs_baseline": None,
+        "dtype": "f32 (bf16 network)", "data": "synthetic (seeded slit room)",
+        "config": dict(WORKLOAD, reference_seconds=round(ref_s, 2)),
+        "plain": {"ms": round(plain_ms, 1), "spp": plain_spp, "rmse": round(plain_err, 5),
+                  "mrays_per_s": round(plain_rays / (plain_ms * 1e3), 1)},
+        "guided": {"ms": round(guided_ms, 1), "spp": guided_spp, "rmse": round(guided_err, 5),
+                   "mrays_per_s": round(guided_rays / (guided_ms * 1e3), 1), "samples": guide.samples()},
+        "trace_plain": plain_trace[-8:], "trace_guided": guided_trace[-8:],
+    }
+    print(json.dumps(line), flush=True)
+
+
 def run_ours(args) -> None:
     import torch
 
     if WORKLOAD["workload"] == "batch64":
         return run_batch(args)
+    if WORKLOAD["workload"] == "slit_room":
+        return run_guiding(args)
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

@@ -2,6 +2,10 @@
 
     python -m muon_gb300.profile_frame [--workload sphere_field] [--frames 1]
         [--warmup 2] [--mode exact|fast] [--width 512 --height 512 --spp 64]
+        [--guided] [--train-steps 4]
+
+With --guided the frames are guided renders (learned path guiding) and the
+network trains for --train-steps Adam steps after each of them.
 
 Used as the target of the ncu captures summarised in profiles/: the same
 workload as bench.py, without its timing, e2e and CPU-baseline parts.
@@ -22,10 +26,31 @@ def main() -> None:
     ap.add_argument("--width", type=int, default=512)
     ap.add_argument("--height", type=int, default=512)
     ap.add_argument("--spp", type=int, default=64)
+    ap.add_argument("--guided", action="store_true")
+    ap.add_argument("--train-steps", type=int, default=4)
+    ap.add_argument("--batch", type=int, default=1 << 18)
     a = ap.parse_args()
     text = scenes.WORKLOADS[a.workload](width=a.width, height=a.height, spp=a.spp)
     scene = Scene.from_string(text)
     mode = {"exact": native.ISECT_EXACT, "fast": native.ISECT_FAST, "watertight": native.ISECT_WATERTIGHT}[a.mode]
+    if a.guided:
+        import torch
+
+        from . import Guide
+
+        guide = Guide(scene, seed=1, batch=a.batch)
+        n = scene.width * scene.height
+        film = [torch.zeros((n, 3), dtype=torch.float64, device="cuda"),
+                torch.zeros((n, 3), dtype=torch.float64, device="cuda"),
+                torch.zeros(n, dtype=torch.int32, device="cuda")]
+        for k in range(a.warmup + a.frames):
+            guide.render_device(scene.params(intersect_mode=mode, seed=k), *[t.data_ptr() for t in film])
+            guide.train(a.train_steps)
+        torch.cuda.synchronize()
+        print(f"guided {a.workload} {a.width}x{a.height}x{a.spp}: {guide.samples()} training samples")
+        guide.close()
+        scene.close()
+        return
     for _ in range(a.warmup):
         scene.render(intersect_mode=mode)
     for _ in range(a.frames):

@@ -40,6 +40,11 @@ struct GuideDev {
   GuideSample *pool;     // training samples (ring buffer)
   unsigned long long *pool_count;  // samples ever appended
   uint32_t pool_cap;
+  // shadow slots that become training samples when unblocked: the area-light
+  // samples [0, area_slots) and the MIS ray (mis_slot, -1 if none); set per
+  // render
+  int32_t area_slots;
+  int32_t mis_slot;
   int32_t pad;
 };
 

@@ -891,29 +891,88 @@ __global__ void __launch_bounds__(kBlock, MUON_SHADE_MIN_BLOCKS)
 // After the occlusion pass of a bounce: each entry's radiance plus its
 // unblocked shadow slots moves to its next-bounce entry, or to the path's
 // final radiance when the path ends here.
+// Training samples from a guided vertex's direct light: every unblocked
+// area-light sample and MIS ray becomes (features, direction, weight) with
+// weight = luminance of its contribution / throughput, i.e. f cos L_e times
+// the MIS weight over the density it was drawn from. Together with the
+// continuation records (indirect light) these estimate the full incident
+// radiance the mixture learns. Called by whole warps.
+__device__ __forceinline__ void GuideDirectSamples(const PathBuffers &b, const GuideDev &g, int bounce, int slots,
+                                                   int j, bool valid) {
+  const int lane = threadIdx.x & 31;
+  const bool shaded = valid && b.hits[j].y >= 0;
+  const float4 *c = b.contrib + static_cast<int64_t>(j) * slots;
+  uint32_t count = 0;
+  if (shaded) {
+    for (int k = 0; k < slots; ++k) {
+      if (k >= g.area_slots && k != g.mis_slot) continue;
+      const float4 v = c[k];
+      if (v.x != 0.0f || v.y != 0.0f || v.z != 0.0f) ++count;
+    }
+  }
+  // warp-wide exclusive scan of the counts, one atomic per warp
+  uint32_t incl = count;
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += y;
+  }
+  const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
+  if (total == 0) return;
+  unsigned long long base = 0;
+  if (lane == 31) base = atomicAdd(g.pool_count, static_cast<unsigned long long>(total));
+  base = __shfl_sync(0xffffffffu, base, 31);
+  if (!count) return;
+  unsigned long long idx = base + (incl - count);
+  const float4 tp = Pick(b.tp, bounce & 1)[j];
+  const float4 f0 = g.feat[2 * static_cast<int64_t>(j)], f1 = g.feat[2 * static_cast<int64_t>(j) + 1];
+  const float tpc[3] = {tp.x, tp.y, tp.z};
+  const float lum[3] = {0.2126f, 0.7152f, 0.0722f};
+  for (int k = 0; k < slots; ++k) {
+    if (k >= g.area_slots && k != g.mis_slot) continue;
+    const float4 v = c[k];
+    if (!(v.x != 0.0f || v.y != 0.0f || v.z != 0.0f)) continue;
+    const float vc[3] = {v.x, v.y, v.z};
+    float wgt = 0.0f;
+    for (int q = 0; q < 3; ++q)
+      if (tpc[q] > 0.0f) wgt += lum[q] * fmaxf(vc[q], 0.0f) / tpc[q];
+    const float4 dir = b.slot_dir[static_cast<int64_t>(j) * slots + k];
+    GuideSample smp;
+    smp.f0 = f0;
+    smp.f1 = f1;
+    // a non-finite weight becomes 0, which training ignores
+    smp.dir_w = make_float4(dir.x, dir.y, dir.z, isfinite(wgt) ? wgt : 0.0f);
+    g.pool[idx % g.pool_cap] = smp;
+    ++idx;
+  }
+}
+
 template <bool kGuide>
 __global__ void __launch_bounds__(kBlock) FoldKernel(PathBuffers b, WaveCounters wc, int bounce, int slots,
                                                      GuideDev g) {
   const int n = static_cast<int>(*wc.count(bounce));
   const int cur = bounce & 1, nxt = cur ^ 1;
-  for (int j = blockIdx.x * kBlock + threadIdx.x; j < n; j += gridDim.x * kBlock) {
-    float4 r = Pick(b.rad, cur)[j];
-    // Only shaded entries (hits) wrote shadow slots this bounce.
-    if (b.hits[j].y >= 0) {
-      const float4 *c = b.contrib + static_cast<int64_t>(j) * slots;
-      for (int k = 0; k < slots; ++k) {
-        float4 v = c[k];
-        r.x += v.x, r.y += v.y, r.z += v.z;
+  for (int base = blockIdx.x * kBlock; base < n; base += gridDim.x * kBlock) {
+    const int j = base + threadIdx.x;
+    if (j < n) {
+      float4 r = Pick(b.rad, cur)[j];
+      // Only shaded entries (hits) wrote shadow slots this bounce.
+      if (b.hits[j].y >= 0) {
+        const float4 *c = b.contrib + static_cast<int64_t>(j) * slots;
+        for (int k = 0; k < slots; ++k) {
+          float4 v = c[k];
+          r.x += v.x, r.y += v.y, r.z += v.z;
+        }
       }
+      int next = b.link[j];
+      if (kGuide && bounce < g.rec_bounces) {
+        GuideRec &rc = g.rec[static_cast<int64_t>(bounce) * g.rec_cap + j];
+        if (next >= 0) rc.after = r;
+        else rc.tp.w = 0.0f;  // no continuation: nothing to learn from this vertex
+      }
+      if (next >= 0) Pick(b.rad, nxt)[next] = r;
+      else b.final_rad[PathOf(Pick(b.ray_o, cur)[j].w)] = r;
     }
-    int next = b.link[j];
-    if (kGuide && bounce < g.rec_bounces) {
-      GuideRec &rc = g.rec[static_cast<int64_t>(bounce) * g.rec_cap + j];
-      if (next >= 0) rc.after = r;
-      else rc.tp.w = 0.0f;  // no continuation: nothing to learn from this vertex
-    }
-    if (next >= 0) Pick(b.rad, nxt)[next] = r;
-    else b.final_rad[PathOf(Pick(b.ray_o, cur)[j].w)] = r;
+    if (kGuide && bounce < g.rec_bounces) GuideDirectSamples(b, g, bounce, slots, j, j < n);
   }
 }
 

@@ -292,6 +292,12 @@ void RenderDevice(MuonScene *sc, const MuonRenderParams &p, double *d_sum, doubl
   const bool timing = (p.flags & MUON_RENDER_TIMING) != 0;
   ShadeParams sp;
   const int slots = SetupShade(p, sc->dev.num_lights, sc->dev.num_other_lights, &sp);
+  GuideDev guide_local{};
+  if (guide) {
+    guide_local = *guide;
+    guide_local.area_slots = sc->dev.num_lights * sp.per_light;
+    guide_local.mis_slot = sp.mis_slot;
+  }
 
   const int W = sc->img.width, H = sc->img.height;
   const int64_t npix_total = static_cast<int64_t>(W) * H;
@@ -359,13 +365,13 @@ void RenderDevice(MuonScene *sc, const MuonRenderParams &p, double *d_sum, doubl
       }
       for (int k = 0; k < (whitted ? 0 : bounces); ++k) {
         timed(0, [&] { LaunchExtend(sc->dev, b, wc, k, w.n, p.intersect_mode, stats_on, st); });
-        if (guide) timed(2, [&] { LaunchGuideInfer(sc->dev, b, wc, k, w.n, p.intersect_mode, *guide, st); });
+        if (guide) timed(2, [&] { LaunchGuideInfer(sc->dev, b, wc, k, w.n, p.intersect_mode, guide_local, st); });
         if (!pt) {
           timed(2, [&] { LaunchShadeDebug(sc->dev, b, wc, p.integrator, w.n, p.intersect_mode, st); });
           break;
         }
         timed(2, [&] {
-          if (guide) LaunchShadePathGuided(sc->dev, w, sp, b, wc, k, w.n, *guide, st);
+          if (guide) LaunchShadePathGuided(sc->dev, w, sp, b, wc, k, w.n, guide_local, st);
           else LaunchShadePath(sc->dev, w, sp, b, wc, k, w.n, st);
         });
         if (slots > 0) {
@@ -375,7 +381,7 @@ void RenderDevice(MuonScene *sc, const MuonRenderParams &p, double *d_sum, doubl
           });
         }
         timed(3, [&] {
-          if (guide) LaunchFoldGuided(b, wc, k, slots, w.n, *guide, st);
+          if (guide) LaunchFoldGuided(b, wc, k, slots, w.n, guide_local, st);
           else LaunchFold(b, wc, k, slots, w.n, st);
         });
         if (host_loop) {
@@ -387,7 +393,7 @@ void RenderDevice(MuonScene *sc, const MuonRenderParams &p, double *d_sum, doubl
       LaunchFilm(w, b, d_sum, d_sq, d_cnt, st);
       ++launches;
       if (guide) {
-        LaunchGuideCollect(b, wc, std::min(bounces, guide->rec_bounces), w.n, *guide, st);
+        LaunchGuideCollect(b, wc, std::min(bounces, guide->rec_bounces), w.n, guide_local, st);
         ++launches;
       }
     }

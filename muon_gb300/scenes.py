@@ -361,13 +361,14 @@ def batch_scene(index: int, seed: int = 1, max_tris: int = 500_000, resolutions=
 
 
 def slit_room(width: int = 1024, height: int = 1024, spp: int = 16, max_depth: int = 10, level: int = 8,
-              clutter: int = 10000, seed: int = 1) -> str:
+              clutter: int = 10000, seed: int = 1, roughness: float | None = None) -> str:
     """Guiding workload: the dense-mesh icosphere and clutter inside a closed
     room [-1,1]x[0,2]x[-1,1] whose only opening is a 0.05-wide slit across the
     ceiling (x in [-0.025, 0.025]); a 1x1 quad light of emission 50 outside,
     0.5 above the slit, lights the room through it. Every object (each wall,
     the icosphere, the clutter) has its own GGX material with alpha
-    U[0.05, 0.5]. Camera inside the room. NEE with MIS, BRDF sampling."""
+    U[0.05, 0.5] (or `roughness` for all). Camera inside the room. NEE with
+    MIS, BRDF sampling."""
     rng = np.random.default_rng(seed)
     L = ["# closed room lit through a ceiling slit",
          f"random_seed {seed}",
@@ -385,7 +386,7 @@ def slit_room(width: int = 1024, height: int = 1024, spp: int = 16, max_depth: i
 
     def ggx(kd):
         return ["brdf ggx", "diffuse " + _v(*kd), "specular 0.04 0.04 0.04",
-                "roughness " + _f(rng.uniform(0.05, 0.5))]
+                "roughness " + _f(rng.uniform(0.05, 0.5) if roughness is None else roughness)]
 
     h = 0.025
     walls = [

@@ -365,13 +365,16 @@ void RenderDevice(MuonScene *sc, const MuonRenderParams &p, double *d_sum, doubl
       }
       for (int k = 0; k < (whitted ? 0 : bounces); ++k) {
         timed(0, [&] { LaunchExtend(sc->dev, b, wc, k, w.n, p.intersect_mode, stats_on, st); });
-        if (guide) timed(2, [&] { LaunchGuideInfer(sc->dev, b, wc, k, w.n, p.intersect_mode, guide_local, st); });
+        // Guiding covers the first rec_bounces vertices of a path (where the
+        // network is trained); deeper vertices sample the BRDF alone.
+        const bool guided = guide && k < guide->rec_bounces;
+        if (guided) timed(2, [&] { LaunchGuideInfer(sc->dev, b, wc, k, w.n, p.intersect_mode, guide_local, st); });
         if (!pt) {
           timed(2, [&] { LaunchShadeDebug(sc->dev, b, wc, p.integrator, w.n, p.intersect_mode, st); });
           break;
         }
         timed(2, [&] {
-          if (guide) LaunchShadePathGuided(sc->dev, w, sp, b, wc, k, w.n, guide_local, st);
+          if (guided) LaunchShadePathGuided(sc->dev, w, sp, b, wc, k, w.n, guide_local, st);
           else LaunchShadePath(sc->dev, w, sp, b, wc, k, w.n, st);
         });
         if (slots > 0) {
@@ -381,7 +384,7 @@ void RenderDevice(MuonScene *sc, const MuonRenderParams &p, double *d_sum, doubl
           });
         }
         timed(3, [&] {
-          if (guide) LaunchFoldGuided(b, wc, k, slots, w.n, guide_local, st);
+          if (guided) LaunchFoldGuided(b, wc, k, slots, w.n, guide_local, st);
           else LaunchFold(b, wc, k, slots, w.n, st);
         });
         if (host_loop) {

@@ -165,7 +165,7 @@ def run_batch(args) -> None:
 
     texts = batch_texts()
     parsed = [m.parse_string(t) for t in texts]
-    sc = [m.Scene(p) for p in parsed]
+    sc = [m.Scene(p, builder=args.builder) for p in parsed]
     batch = m.Batch(sc)
     params = [s.params(intersect_mode=native.ISECT_EXACT, seed=1000 * rank + i) for i, s in enumerate(sc)]
     t_tune = time.perf_counter()
@@ -209,7 +209,7 @@ def run_batch(args) -> None:
     t0 = time.perf_counter()
     e2e_counted = 0
     for _ in range(e2e_steps):
-        scs = [m.Scene(p) for p in parsed]
+        scs = [m.Scene(p, builder=args.builder) for p in parsed]
         b2 = m.Batch(scs)
         b2.render(params)
         tot, _ = b2.stats()
@@ -234,7 +234,7 @@ def run_batch(args) -> None:
         "metric": METRIC, "value": round(value, 2), "unit": METRIC, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(dev_ms / args.steps, 3), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (64 seeded scenes)",
-        "config": dict(WORKLOAD, parallelism=f"replicas{world}", intersect_mode="exact",
+        "config": dict(WORKLOAD, parallelism=f"replicas{world}", intersect_mode="exact", bvh_builder=args.builder,
                        total_triangles=int(sum(p.desc.num_triangles for p in parsed)),
                        paths_per_step=int(total["paths"]),
                        l2="flushed between steps (256 MiB write)"),
@@ -389,7 +389,7 @@ def run_ours(args) -> None:
     from muon_gb300 import native
 
     text = scene_text()
-    scene = m.Scene.from_string(text)
+    scene = m.Scene.from_string(text, builder=args.builder)
     seed = 1000 + rank
     # Every kernel is timed with CUDA events inside the frame's graph; the
     # frame time below includes that cost.
@@ -452,12 +452,12 @@ def run_ours(args) -> None:
     desc_bytes = (parsed.desc.num_triangles * 80 + parsed.desc.num_spheres * 32 + parsed.desc.num_materials * 56 +
                   parsed.desc.num_lights * 52 + parsed.desc.num_transforms * 192)
     film_bytes = h * w * (3 * 8 * 2 + 4)
-    m.Scene(parsed).render(params)  # warm
+    m.Scene(parsed, builder=args.builder).render(params)  # warm
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     e2e_counted = 0
     for _ in range(e2e_steps):
-        sc = m.Scene(parsed)
+        sc = m.Scene(parsed, builder=args.builder)
         sc.render(params)
         st = sc.stats()
         e2e_counted += st["primary_rays"] + st["secondary_rays"]
@@ -490,7 +490,7 @@ def run_ours(args) -> None:
         "metric": METRIC, "value": round(value, 2), "unit": METRIC, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(dev_ms_max / args.steps, 4), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": f"synthetic (seeded {WORKLOAD['workload'].replace('_', ' ')})",
-        "config": dict(WORKLOAD, parallelism=f"replicas{world}", intersect_mode="exact",
+        "config": dict(WORKLOAD, parallelism=f"replicas{world}", intersect_mode="exact", bvh_builder=args.builder,
                        l2="flushed between steps (256 MiB write)", counted_rays_per_step=counted // args.steps),
         "e2e": {"value": round(e2e_value, 2), "unit": METRIC, "h2d_bytes_per_step": int(desc_bytes),
                 "d2h_bytes_per_step": int(film_bytes),
@@ -587,6 +587,8 @@ def main() -> None:
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="sphere_field")
+    ap.add_argument("--builder", choices=["host", "gpu"], default="host",
+                    help="BVH builder: binned SAH on the host, or the linear BVH built on the GPU")
     a = ap.parse_args()
     WORKLOAD.clear()
     WORKLOAD.update(WORKLOADS[a.workload])

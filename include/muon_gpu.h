@@ -88,6 +88,13 @@ extern "C" {
 #define MUON_ISECT_WATERTIGHT 1
 #define MUON_ISECT_EXACT 2
 
+/* BVH builders (MuonSceneDesc.builder). HOST_SAH: binned SAH on the host
+ * threads (acceleration and partition_strategy apply). GPU_LBVH: linear BVH
+ * over Morton-sorted centroids on the device (Karras 2012), leaves of at most
+ * 4 primitives; much faster to build, somewhat slower to traverse. */
+#define MUON_BUILDER_HOST_SAH 0
+#define MUON_BUILDER_GPU_LBVH 1
+
 /* render flags */
 #define MUON_RENDER_STATS 1u      /* count bounds/object tests (slower)        */
 #define MUON_RENDER_ACCUMULATE 2u /* add into the caller's film, do not zero   */
@@ -165,7 +172,7 @@ typedef struct MuonSceneDesc {
   int32_t acceleration;       /* MUON_ACCEL_*                       */
   int32_t partition_strategy; /* MUON_PARTITION_*                   */
   int32_t max_leaf_size;      /* 0 = default (4)                    */
-  int32_t pad;
+  int32_t builder;            /* MUON_BUILDER_*                     */
 } MuonSceneDesc;
 
 /* Render settings: the integrator properties of muon::Scene

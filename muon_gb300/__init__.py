@@ -121,12 +121,13 @@ class Scene:
     """A scene resident on the GPU (Structure::Init + upload)."""
 
     def __init__(self, parsed: ParsedScene, acceleration: str = "bvh", partition_strategy: str = "sah",
-                 max_leaf_size: int = 0):
+                 max_leaf_size: int = 0, builder: str = "host"):
         self.parsed = parsed
         desc = parsed.desc
         desc.acceleration = native.ACCEL_LINEAR if acceleration == "linear" else native.ACCEL_BVH
         desc.partition_strategy = native.PARTITION[partition_strategy]
         desc.max_leaf_size = max_leaf_size
+        desc.builder = 1 if builder == "gpu" else 0
         h = C.c_void_p()
         check(load().muon_gpu_scene_create(C.byref(desc), C.byref(h)))
         self._h = h

@@ -15,6 +15,7 @@
 #include <string>
 #include <vector>
 
+#include "bvh_build.h"
 #include "guide.h"
 #include "host_cuda.h"
 #include "host_scene.h"
@@ -186,6 +187,88 @@ void ComputeCamera(const MuonCameraDesc &c, DevCamera *out) {
   out->tan_fov_y = tan_y;
   out->width = c.width;
   out->height = c.height;
+}
+
+// Builds the BVH of a scene whose records BuildSceneImage left in input
+// order (defer_bvh): linear BVH on the device, records gathered into leaf
+// order in the scene's buffers, and the result copied back into the host
+// image so that host-side users (batch merge, scene box) see the same data.
+void BuildBvhOnGpu(MuonScene *sc, cudaStream_t st) {
+  SceneImage &im = sc->img;
+  const int n = static_cast<int>(im.prims.size());
+  const int nn = std::max(n - 1, 1);
+  DeviceBuffer boxes, in_prims, in_obj, in_shade, in_sn, in_sno, scratch, order, last;
+  Upload(boxes, im.boxes, st);
+  Upload(in_prims, im.prims, st);
+  Upload(in_obj, im.prims_obj, st);
+  Upload(in_shade, im.shade, st);
+  if (im.any_smooth) {
+    Upload(in_sn, im.smooth_normals, st);
+    Upload(in_sno, im.smooth_normals_obj, st);
+  }
+  const size_t sbytes = GpuLbvhScratchBytes(n);
+  scratch.Ensure(sbytes);
+  order.Ensure(sizeof(int32_t) * n);
+  last.Ensure(static_cast<size_t>(n));
+  sc->nodes.Ensure(sizeof(BvhNode) * nn);
+  sc->prims.Ensure(sizeof(PrimRecord) * n);
+  sc->prims_obj.Ensure(sizeof(PrimRecord) * n);
+  sc->shade.Ensure(sizeof(ShadeRecord) * n);
+  sc->smooth.Ensure(im.any_smooth ? sizeof(F4) * 3 * n : 16);
+  sc->smooth_obj.Ensure(im.any_smooth ? sizeof(F4) * 3 * n : 16);
+  LaunchGpuLbvh(boxes.as<float>(), n, scratch.ptr, sbytes, sc->nodes.as<BvhNode>(), order.as<int32_t>(),
+                last.as<uint8_t>(), st);
+  LaunchGatherPrims(order.as<int32_t>(), last.as<uint8_t>(), n, in_prims.as<PrimRecord>(), in_obj.as<PrimRecord>(),
+                    in_shade.as<ShadeRecord>(), im.any_smooth ? in_sn.as<F4>() : nullptr,
+                    im.any_smooth ? in_sno.as<F4>() : nullptr, sc->prims.as<PrimRecord>(),
+                    sc->prims_obj.as<PrimRecord>(), sc->shade.as<ShadeRecord>(),
+                    im.any_smooth ? sc->smooth.as<F4>() : nullptr, im.any_smooth ? sc->smooth_obj.as<F4>() : nullptr,
+                    st);
+  CUDA_TRY(cudaGetLastError());
+  im.nodes.resize(nn);
+  std::vector<int32_t> h_order(n);
+  CUDA_TRY(cudaMemcpyAsync(im.nodes.data(), sc->nodes.ptr, sizeof(BvhNode) * nn, cudaMemcpyDeviceToHost, st));
+  CUDA_TRY(cudaMemcpyAsync(im.prims.data(), sc->prims.ptr, sizeof(PrimRecord) * n, cudaMemcpyDeviceToHost, st));
+  CUDA_TRY(cudaMemcpyAsync(im.prims_obj.data(), sc->prims_obj.ptr, sizeof(PrimRecord) * n, cudaMemcpyDeviceToHost,
+                           st));
+  CUDA_TRY(cudaMemcpyAsync(im.shade.data(), sc->shade.ptr, sizeof(ShadeRecord) * n, cudaMemcpyDeviceToHost, st));
+  if (im.any_smooth) {
+    CUDA_TRY(cudaMemcpyAsync(im.smooth_normals.data(), sc->smooth.ptr, sizeof(F4) * 3 * n, cudaMemcpyDeviceToHost,
+                             st));
+    CUDA_TRY(cudaMemcpyAsync(im.smooth_normals_obj.data(), sc->smooth_obj.ptr, sizeof(F4) * 3 * n,
+                             cudaMemcpyDeviceToHost, st));
+  }
+  CUDA_TRY(cudaMemcpyAsync(h_order.data(), order.ptr, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, st));
+  CUDA_TRY(cudaStreamSynchronize(st));
+  im.boxes.clear();
+  im.boxes.shrink_to_fit();
+  for (int slot = 0; slot < n; ++slot) im.leaf_of_prim_id[im.shade[slot].s1.y] = slot;
+  // statistics: depth (iterative walk from the root) and leaves
+  BvhBuildStats &bs = im.bvh;
+  bs = BvhBuildStats();
+  bs.nodes = nn;
+  std::vector<std::pair<int32_t, int32_t>> stack{{0, 1}};
+  while (!stack.empty()) {
+    auto [node, depth] = stack.back();
+    stack.pop_back();
+    bs.max_depth = std::max(bs.max_depth, depth);
+    const int32_t links[2] = {im.nodes[node].d.x, im.nodes[node].d.y};
+    for (int32_t l : links) {
+      if (l >= 0) {
+        if (l < nn && depth < 1000) stack.push_back({l, depth + 1});
+      } else if (l != kEmptyLink) {
+        ++bs.leaves;
+        int count = 0;
+        for (int i = ~l; i < n; ++i) {
+          ++count;
+          uint32_t flags;
+          std::memcpy(&flags, &im.prims[i].p3.w, 4);
+          if (flags & kPrimLast) break;
+        }
+        bs.max_leaf = std::max(bs.max_leaf, count);
+      }
+    }
+  }
 }
 
 // ShadeParams of a render (PathTracer settings and the shadow-slot layout of
@@ -525,7 +608,10 @@ int muon_gpu_scene_create(const MuonSceneDesc *desc, MuonScene **out) {
   try {
     sc.reset(new MuonScene());
     std::string err;
-    if (!BuildSceneImage(*desc, &sc->img, &err)) return Fail(MUON_ERR_INVALID_ARG, err);
+    if (desc->builder != MUON_BUILDER_HOST_SAH && desc->builder != MUON_BUILDER_GPU_LBVH)
+      return Fail(MUON_ERR_INVALID_ARG, "unknown BVH builder");
+    const bool gpu_bvh = desc->builder == MUON_BUILDER_GPU_LBVH && desc->acceleration == MUON_ACCEL_BVH;
+    if (!BuildSceneImage(*desc, &sc->img, &err, gpu_bvh)) return Fail(MUON_ERR_INVALID_ARG, err);
     if (sc->img.bvh.max_depth >= 60) return Fail(MUON_ERR_INVALID_ARG, "BVH too deep for the traversal stack");
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return Fail(MUON_ERR_CUDA, "no CUDA device available");
@@ -537,12 +623,17 @@ int muon_gpu_scene_create(const MuonSceneDesc *desc, MuonScene **out) {
     CUDA_TRY(cudaStreamCreateWithFlags(&sc->stream, cudaStreamNonBlocking));
     cudaStream_t st = sc->stream;
     const SceneImage &im = sc->img;
-    Upload(sc->nodes, im.nodes, st);
-    Upload(sc->prims, im.prims, st);
-    Upload(sc->prims_obj, im.prims_obj, st);
-    Upload(sc->shade, im.shade, st);
-    Upload(sc->smooth, im.smooth_normals, st);
-    Upload(sc->smooth_obj, im.smooth_normals_obj, st);
+    if (gpu_bvh && !im.prims.empty()) {
+      BuildBvhOnGpu(sc.get(), st);
+      if (sc->img.bvh.max_depth >= 60) return Fail(MUON_ERR_INVALID_ARG, "BVH too deep for the traversal stack");
+    } else {
+      Upload(sc->nodes, im.nodes, st);
+      Upload(sc->prims, im.prims, st);
+      Upload(sc->prims_obj, im.prims_obj, st);
+      Upload(sc->shade, im.shade, st);
+      Upload(sc->smooth, im.smooth_normals, st);
+      Upload(sc->smooth_obj, im.smooth_normals_obj, st);
+    }
     Upload(sc->transforms, im.transforms, st);
     Upload(sc->materials, im.materials, st);
     Upload(sc->lights, im.lights, st);

@@ -401,7 +401,7 @@ float Reflectiveness(const MuonMaterialDesc &m) {
 
 }  // namespace
 
-bool BuildSceneImage(const MuonSceneDesc &desc, SceneImage *img, std::string *error) {
+bool BuildSceneImage(const MuonSceneDesc &desc, SceneImage *img, std::string *error, bool defer_bvh) {
   if (desc.num_triangles < 0 || desc.num_spheres < 0 || desc.num_materials < 0 ||
       desc.num_lights < 0 || desc.num_transforms < 0) {
     *error = "negative array size in scene description";
@@ -617,7 +617,17 @@ bool BuildSceneImage(const MuonSceneDesc &desc, SceneImage *img, std::string *er
   std::vector<int32_t> order;
   std::vector<uint8_t> last;
   int max_leaf = desc.max_leaf_size > 0 ? desc.max_leaf_size : 4;
-  BuildBvh(boxes, desc.acceleration, desc.partition_strategy, max_leaf, &img->nodes, &order, &last, &img->bvh);
+  if (defer_bvh) {
+    order.resize(boxes.size());
+    for (size_t i = 0; i < order.size(); ++i) order[i] = static_cast<int32_t>(i);
+    last.assign(boxes.size(), 1);
+    img->nodes.clear();
+    img->boxes.resize(6 * boxes.size());
+    for (size_t i = 0; i < boxes.size(); ++i)
+      for (int k = 0; k < 3; ++k) img->boxes[6 * i + k] = boxes[i].lo[k], img->boxes[6 * i + 3 + k] = boxes[i].hi[k];
+  } else {
+    BuildBvh(boxes, desc.acceleration, desc.partition_strategy, max_leaf, &img->nodes, &order, &last, &img->bvh);
+  }
   img->prims.resize(order.size());
   img->prims_obj.resize(order.size());
   img->shade.resize(order.size());

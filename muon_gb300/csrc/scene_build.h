@@ -47,12 +47,15 @@ struct SceneImage {
   std::vector<int32_t> leaf_of_prim_id;   // parse-order id -> leaf slot (-1 = never hit)
   int64_t num_prims = 0;                  // primitives in the scene, including never-hit ones
   bool any_smooth = false;
+  std::vector<float> boxes;               // 6 per record, when the GPU builds the BVH
   MuonCameraDesc camera{};
   int32_t width = 0, height = 0;
   BvhBuildStats bvh;
 };
 
 // Flattens a scene description. Returns false with a message on invalid input.
-bool BuildSceneImage(const MuonSceneDesc &desc, SceneImage *img, std::string *error);
+// With defer_bvh the BVH is left to the GPU builder: `nodes` stays empty, the
+// records are in input order and `boxes` holds their world bounds.
+bool BuildSceneImage(const MuonSceneDesc &desc, SceneImage *img, std::string *error, bool defer_bvh = false);
 
 }  // namespace muon_gpu

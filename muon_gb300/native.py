@@ -65,7 +65,7 @@ class SceneDesc(C.Structure):
                 ("triangles", C.POINTER(TriangleDesc)), ("num_triangles", C.c_int64),
                 ("spheres", C.POINTER(SphereDesc)), ("num_spheres", C.c_int64),
                 ("acceleration", C.c_int32), ("partition_strategy", C.c_int32), ("max_leaf_size", C.c_int32),
-                ("pad", C.c_int32)]
+                ("builder", C.c_int32)]
 
 
 class RenderParams(C.Structure):

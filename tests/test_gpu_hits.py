@@ -137,3 +137,43 @@ def test_scene_whose_bvh_root_is_a_leaf(lib, name):
     assert np.array_equal(pid >= 0, id_ref >= 0)
     hit = id_ref >= 0
     assert np.array_equal(dist[hit], d_ref[hit].astype(np.float32))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", SCENES)
+def test_gpu_built_bvh_gives_the_same_hits(lib, name):
+    """The device-built linear BVH (MUON_BUILDER_GPU_LBVH) holds every
+    primitive exactly once: closest hits equal the reference's as with the
+    host-built tree (ties aside), and any-hit queries agree with them."""
+    fx = load(name)
+    scene = m.Scene.from_string(str(fx["scene"]), builder="gpu")
+    rays = fx["rays"]
+    dist, pid, pos, nrm = scene.intersect(rays[:, :3], rays[:, 3:], native.ISECT_EXACT)
+    rid = ref_ids(fx)
+    agree = pid == rid
+    tie = ~agree & (pid >= 0) & (rid >= 0) & (dist == fx["distance"])
+    assert not (~agree & ~tie).any()
+    both = agree & (rid >= 0)
+    assert np.array_equal(dist[both], fx["distance"][both])
+    assert np.array_equal(nrm[both], fx["normal"][both])
+    hit = pid >= 0
+    far = np.where(hit, dist * 1.001, np.float32(1e30)).astype(np.float32)
+    assert np.array_equal(scene.occluded(rays[:, :3], rays[:, 3:], far), hit)
+    st_scene = m.Scene.from_string(str(fx["scene"]))
+    a = scene.render(integrator="depth", pixel_samples=1)
+    b = st_scene.render(integrator="depth", pixel_samples=1)
+    same = agree | tie
+    assert np.array_equal(a.sum.reshape(-1, 3)[same], b.sum.reshape(-1, 3)[same])
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", sorted(TINY))
+def test_gpu_built_bvh_of_a_tiny_scene(lib, name):
+    text = TINY[name]
+    from oracle import port
+
+    rays = port.camera_rays(text)
+    scene = m.Scene.from_string(text, builder="gpu")
+    _, pid, _, _ = scene.intersect(rays[:, :3], rays[:, 3:], native.ISECT_EXACT)
+    _, id_ref, _, _ = port.intersect(text, rays, precision=32, linear=True)
+    assert np.array_equal(pid >= 0, id_ref >= 0)

@@ -278,7 +278,14 @@ __global__ void __launch_bounds__(kBlock) CameraBatchKernel(const BatchScene *sc
 // than kRefillThreshold lanes of its warp are still traversing, so warps stay
 // full while the work per ray varies (dynamic fetch, after Aila and Laine,
 // "Understanding the Efficiency of Ray Traversal on GPUs", HPG 2009).
-constexpr int kRefillThreshold = 20;
+#ifndef MUON_REFILL_THRESHOLD
+#define MUON_REFILL_THRESHOLD 20
+#endif
+constexpr int kRefillThreshold = MUON_REFILL_THRESHOLD;
+// Minimum resident blocks per SM the traversal kernels are compiled for.
+#ifndef MUON_TRAVERSAL_MIN_BLOCKS
+#define MUON_TRAVERSAL_MIN_BLOCKS 1
+#endif
 
 template <bool kAnyHit, bool kStats, int kMode, class Load, class Finish>
 __device__ __forceinline__ void PersistentTraverse(const DevScene &s, int n, uint32_t *fetch, Load load,
@@ -319,7 +326,7 @@ __device__ __forceinline__ void PersistentTraverse(const DevScene &s, int n, uin
 }
 
 template <bool kStats, int kTri>
-__global__ void __launch_bounds__(kBlock) ExtendKernel(DevScene s, PathBuffers b, WaveCounters wc, int bounce) {
+__global__ void __launch_bounds__(kBlock, MUON_TRAVERSAL_MIN_BLOCKS) ExtendKernel(DevScene s, PathBuffers b, WaveCounters wc, int bounce) {
   const int n = static_cast<int>(*wc.count(bounce));
   const float4 *__restrict__ ray_o = Pick(b.ray_o, bounce & 1);
   const float4 *__restrict__ ray_d = Pick(b.ray_d, bounce & 1);
@@ -366,7 +373,7 @@ __global__ void __launch_bounds__(kBlock) ExtendKernel(DevScene s, PathBuffers b
 // Shadow queue entries are slot indices (entry * S + slot). A blocked slot's
 // contribution is zeroed.
 template <bool kStats, int kTri>
-__global__ void __launch_bounds__(kBlock) OccludeKernel(DevScene s, PathBuffers b, WaveCounters wc, int bounce,
+__global__ void __launch_bounds__(kBlock, MUON_TRAVERSAL_MIN_BLOCKS) OccludeKernel(DevScene s, PathBuffers b, WaveCounters wc, int bounce,
                                                         int slots) {
   const int n = static_cast<int>(*wc.shadow(bounce));
   TraceCounters c;

@@ -60,6 +60,17 @@ PT_SCENES = {
     "cornell_nee_on": (lambda: scenes.cornell(32, 32, 64, 5, 1, "pathtracer", "on"), 32, 1024),
     "cornell_nee_off": (lambda: scenes.cornell(32, 32, 64, 5, 1, "pathtracer", "off"), 32, 1024),
     "dense_mesh": (lambda: scenes.dense_mesh(32, 32, 64, 10, level=3, clutter=200), 32, 512),
+    # sampler and estimator options (muon/integration.cc:247-249, 313-321, 393-394, 503-562)
+    "cornell_is_hemisphere": (lambda: scenes.cornell(32, 32, 64, 5, 1, "pathtracer").replace(
+        "importance_sampling brdf", "importance_sampling hemisphere"), 32, 1024),
+    "feature_mix_is_cosine": (lambda: scenes.feature_mix(32, 32, 64, "pathtracer", "mis", 5).replace(
+        "importance_sampling brdf", "importance_sampling cosine"), 32, 1024),
+    "cornell_rr_unbounded": (lambda: scenes.cornell(32, 32, 64, 5, 1, "pathtracer").replace(
+        "russian_roulette off", "russian_roulette on").replace("max_depth 5", "max_depth -1"), 32, 1024),
+    "cornell_stratified": (lambda: scenes.cornell(32, 32, 64, 5, 1, "pathtracer").replace(
+        "russian_roulette off", "russian_roulette off\nlight_samples 4\nlight_stratify on"), 32, 512),
+    "feature_mix_min_depth": (lambda: scenes.feature_mix(32, 32, 64, "pathtracer", "mis", 5).replace(
+        "max_depth 5", "max_depth 5\nmin_depth 2"), 32, 1024),
 }
 
 

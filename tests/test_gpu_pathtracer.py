@@ -20,7 +20,11 @@ import muon_gb300 as m
 from conftest import GOLDEN
 from muon_gb300 import native
 
-CASES = ["cornell", "cornell_nee_on", "cornell_nee_off", "feature_mix", "sphere_field", "dense_mesh"]
+CASES = ["cornell", "cornell_nee_on", "cornell_nee_off", "feature_mix", "sphere_field", "dense_mesh",
+         # sampler / estimator options: hemisphere and cosine sampling, Russian
+         # roulette with unbounded depth, stratified light samples, min_depth
+         "cornell_is_hemisphere", "feature_mix_is_cosine", "cornell_rr_unbounded", "cornell_stratified",
+         "feature_mix_min_depth"]
 GPU_SPP = 8192
 
 

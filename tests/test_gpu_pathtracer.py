@@ -1,12 +1,21 @@
 """Statistical parity of the GPU path tracer with the reference.
 
-The fixtures hold FP64 films of 16 independent single-thread renders by the
-reference's own code (distinct seeds, 64 spp each; make_fixtures.py). The GPU
+The fixtures hold FP64 films of 32 single-thread renders by the reference's
+own code (distinct seeds, 512 or 1024 spp each; make_fixtures.py). The GPU
 renders the same scene text with its own counter-based RNG, so agreement is
 statistical: per pixel, z = (mean_gpu - mean_ref) / sqrt(se_gpu^2 + se_ref^2)
 with standard errors from the sample variances. Under the null hypothesis
-|z| > 4 is rare; the test allows 0.5% of pixels beyond it (heavy-tailed
-light paths) and requires the image means to agree within 4 standard errors.
+|z| > 4 is rare; the test allows 1% of pixels beyond it (heavy-tailed light
+paths) and requires the image means to agree within 4 standard errors.
+
+The reference's runs are not independent everywhere: its first tile (the top
+rows of the film) gets no seed of its own (muon/sampling.cc:41-46), so every
+run jitters those pixels with the same sub-pixel positions and only the path
+randomness differs between runs. Where pixel coverage dominates the variance
+(the light's edges) the runs then agree with each other far better than their
+sample variance says, and the pooled mean is only as good as one run's
+positions. The reference's standard error in those rows is therefore taken
+from one run's sample count (spp), not from runs x spp.
 The reference divides 0 by 0 when a GGX lobe sampled with probability one is
 evaluated from inside a sphere (a zero density, muon/integration.cc:557 with
 muon/materials.cc:219-227); the GPU counts such a zero-density sample as
@@ -28,6 +37,14 @@ CASES = ["cornell", "cornell_nee_on", "cornell_nee_off", "feature_mix", "sphere_
 GPU_SPP = 8192
 
 
+def first_tile_rows(width, height, spp):
+    """Height of the reference's first tile for a one-thread render
+    (muon/sampling.cc:9-26 NumTiles, :28-46 TileImage)."""
+    num = min(max(width * height * spp // (500 * 50 * 2), 3), height)
+    th = height // num
+    return th + (height - th * num)
+
+
 def reference_stats(fx):
     sums, sqs = fx["sums"], fx["sum_sq"]
     spp = int(fx["spp"])
@@ -38,7 +55,11 @@ def reference_stats(fx):
     n = (runs * spp)[..., None].astype(np.float64)
     mean = s / np.maximum(n, 1)
     var = np.maximum(q / np.maximum(n, 1) - mean * mean, 0) * n / np.maximum(n - 1, 1)
-    return mean, var / np.maximum(n, 1), runs
+    # the first tile's rows share their sub-pixel positions across runs
+    n_eff = n.copy()
+    rows = first_tile_rows(sums.shape[2], sums.shape[1], spp)
+    n_eff[:rows] = np.minimum(n[:rows], spp)
+    return mean, var / np.maximum(n_eff, 1), runs
 
 
 @pytest.mark.gpu
@@ -56,7 +77,7 @@ def test_path_tracer_converges_to_reference(lib, name, mode):
     z = np.where(denom > 0, (mean_g - mean_r) / np.where(denom > 0, denom, 1), 0.0)[ok]
     frac = (np.abs(z) > 4).mean()
     img_g, img_r = mean_g[ok].mean(), mean_r[ok].mean()
-    se_img = np.sqrt(se2_g[ok].sum() + se2_r[ok].sum()) / ok.sum()
+    se_img = np.sqrt(se2_g[ok].sum() + se2_r[ok].sum()) / se2_g[ok].size
     rmse = np.sqrt(((mean_g - mean_r)[ok] ** 2).mean())
     print(f"{name} mode {mode}: |z|>4 on {frac * 100:.3f}% of pixels, image mean gpu {img_g:.5f} ref {img_r:.5f} "
           f"({(img_g - img_r) / se_img:+.2f} se), rmse {rmse:.5f}")

@@ -6,7 +6,7 @@
 // gradient per sample, the backward pass layer by layer, and weight gradients
 // as per-chunk partial sums reduced in a fixed order, so a step's gradients do
 // not depend on scheduling. Adam then updates the FP32 master weights, which
-// are repacked as the BF16 tensor-core operand layout for inference.
+// are repacked as the BF16 tensor-core operand image for inference.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -16,6 +16,7 @@
 #include "dev_common.cuh"
 #include "guide.h"
 #include "guide_mlp.cuh"
+#include "guide_tc.cuh"
 
 namespace muon_gpu {
 
@@ -27,21 +28,36 @@ constexpr int kThreads = 256;
 constexpr int kChunk = 2048;  // samples per weight-gradient partial
 
 // ---- packing and initialisation ------------------------------------------------
-__global__ void PackKernel(const float *params, __nv_bfloat16 *wt, float *bias) {
+// The inference image (guide_mlp.cuh): one thread per 16-byte chunk of a
+// layer's operand (8 BF16 weights of one output along K) or per bias.
+constexpr int kImgChunks = kImgBiasOffset / 16;
+
+__global__ void PackKernel(const float *params, unsigned char *img) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < kWtElems) {
+  if (i < kImgChunks) {
+    const int byte = 16 * i;
     int l = 0;
-    while (l + 1 < kLayers && i >= WtOffset(l + 1)) ++l;
-    const int local = i - WtOffset(l);
-    const int o = local / Stride(l), k = local % Stride(l);
-    float v = 0.0f;
-    if (k < In(l)) v = params[MasterOffset(l) + k * Out(l) + o];
-    wt[i] = __float2bfloat16_rn(v);
+    while (l + 1 < kLayers && byte >= ImgOffset(l + 1)) ++l;
+    const int K = In(l);
+    const int local = byte - ImgOffset(l);
+    const int rb = local / ((K / 8) * 128), rem = local % ((K / 8) * 128);
+    const int kb = rem / 128, r = rb * 8 + (rem % 128) / 16;
+    uint32_t w[4];
+    for (int e = 0; e < 4; ++e) {
+      const int k = 8 * kb + 2 * e;
+      float lo = 0.0f, hi = 0.0f;
+      if (r < Out(l)) {
+        lo = params[MasterOffset(l) + k * Out(l) + r];
+        hi = params[MasterOffset(l) + (k + 1) * Out(l) + r];
+      }
+      w[e] = PackBf16(lo, hi);
+    }
+    *reinterpret_cast<uint4 *>(img + byte) = make_uint4(w[0], w[1], w[2], w[3]);
   }
   if (i < kBiasFloats) {
     const int l = i < 4 * kWidth ? i / kWidth : kLayers - 1;
     const int o = i - BiasOffset(l);
-    bias[i] = params[MasterOffset(l) + In(l) * Out(l) + o];
+    reinterpret_cast<float *>(img + kImgBiasOffset)[i] = params[MasterOffset(l) + In(l) * Out(l) + o];
   }
 }
 
@@ -63,27 +79,27 @@ __global__ void InitKernel(float *params, uint64_t seed) {
 }
 
 // ---- tensor-core forward for given features ------------------------------------
-__global__ void __launch_bounds__(128) ForwardKernel(const __nv_bfloat16 *wt, const float *bias,
-                                                     const float *features, int n, float *out) {
-  extern __shared__ __align__(16) unsigned char smem[];
-  LoadNetwork(wt, bias, smem);
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  float *sfeat = reinterpret_cast<float *>(smem + kSmemBytes) + warp * (32 * kFeatures + 32 * kOut);
-  float *sout = sfeat + 32 * kFeatures;
-  __syncthreads();
-  const int base = (blockIdx.x * 4 + warp) * 32;
-  if (base >= n) return;  // whole warp leaves together
-  for (int d = 0; d < kFeatures; ++d) {
-    const int r = base + lane;
-    sfeat[lane * kFeatures + d] = r < n ? features[static_cast<int64_t>(r) * kFeatures + d] : 0.0f;
+// The inference kernel's network pass (guide_tc.cuh) over features read from
+// memory: one CTA per SM, 128 rows per group.
+__global__ void __launch_bounds__(kTcThreads, 1) ForwardKernel(const void *img, const float *features, int n,
+                                                               float *out, int32_t *status) {
+  extern __shared__ __align__(1024) unsigned char smem[];
+  if (static_cast<int>(blockIdx.x) * kTcThreads >= n) return;  // the whole CTA
+  TcGroup grp;
+  bool ok = TcBegin(smem, img, &grp);
+  const int group = threadIdx.x / kTcRows;
+  for (int base = (blockIdx.x * 2 + group) * kTcRows; ok && base < n; base += gridDim.x * kTcThreads) {
+    const int r = base + grp.row;
+    float f[kFeatures];
+#pragma unroll
+    for (int d = 0; d < kFeatures; ++d) f[d] = r < n ? features[static_cast<int64_t>(r) * kFeatures + d] : 0.0f;
+    float o[kOut];
+    ok = TcForward(grp, f, o);
+    if (ok && r < n)
+#pragma unroll
+      for (int c = 0; c < kOut; ++c) out[static_cast<int64_t>(r) * kOut + c] = o[c];
   }
-  __syncwarp();
-  ForwardWarp(smem, [&](int r, int d) { return sfeat[r * kFeatures + d]; }, sout);
-  __syncwarp();
-  for (int k = lane; k < 32 * kOut; k += 32) {
-    const int r = base + k / kOut;
-    if (r < n) out[static_cast<int64_t>(r) * kOut + k % kOut] = sout[k];
-  }
+  TcEnd(smem, grp, status);
 }
 
 // ---- training: forward ----------------------------------------------------------
@@ -355,21 +371,24 @@ inline unsigned Grid(int64_t n, int block) { return static_cast<unsigned>((n + b
 
 }  // namespace
 
-void LaunchGuidePack(const float *params, void *wt, float *bias, cudaStream_t st) {
-  PackKernel<<<Grid(std::max(kWtElems, kBiasFloats), 256), 256, 0, st>>>(params, static_cast<__nv_bfloat16 *>(wt),
-                                                                        bias);
+void LaunchGuidePack(const float *params, void *img, cudaStream_t st) {
+  PackKernel<<<Grid(std::max(kImgChunks, kBiasFloats), 256), 256, 0, st>>>(params, static_cast<unsigned char *>(img));
 }
 
 void LaunchGuideInit(float *params, uint64_t seed, cudaStream_t st) {
   InitKernel<<<Grid(kParams, 256), 256, 0, st>>>(params, seed);
 }
 
-void LaunchGuideForward(const void *wt, const float *bias, const float *features, int n, float *out,
+void LaunchGuideForward(const void *img, const float *features, int n, float *out, int32_t *status,
                         cudaStream_t st) {
   if (n <= 0) return;
-  const int smem = kSmemBytes + 4 * (32 * kFeatures + 32 * kOut) * 4;
-  cudaFuncSetAttribute(ForwardKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-  ForwardKernel<<<Grid(n, 128), 128, smem, st>>>(static_cast<const __nv_bfloat16 *>(wt), bias, features, n, out);
+  int dev = 0, sms = 1;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const unsigned grid = static_cast<unsigned>(std::max<int64_t>(
+      1, std::min<int64_t>((static_cast<int64_t>(n) + kTcThreads - 1) / kTcThreads, std::max(sms, 1))));
+  cudaFuncSetAttribute(ForwardKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmemBytes);
+  ForwardKernel<<<grid, kTcThreads, kTcSmemBytes, st>>>(img, features, n, out, status);
 }
 
 size_t GuideTrainBytes(int batch) {

@@ -28,8 +28,8 @@ struct GuideSample {
 
 // Device view of a guide for the render kernels.
 struct GuideDev {
-  const void *wt;        // BF16 transposed network weights (guide::WtOffset layout)
-  const float *bias;     // FP32 biases (guide::BiasOffset layout)
+  const void *wt;        // the inference image (guide_mlp.cuh): BF16 operands, then FP32 biases
+  int32_t *status;       // set to 1 by an inference kernel whose tensor-core wait gave up
   float4 *mix;           // 10 per queue entry: the processed mixture
   float4 *feat;          // 2 per queue entry: the features
   GuideRec *rec;         // rec_bounces x rec_cap
@@ -66,10 +66,12 @@ void LaunchGuideCollect(const PathBuffers &b, WaveCounters wc, int bounces, int 
 
 // Training and network kernels (guide.cu). `params` is the FP32 master copy
 // (guide::MasterOffset layout).
-void LaunchGuidePack(const float *params, void *wt, float *bias, cudaStream_t st);
+// Writes the inference image (guide_mlp.cuh) of the master copy.
+void LaunchGuidePack(const float *params, void *img, cudaStream_t st);
 void LaunchGuideInit(float *params, uint64_t seed, cudaStream_t st);
-// Network outputs (n x 40) for features (n x 8) on the tensor-core path.
-void LaunchGuideForward(const void *wt, const float *bias, const float *features, int n, float *out,
+// Network outputs (n x 40) for features (n x 8) on the tensor-core path;
+// `status` as in GuideDev.
+void LaunchGuideForward(const void *img, const float *features, int n, float *out, int32_t *status,
                         cudaStream_t st);
 
 // Working memory of one training step over `batch` samples.

@@ -21,7 +21,7 @@ struct MuonGuide {
   MuonScene *scene = nullptr;
   SceneView view{};
   MuonGuideConfig cfg{};
-  DeviceBuffer params, adam_m, adam_v, wt, bias, mix, feat, rec, pool, pool_count, train, batch_feat, batch_dir,
+  DeviceBuffer params, adam_m, adam_v, wt, status, mix, feat, rec, pool, pool_count, train, batch_feat, batch_dir,
       batch_w, io_in, io_dir, io_w, io_out;
   GuideDev dev{};
   int step = 0;
@@ -54,6 +54,15 @@ void SceneBox(const SceneImage &im, float lo[3], float hi[3]) {
   }
 }
 
+// The status word of the tensor-core inference kernels (see GuideDev::status).
+int CheckInferenceStatus(const MuonGuide *g) {
+  int32_t v = 0;
+  CUDA_TRY(cudaMemcpyAsync(&v, g->status.ptr, sizeof(v), cudaMemcpyDeviceToHost, g->view.stream));
+  CUDA_TRY(cudaStreamSynchronize(g->view.stream));
+  if (v != 0) return Fail(MUON_ERR_CUDA, "guide inference: a tensor-core wait timed out");
+  return MUON_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -74,8 +83,8 @@ int muon_gpu_guide_create(MuonScene *scene, const MuonGuideConfig *config, MuonG
     g->params.Ensure(sizeof(float) * guide::kParams);
     g->adam_m.Ensure(sizeof(float) * guide::kParams);
     g->adam_v.Ensure(sizeof(float) * guide::kParams);
-    g->wt.Ensure(2 * guide::kWtElems);
-    g->bias.Ensure(sizeof(float) * guide::kBiasFloats);
+    g->wt.Ensure(guide::kImgBytes);
+    g->status.Ensure(sizeof(int32_t));
     const size_t cap = static_cast<size_t>(c.wave_paths);
     g->mix.Ensure(cap * 10 * sizeof(float4));
     g->feat.Ensure(cap * 2 * sizeof(float4));
@@ -89,13 +98,14 @@ int muon_gpu_guide_create(MuonScene *scene, const MuonGuideConfig *config, MuonG
     CUDA_TRY(cudaMemsetAsync(g->adam_m.ptr, 0, sizeof(float) * guide::kParams, st));
     CUDA_TRY(cudaMemsetAsync(g->adam_v.ptr, 0, sizeof(float) * guide::kParams, st));
     CUDA_TRY(cudaMemsetAsync(g->pool_count.ptr, 0, sizeof(unsigned long long), st));
+    CUDA_TRY(cudaMemsetAsync(g->status.ptr, 0, sizeof(int32_t), st));
     CUDA_TRY(cudaMemsetAsync(g->rec.ptr, 0, cap * c.record_bounces * sizeof(GuideRec), st));
     LaunchGuideInit(g->params.as<float>(), c.seed, st);
-    LaunchGuidePack(g->params.as<float>(), g->wt.ptr, g->bias.as<float>(), st);
+    LaunchGuidePack(g->params.as<float>(), g->wt.ptr, st);
     CUDA_TRY(cudaGetLastError());
     GuideDev &d = g->dev;
     d.wt = g->wt.ptr;
-    d.bias = g->bias.as<float>();
+    d.status = g->status.as<int32_t>();
     d.mix = g->mix.as<float4>();
     d.feat = g->feat.as<float4>();
     d.rec = g->rec.as<GuideRec>();
@@ -142,6 +152,7 @@ int muon_gpu_guide_render_device(MuonGuide *guide, const MuonRenderParams *param
       CUDA_TRY(cudaMemsetAsync(d_count, 0, np * sizeof(uint32_t), st));
     }
     RenderGuided(guide->scene, p, d_sum, d_sum_sq, d_count, guide->dev);
+    return CheckInferenceStatus(guide);
   } catch (const CudaError &e) {
     return FailCuda(e);
   } catch (const std::bad_alloc &) {
@@ -171,7 +182,7 @@ int muon_gpu_guide_train(MuonGuide *guide, int32_t steps, double *loss) {
       LaunchGuideAdam(guide->params.as<float>(), guide->adam_m.as<float>(), guide->adam_v.as<float>(), tb.grad,
                       guide->cfg.learning_rate, ++guide->step, st);
     }
-    LaunchGuidePack(guide->params.as<float>(), guide->wt.ptr, guide->bias.as<float>(), st);
+    LaunchGuidePack(guide->params.as<float>(), guide->wt.ptr, st);
     CUDA_TRY(cudaGetLastError());
     if (loss) {
       std::vector<double> parts(batch / 256 + 1, 0.0);
@@ -200,11 +211,12 @@ int muon_gpu_guide_forward(MuonGuide *guide, const float *features, int64_t n, f
     guide->io_out.Ensure(sizeof(float) * n * guide::kOut);
     CUDA_TRY(cudaMemcpyAsync(guide->io_in.ptr, features, sizeof(float) * n * guide::kFeatures,
                              cudaMemcpyHostToDevice, st));
-    LaunchGuideForward(guide->wt.ptr, guide->bias.as<float>(), guide->io_in.as<float>(), static_cast<int>(n),
-                       guide->io_out.as<float>(), st);
+    LaunchGuideForward(guide->wt.ptr, guide->io_in.as<float>(), static_cast<int>(n), guide->io_out.as<float>(),
+                       guide->status.as<int32_t>(), st);
     CUDA_TRY(cudaGetLastError());
     CUDA_TRY(cudaMemcpyAsync(out, guide->io_out.ptr, sizeof(float) * n * guide::kOut, cudaMemcpyDeviceToHost, st));
     CUDA_TRY(cudaStreamSynchronize(st));
+    return CheckInferenceStatus(guide);
   } catch (const CudaError &e) {
     return FailCuda(e);
   }
@@ -266,7 +278,7 @@ int muon_gpu_guide_set_params(MuonGuide *guide, const float *params) {
     CUDA_TRY(cudaSetDevice(guide->view.device));
     cudaStream_t st = guide->view.stream;
     CUDA_TRY(cudaMemcpyAsync(guide->params.ptr, params, sizeof(float) * guide::kParams, cudaMemcpyHostToDevice, st));
-    LaunchGuidePack(guide->params.as<float>(), guide->wt.ptr, guide->bias.as<float>(), st);
+    LaunchGuidePack(guide->params.as<float>(), guide->wt.ptr, st);
     CUDA_TRY(cudaGetLastError());
     CUDA_TRY(cudaStreamSynchronize(st));
   } catch (const CudaError &e) {

@@ -24,6 +24,7 @@
 #include "kernels.cuh"
 #include "guide.h"
 #include "guide_mlp.cuh"
+#include "guide_tc.cuh"
 
 namespace muon_gpu {
 
@@ -1028,46 +1029,66 @@ __device__ __forceinline__ void GuideFeatures(const GuideDev &g, float3 p, float
   f[7] = fminf(fmaxf(r, 0.0f), 1.0f);
 }
 
-// For every hit of the bounce's queue: its features and the network's mixture
-// (one warp per 32 queue entries, network in shared memory).
+// For every hit of the bounce's queue: its guiding features (one thread per
+// entry at full occupancy, which hides the dependent loads of the surface).
 template <int kMode>
-__global__ void __launch_bounds__(128) GuideInferKernel(DevScene s, PathBuffers b, WaveCounters wc, int bounce,
-                                                        GuideDev g) {
-  extern __shared__ __align__(16) unsigned char smem[];
-  guide::LoadNetwork(static_cast<const __nv_bfloat16 *>(g.wt), g.bias, smem);
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  float *sfeat = reinterpret_cast<float *>(smem + guide::kSmemBytes) + warp * (32 * guide::kFeatures + 32 * guide::kOut);
-  float *sout = sfeat + 32 * guide::kFeatures;
-  __syncthreads();
+__global__ void __launch_bounds__(kBlock) GuideFeatureKernel(DevScene s, PathBuffers b, WaveCounters wc, int bounce,
+                                                            GuideDev g) {
   const int n = static_cast<int>(*wc.count(bounce));
   const int cur = bounce & 1;
-  for (int base = (blockIdx.x * 4 + warp) * 32; base < n; base += gridDim.x * 4 * 32) {
-    const int j = base + lane;
-    float f[guide::kFeatures] = {0, 0, 0, 0, 0, 0, 0, 0};
-    bool hit = false;
-    if (j < n) {
-      const int2 h = b.hits[j];
-      if (h.y >= 0) {
-        hit = true;
-        const float4 o4 = Pick(b.ray_o, cur)[j], d4 = Pick(b.ray_d, cur)[j];
-        float3 p, nrm;
-        float dist;
-        int mat, light, pid;
-        const float3 d = f3(d4.x, d4.y, d4.z);
-        Surface<kMode>(s, h.y, f3(o4.x, o4.y, o4.z), d, __int_as_float(h.x), &p, &nrm, &dist, &mat, &light, &pid);
-        GuideFeatures(g, p, nrm, d, LoadMat(s.materials, mat), f);
-        g.feat[2 * static_cast<int64_t>(j)] = make_float4(f[0], f[1], f[2], f[3]);
-        g.feat[2 * static_cast<int64_t>(j) + 1] = make_float4(f[4], f[5], f[6], f[7]);
-      }
-    }
-#pragma unroll
-    for (int d = 0; d < guide::kFeatures; ++d) sfeat[lane * guide::kFeatures + d] = f[d];
-    __syncwarp();
-    guide::ForwardWarp(smem, [&](int r, int d) { return sfeat[r * guide::kFeatures + d]; }, sout);
-    __syncwarp();
-    if (hit) guide::MakeMixture(sout + lane * guide::kOut, reinterpret_cast<float *>(g.mix + 10 * static_cast<int64_t>(j)));
-    __syncwarp();
+  for (int j = blockIdx.x * kBlock + threadIdx.x; j < n; j += gridDim.x * kBlock) {
+    const int2 h = b.hits[j];
+    if (h.y < 0) continue;
+    const float4 o4 = Pick(b.ray_o, cur)[j], d4 = Pick(b.ray_d, cur)[j];
+    float3 p, nrm;
+    float dist;
+    int mat, light, pid;
+    const float3 d = f3(d4.x, d4.y, d4.z);
+    Surface<kMode>(s, h.y, f3(o4.x, o4.y, o4.z), d, __int_as_float(h.x), &p, &nrm, &dist, &mat, &light, &pid);
+    float f[guide::kFeatures];
+    GuideFeatures(g, p, nrm, d, LoadMat(s.materials, mat), f);
+    g.feat[2 * static_cast<int64_t>(j)] = make_float4(f[0], f[1], f[2], f[3]);
+    g.feat[2 * static_cast<int64_t>(j) + 1] = make_float4(f[4], f[5], f[6], f[7]);
   }
+}
+
+// For every hit of the bounce's queue: the network's mixture for its features.
+// Tensor-core inference (guide_tc.cuh): one CTA per SM, two groups of 128
+// queue entries in flight, one thread per entry; the next tile's hits and
+// features are loaded while the current tile runs.
+__global__ void __launch_bounds__(guide::kTcThreads, 1) GuideInferKernel(PathBuffers b, WaveCounters wc, int bounce,
+                                                                         GuideDev g) {
+  extern __shared__ __align__(1024) unsigned char smem[];
+  const int n = static_cast<int>(*wc.count(bounce));
+  if (static_cast<int>(blockIdx.x) * guide::kTcThreads >= n) return;  // the whole CTA
+  guide::TcGroup grp;
+  bool ok = guide::TcBegin(smem, g.wt, &grp);
+  const int group = threadIdx.x / guide::kTcRows;
+  const int stride = gridDim.x * guide::kTcThreads;
+  auto fetch = [&](int j, bool *hit, float4 *f0, float4 *f1) {
+    *hit = j < n && b.hits[j].y >= 0;
+    *f0 = *f1 = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    if (*hit) {
+      *f0 = g.feat[2 * static_cast<int64_t>(j)];
+      *f1 = g.feat[2 * static_cast<int64_t>(j) + 1];
+    }
+  };
+  int base = (blockIdx.x * 2 + group) * guide::kTcRows;
+  bool hit;
+  float4 f0, f1;
+  fetch(base + grp.row, &hit, &f0, &f1);
+  for (; ok && base < n; base += stride) {
+    const int j = base + grp.row;
+    const float f[guide::kFeatures] = {f0.x, f0.y, f0.z, f0.w, f1.x, f1.y, f1.z, f1.w};
+    const bool cur_hit = hit;
+    fetch(j + stride, &hit, &f0, &f1);
+    float raw[guide::kOut];
+    ok = guide::TcForward(grp, f, raw);
+    if (!ok) break;
+    if (cur_hit) guide::MakeMixture(raw, guide::TcMixRow(grp));  // rows of misses stay unused
+    guide::TcStoreMix(grp, base, n, g.mix);
+  }
+  guide::TcEnd(smem, grp, g.status);
 }
 
 // After a guided wave: every recorded vertex becomes a training sample whose
@@ -1186,6 +1207,7 @@ inline unsigned Blocks(int64_t n) { return static_cast<unsigned>((n + kBlock - 1
 
 int g_persistent_blocks = 152 * 8;
 int g_traversal_blocks = 152 * 4;
+int g_sms = 152;
 
 // Grid for a device-counted launch whose queue holds at most `bound` entries.
 inline unsigned CountedBlocks(int64_t bound) {
@@ -1222,6 +1244,7 @@ void SetTraversalGrid(int sms) {
       per_sm < 1)
     per_sm = 4;
   g_traversal_blocks = std::max(1, sms * per_sm);
+  g_sms = std::max(1, sms);
 }
 
 void LaunchCamera(const DevCamera &cam, const WaveInfo &w, const PathBuffers &b, WaveCounters wc, cudaStream_t st) {
@@ -1311,13 +1334,14 @@ void LaunchFilmBatch(const BatchScene *scenes, const BatchSeg *segs, int nseg, i
 void LaunchGuideInfer(const DevScene &s, const PathBuffers &b, WaveCounters wc, int bounce, int bound, int isect,
                       const GuideDev &g, cudaStream_t st) {
   if (bound <= 0) return;
-  const int smem = guide::kSmemBytes + 4 * (32 * guide::kFeatures + 32 * guide::kOut) * 4;
-  const unsigned grid = static_cast<unsigned>(std::max<int64_t>(1, std::min<int64_t>((bound + 127) / 128, 2 * g_traversal_blocks)));
   WithMode(isect, [&](auto m) {
-    constexpr int M = decltype(m)::value;
-    cudaFuncSetAttribute(GuideInferKernel<M>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    GuideInferKernel<M><<<grid, 128, smem, st>>>(s, b, wc, bounce, g);
+    GuideFeatureKernel<decltype(m)::value><<<CountedBlocks(bound), kBlock, 0, st>>>(s, b, wc, bounce, g);
   });
+  // one CTA per SM (the shared memory of the two groups fills an SM)
+  const unsigned grid = static_cast<unsigned>(
+      std::max<int64_t>(1, std::min<int64_t>((bound + guide::kTcThreads - 1) / guide::kTcThreads, g_sms)));
+  cudaFuncSetAttribute(GuideInferKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, guide::kTcSmemBytes);
+  GuideInferKernel<<<grid, guide::kTcThreads, guide::kTcSmemBytes, st>>>(b, wc, bounce, g);
 }
 
 void LaunchShadePathGuided(const DevScene &s, const WaveInfo &w, const ShadeParams &sp, const PathBuffers &b,

@@ -451,7 +451,11 @@ void RenderDevice(MuonScene *sc, const MuonRenderParams &p, double *d_sum, doubl
         // Guiding covers the first rec_bounces vertices of a path (where the
         // network is trained); deeper vertices sample the BRDF alone.
         const bool guided = guide && k < guide->rec_bounces;
-        if (guided) timed(2, [&] { LaunchGuideInfer(sc->dev, b, wc, k, w.n, p.intersect_mode, guide_local, st); });
+        if (guided) {
+          // two kernels: the features, then the tensor-core network pass
+          timed(2, [&] { LaunchGuideInfer(sc->dev, b, wc, k, w.n, p.intersect_mode, guide_local, st); });
+          ++launches;
+        }
         if (!pt) {
           timed(2, [&] { LaunchShadeDebug(sc->dev, b, wc, p.integrator, w.n, p.intersect_mode, st); });
           break;

@@ -50,8 +50,7 @@ WORKLOADS = {
     "guiding": {"workload": "slit_room", "triangles": 1320756 + 10000 + 14, "width": 1024, "height": 1024,
                 "max_depth": 10, "nee": "mis", "importance_sampling": "brdf", "seed": 1, "target_rmse": 1e-2,
                 "reference_spp": 8192, "pass_spp": 16, "train_steps_per_pass": 8, "train_passes": 24,
-                "batch": 1 << 18,
-                "mixture_fraction": 0.5},
+                "batch": 1 << 18, "guide_targets": "direct", "mixture_fraction": 0.9},
     # 64 seeded scenes of uneven size in one batched wavefront
     "batch64": {"workload": "batch64", "scenes": 64, "triangles": "log-uniform 1k-500k per scene",
                 "resolutions": [128, 256, 512, 1024], "spp": "uniform 4-64", "max_depth": "uniform 4-10",
@@ -328,7 +327,8 @@ def run_guiding(args) -> None:
         st = scene.stats()
         return st["primary_rays"] + st["secondary_rays"]
 
-    guide = m.Guide(scene, seed=w["seed"], batch=w["batch"], mixture_fraction=w["mixture_fraction"])
+    guide = m.Guide(scene, seed=w["seed"], batch=w["batch"], mixture_fraction=w["mixture_fraction"],
+                    targets=native.GUIDE_DIRECT if w["guide_targets"] == "direct" else native.GUIDE_ALL)
 
     def guided_pass(f, spp):
         guide.render_device(scene.params(pixel_samples=w["pass_spp"], seed=12, sample_offset=spp,
@@ -589,9 +589,18 @@ def main() -> None:
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="sphere_field")
     ap.add_argument("--builder", choices=["host", "gpu"], default="host",
                     help="BVH builder: binned SAH on the host, or the linear BVH built on the GPU")
+    ap.add_argument("--guide-targets", choices=["direct", "all"], default=None,
+                    help="guiding workload: what the network learns (default: direct light)")
+    ap.add_argument("--mixture-fraction", type=float, default=None,
+                    help="guiding workload: probability that a guided ray samples the mixture")
     a = ap.parse_args()
     WORKLOAD.clear()
     WORKLOAD.update(WORKLOADS[a.workload])
+    if a.workload == "guiding":
+        if a.guide_targets:
+            WORKLOAD["guide_targets"] = a.guide_targets
+        if a.mixture_fraction is not None:
+            WORKLOAD["mixture_fraction"] = a.mixture_fraction
     if a.warmup < 3:
         a.warmup = 3
     if a.impl == "reference":

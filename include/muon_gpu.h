@@ -383,6 +383,11 @@ int muon_gpu_scene_stream(const MuonScene *scene, void **stream);
  * guide's own renders. */
 typedef struct MuonGuide MuonGuide;
 
+/* What the network learns and which rays it guides (MuonGuideConfig.targets). */
+#define MUON_GUIDE_DIRECT 0 /* where direct light arrives; guides the light-hit (MIS) ray,
+                               continuations sample the BRDF */
+#define MUON_GUIDE_ALL 1    /* all incident light; guides the MIS ray and continuations */
+
 typedef struct MuonGuideConfig {
   int32_t batch;            /* training batch (0: 2^18)                            */
   int32_t wave_paths;       /* paths per wavefront of guided renders (0: 2^22)     */
@@ -390,7 +395,11 @@ typedef struct MuonGuideConfig {
                                training samples (0: 4); deeper ones sample the BRDF */
   int32_t pool_capacity;    /* training samples kept, newest first (0: 2^22)       */
   float learning_rate;      /* Adam step size (0: 1e-3)                            */
-  float mixture_fraction;   /* probability of sampling the mixture (0: 0.5)        */
+  float mixture_fraction;   /* probability that a guided ray samples the mixture
+                               rather than the BRDF (0: 0.9 with MUON_GUIDE_DIRECT,
+                               0.5 with MUON_GUIDE_ALL)                            */
+  int32_t targets;          /* MUON_GUIDE_DIRECT or MUON_GUIDE_ALL                 */
+  int32_t reserved;         /* 0                                                   */
   uint64_t seed;            /* network initialisation and batch selection          */
 } MuonGuideConfig;
 

@@ -45,7 +45,8 @@ struct GuideDev {
   // render
   int32_t area_slots;
   int32_t mis_slot;
-  int32_t pad;
+  int32_t direct_only;   // MUON_GUIDE_DIRECT: only the light-hit (MIS) ray is guided and
+                         // only light samples train; continuations sample the BRDF
 };
 
 // A path-traced render with guiding (render.cc): the single-scene wavefront

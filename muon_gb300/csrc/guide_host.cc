@@ -37,7 +37,8 @@ void Defaults(MuonGuideConfig *c) {
   if (c->record_bounces <= 0) c->record_bounces = 4;
   if (c->pool_capacity <= 0) c->pool_capacity = 1 << 22;
   if (!(c->learning_rate > 0.0f)) c->learning_rate = 1e-3f;
-  if (!(c->mixture_fraction > 0.0f) || c->mixture_fraction > 1.0f) c->mixture_fraction = 0.5f;
+  if (!(c->mixture_fraction > 0.0f) || c->mixture_fraction > 1.0f)
+    c->mixture_fraction = c->targets == MUON_GUIDE_DIRECT ? 0.9f : 0.5f;
 }
 
 // Scene box from the BVH root's two child boxes.
@@ -76,6 +77,8 @@ int muon_gpu_guide_create(MuonScene *scene, const MuonGuideConfig *config, MuonG
     g->scene = scene;
     if (!GetSceneView(scene, &g->view)) return Fail(MUON_ERR_INVALID_ARG, "null scene");
     if (config) g->cfg = *config;
+    if (g->cfg.targets != MUON_GUIDE_DIRECT && g->cfg.targets != MUON_GUIDE_ALL)
+      return Fail(MUON_ERR_INVALID_ARG, "unknown guide targets");
     Defaults(&g->cfg);
     const MuonGuideConfig &c = g->cfg;
     CUDA_TRY(cudaSetDevice(g->view.device));
@@ -88,7 +91,8 @@ int muon_gpu_guide_create(MuonScene *scene, const MuonGuideConfig *config, MuonG
     const size_t cap = static_cast<size_t>(c.wave_paths);
     g->mix.Ensure(cap * 10 * sizeof(float4));
     g->feat.Ensure(cap * 2 * sizeof(float4));
-    g->rec.Ensure(cap * c.record_bounces * sizeof(GuideRec));
+    const bool records = c.targets == MUON_GUIDE_ALL;  // continuation records (guided continuations only)
+    if (records) g->rec.Ensure(cap * c.record_bounces * sizeof(GuideRec));
     g->pool.Ensure(static_cast<size_t>(c.pool_capacity) * sizeof(GuideSample));
     g->pool_count.Ensure(sizeof(unsigned long long));
     g->train.Ensure(GuideTrainBytes(c.batch));
@@ -99,7 +103,7 @@ int muon_gpu_guide_create(MuonScene *scene, const MuonGuideConfig *config, MuonG
     CUDA_TRY(cudaMemsetAsync(g->adam_v.ptr, 0, sizeof(float) * guide::kParams, st));
     CUDA_TRY(cudaMemsetAsync(g->pool_count.ptr, 0, sizeof(unsigned long long), st));
     CUDA_TRY(cudaMemsetAsync(g->status.ptr, 0, sizeof(int32_t), st));
-    CUDA_TRY(cudaMemsetAsync(g->rec.ptr, 0, cap * c.record_bounces * sizeof(GuideRec), st));
+    if (records) CUDA_TRY(cudaMemsetAsync(g->rec.ptr, 0, cap * c.record_bounces * sizeof(GuideRec), st));
     LaunchGuideInit(g->params.as<float>(), c.seed, st);
     LaunchGuidePack(g->params.as<float>(), g->wt.ptr, st);
     CUDA_TRY(cudaGetLastError());
@@ -108,10 +112,11 @@ int muon_gpu_guide_create(MuonScene *scene, const MuonGuideConfig *config, MuonG
     d.status = g->status.as<int32_t>();
     d.mix = g->mix.as<float4>();
     d.feat = g->feat.as<float4>();
-    d.rec = g->rec.as<GuideRec>();
+    d.rec = records ? g->rec.as<GuideRec>() : nullptr;
     d.rec_cap = c.wave_paths;
     d.rec_bounces = c.record_bounces;
     d.alpha = c.mixture_fraction;
+    d.direct_only = c.targets == MUON_GUIDE_DIRECT ? 1 : 0;
     float lo[3], hi[3];
     SceneBox(*g->view.img, lo, hi);
     for (int k = 0; k < 3; ++k) {

@@ -744,8 +744,9 @@ __device__ __forceinline__ void ShadeEntry(const DevScene &s, const WaveInfo &w,
       for (int pass = mis ? 0 : 1; pass < 2; ++pass) {
         float3 dir, ntp;
         float pdf;
-        if (!(gd ? SampleGuided(gd, mx, sp.is_mode, m, nrm, d, tp, rng, &dir, &pdf, &ntp)
-                 : SampleReflection(sp.is_mode, m, nrm, d, tp, rng, &dir, &pdf, &ntp)))
+        const bool guided = gd && (pass == 0 || !gd->direct_only);
+        if (!(guided ? SampleGuided(gd, mx, sp.is_mode, m, nrm, d, tp, rng, &dir, &pdf, &ntp)
+                     : SampleReflection(sp.is_mode, m, nrm, d, tp, rng, &dir, &pdf, &ntp)))
           continue;
         if (pass == 0) {
           ++counted;
@@ -789,7 +790,7 @@ __device__ __forceinline__ void ShadeEntry(const DevScene &s, const WaveInfo &w,
             out.cont_o = shift;
             out.cont_d = dir;
             out.cont_tp = ntp;
-            if (gd && bounce < gd->rec_bounces) {
+            if (gd && !gd->direct_only && bounce < gd->rec_bounces) {
               // training record; the fold adds the radiance after this vertex
               GuideRec &r = gd->rec[static_cast<int64_t>(bounce) * gd->rec_cap + jj];
               r.f0 = gd->feat[2 * static_cast<int64_t>(jj)];
@@ -972,7 +973,7 @@ __global__ void __launch_bounds__(kBlock) FoldKernel(PathBuffers b, WaveCounters
         }
       }
       int next = b.link[j];
-      if (kGuide && bounce < g.rec_bounces) {
+      if (kGuide && !g.direct_only && bounce < g.rec_bounces) {
         GuideRec &rc = g.rec[static_cast<int64_t>(bounce) * g.rec_cap + j];
         if (next >= 0) rc.after = r;
         else rc.tp.w = 0.0f;  // no continuation: nothing to learn from this vertex

@@ -482,7 +482,7 @@ void RenderDevice(MuonScene *sc, const MuonRenderParams &p, double *d_sum, doubl
       }
       LaunchFilm(w, b, d_sum, d_sq, d_cnt, st);
       ++launches;
-      if (guide) {
+      if (guide && !guide->direct_only) {
         LaunchGuideCollect(b, wc, std::min(bounces, guide->rec_bounces), w.n, guide_local, st);
         ++launches;
       }

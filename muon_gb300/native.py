@@ -115,7 +115,10 @@ class BatchTuning(C.Structure):
 class GuideConfig(C.Structure):
     _fields_ = [("batch", C.c_int32), ("wave_paths", C.c_int32), ("record_bounces", C.c_int32),
                 ("pool_capacity", C.c_int32), ("learning_rate", C.c_float), ("mixture_fraction", C.c_float),
-                ("seed", C.c_uint64)]
+                ("targets", C.c_int32), ("reserved", C.c_int32), ("seed", C.c_uint64)]
+
+
+GUIDE_DIRECT, GUIDE_ALL = 0, 1
 
 
 GUIDE_PARAMS = 31528

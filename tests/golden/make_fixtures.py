@@ -10,6 +10,11 @@ muon_gb300.scenes and stores small .npz files next to this script:
                    renders (distinct seeds) for statistical parity tests
   img_<name>.npz   1-spp films of the deterministic ray tracer and analytic
                    direct integrators (FP32 values) and the ray counters
+  pt65k_<name>.npz one single-thread render of 65,536 spp per path-traced
+                   scene (seed 4242): a converged reference for per-pixel
+                   z-tests, free of the correlation between runs that the
+                   reference's unseeded first tile (muon/sampling.cc:41-46)
+                   puts into pt_<name>.npz
 
 Usage: python tests/golden/make_fixtures.py [--only NAME ...]
 Requires the reference sources (to build oracle/_ref); the GPU machine only reads
@@ -131,6 +136,25 @@ def img(name: str) -> None:
     print(f"img_{name}: mean {s.mean():.5f}, counters {counters.tolist()}")
 
 
+PT65K_SPP = 65536
+
+
+def _pt65k(name: str) -> str:
+    make, _, _ = PT_SCENES[name]
+    text = make()
+    s, q, n, counters = _render((text, PT65K_SPP, 4242))
+    np.savez_compressed(os.path.join(HERE, f"pt65k_{name}.npz"), scene=np.array(text), sum=s.astype(np.float64),
+                        sum_sq=q.astype(np.float64), spp=np.int32(PT65K_SPP), counters=counters.astype(np.int64))
+    return f"pt65k_{name}: {PT65K_SPP} spp, mean {np.nanmean(s) / PT65K_SPP:.6f}"
+
+
+def pt65k(names: list[str]) -> None:
+    """One long render per scene, the scenes on parallel host threads."""
+    with ThreadPoolExecutor(max_workers=os.cpu_count() or 4) as ex:
+        for line in ex.map(_pt65k, names):
+            print(line, flush=True)
+
+
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--only", nargs="*")
@@ -145,6 +169,7 @@ def main() -> None:
     for name in IMG_SCENES:
         if not a.only or ("img_" + name) in a.only:
             img(name)
+    pt65k([name for name in PT_SCENES if not a.only or ("pt65k_" + name) in a.only])
 
 
 if __name__ == "__main__":

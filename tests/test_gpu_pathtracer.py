@@ -92,6 +92,37 @@ def test_path_tracer_converges_to_reference(lib, name, mode):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("name", CASES)
+def test_path_tracer_matches_65k_spp_reference(lib, name):
+    """Per-pixel z-test against one converged render of the reference build:
+    65,536 spp in a single run (make_fixtures.py, pt65k_<name>.npz), so every
+    pixel's standard error comes from independent samples. The GPU renders
+    the same number of samples. Pixels where the reference's 0/0 (see the
+    module docstring) made the sum non-finite are left out."""
+    fx = np.load(f"{GOLDEN}/pt65k_{name}.npz")
+    spp = int(fx["spp"])
+    scene = m.Scene.from_string(str(fx["scene"]))
+    film = scene.render(pixel_samples=spp, seed=9)
+    mean_g, se2_g = film.mean(), film.variance_of_mean()
+    s, q = fx["sum"], fx["sum_sq"]
+    ok = np.isfinite(s).all(axis=-1) & np.isfinite(q).all(axis=-1)
+    assert ok.mean() >= 0.5
+    n = float(spp)
+    mean_r = np.where(ok[..., None], s, 0.0) / n
+    var_r = np.maximum(np.where(ok[..., None], q, 0.0) / n - mean_r * mean_r, 0.0) * n / (n - 1)
+    se2_r = var_r / n
+    denom = np.sqrt(se2_g + se2_r)
+    z = np.where(denom > 0, (mean_g - mean_r) / np.where(denom > 0, denom, 1), 0.0)[ok]
+    frac = (np.abs(z) > 4).mean()
+    img_g, img_r = mean_g[ok].mean(), mean_r[ok].mean()
+    se_img = np.sqrt(se2_g[ok].sum() + se2_r[ok].sum()) / se2_g[ok].size
+    print(f"{name}: {spp} spp each, |z|>4 on {frac * 100:.3f}% of pixel channels, |z| max {np.abs(z).max():.2f}, "
+          f"image mean gpu {img_g:.6f} ref {img_r:.6f} ({(img_g - img_r) / se_img:+.2f} se)")
+    assert abs(img_g - img_r) <= 4 * se_img
+    assert frac <= 0.01
+
+
+@pytest.mark.gpu
 def test_render_is_deterministic_and_seeded(lib):
     fx = np.load(f"{GOLDEN}/pt_cornell.npz")
     scene = m.Scene.from_string(str(fx["scene"]))

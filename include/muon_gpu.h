@@ -390,7 +390,7 @@ typedef struct MuonGuide MuonGuide;
 
 typedef struct MuonGuideConfig {
   int32_t batch;            /* training batch (0: 2^18)                            */
-  int32_t wave_paths;       /* paths per wavefront of guided renders (0: 2^22)     */
+  int32_t wave_paths;       /* paths per wavefront of guided renders (0: 2^24)     */
   int32_t record_bounces;   /* first vertices of a path that are guided and kept as
                                training samples (0: 4); deeper ones sample the BRDF */
   int32_t pool_capacity;    /* training samples kept, newest first (0: 2^22)       */

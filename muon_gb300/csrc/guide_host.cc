@@ -32,7 +32,7 @@ namespace {
 
 void Defaults(MuonGuideConfig *c) {
   if (c->batch <= 0) c->batch = 1 << 18;
-  if (c->wave_paths <= 0) c->wave_paths = 1 << 22;
+  if (c->wave_paths <= 0) c->wave_paths = kMaxWavePaths;
   c->wave_paths = std::min(c->wave_paths, kMaxWavePaths);
   if (c->record_bounces <= 0) c->record_bounces = 4;
   if (c->pool_capacity <= 0) c->pool_capacity = 1 << 22;

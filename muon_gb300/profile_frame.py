@@ -29,6 +29,7 @@ def main() -> None:
     ap.add_argument("--guided", action="store_true")
     ap.add_argument("--train-steps", type=int, default=4)
     ap.add_argument("--batch", type=int, default=1 << 18)
+    ap.add_argument("--mixture-fraction", type=float, default=0.0, help="guided ray mixture fraction (0: default)")
     a = ap.parse_args()
     text = scenes.WORKLOADS[a.workload](width=a.width, height=a.height, spp=a.spp)
     scene = Scene.from_string(text)
@@ -38,7 +39,7 @@ def main() -> None:
 
         from . import Guide
 
-        guide = Guide(scene, seed=1, batch=a.batch)
+        guide = Guide(scene, seed=1, batch=a.batch, mixture_fraction=a.mixture_fraction)
         n = scene.width * scene.height
         film = [torch.zeros((n, 3), dtype=torch.float64, device="cuda"),
                 torch.zeros((n, 3), dtype=torch.float64, device="cuda"),

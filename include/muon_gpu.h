@@ -283,7 +283,12 @@ typedef struct MuonScene MuonScene;
  * Replaces Structure::AddPrimitive + Structure::Init (muon/acceleration.h:
  * 30-35). */
 int muon_gpu_scene_create(const MuonSceneDesc *desc, MuonScene **out);
+/* Frees the scene. Its large work arrays stay cached in the process for the
+ * next scene on the same device (at most 1/8 of the device's memory; no
+ * counterpart in the reference, whose scenes live in host memory). */
 void muon_gpu_scene_destroy(MuonScene *scene);
+/* Frees every cached work array on every device. */
+void muon_gpu_release_cached(void);
 
 /* Renders the whole film: replaces the per-thread sample loop of
  * Renderer::Render (muon/renderer.cc:41-76). Host film in, host film out. */

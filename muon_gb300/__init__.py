@@ -161,11 +161,23 @@ class Scene:
             setattr(p, k, v)
         return p
 
-    def render(self, params: native.RenderParams | None = None, **overrides) -> FilmResult:
-        """Renders the whole film (Renderer::Render's sample loop) on the GPU."""
+    def render(self, params: native.RenderParams | None = None, out: FilmResult | None = None,
+               **overrides) -> FilmResult:
+        """Renders the whole film (Renderer::Render's sample loop) on the GPU.
+        `out`, if given, receives the film (C-contiguous arrays of the film's
+        shape; pinned host memory makes the copies fastest)."""
         p = params if params is not None else self.params(**overrides)
         h, w = self.height, self.width
-        film = FilmResult(np.zeros((h, w, 3)), np.zeros((h, w, 3)), np.zeros((h, w), dtype=np.uint32))
+        if out is not None:
+            film = out
+            ok = (film.sum.shape == (h, w, 3) and film.sum_sq.shape == (h, w, 3) and film.count.shape == (h, w)
+                  and film.sum.dtype == np.float64 and film.sum_sq.dtype == np.float64
+                  and film.count.dtype == np.uint32
+                  and all(a.flags["C_CONTIGUOUS"] for a in (film.sum, film.sum_sq, film.count)))
+            if not ok:
+                raise ValueError("out film does not match the scene's film")
+        else:
+            film = FilmResult(np.zeros((h, w, 3)), np.zeros((h, w, 3)), np.zeros((h, w), dtype=np.uint32))
         f = film._cfilm()
         check(load().muon_gpu_render(self._h, C.byref(p), C.byref(f)))
         return film

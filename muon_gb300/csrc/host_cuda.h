@@ -64,6 +64,18 @@ struct DeviceBuffer {
   }
 };
 
+// A process-wide cache of device blocks, per device, for the large per-scene
+// work arrays: a destroyed scene gives its blocks back (PoolGive) and the next
+// scene's EnsurePooled takes one of at least the wanted size (at most 1.5x),
+// so that creating and destroying scenes does not pay cudaMalloc/cudaFree of
+// gigabytes each time. Only blocks whose last use on the device has finished
+// may be given. The cache holds at most 1/8 of the device's memory (oldest
+// blocks are freed first) and is emptied before an allocation is allowed to
+// fail; muon_gpu_release_cached() empties it on request.
+void PoolGive(DeviceBuffer &buf, int device) noexcept;
+void EnsurePooled(DeviceBuffer &buf, size_t want, int device);
+void PoolTrim(int device) noexcept;  // device < 0: every device
+
 template <typename T>
 void Upload(DeviceBuffer &buf, const std::vector<T> &v, cudaStream_t st) {
   buf.Ensure(std::max<size_t>(v.size() * sizeof(T), 16));

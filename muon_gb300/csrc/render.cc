@@ -7,6 +7,8 @@
 // wavefront is advanced one bounce at a time by whole-GPU kernels.
 #include <cuda_runtime.h>
 
+#include <mutex>
+
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -59,8 +61,24 @@ struct MuonScene {
   std::string graph_key;
   int graph_events = 0;
   uint64_t graph_launches = 0;
+  // Launch configuration of the last render launched kernel by kernel: a
+  // graph is captured when the same configuration renders again (a one-off
+  // render would pay more to instantiate a graph than the graph saves).
+  std::string seen_key;
 
   ~MuonScene() {
+    // The work arrays go to the process-wide cache once the stream is idle.
+    if (stream && cudaStreamSynchronize(stream) == cudaSuccess) {
+      for (int k = 0; k < 2; ++k) {
+        PoolGive(ray_o[k], device);
+        PoolGive(ray_d[k], device);
+        PoolGive(tp[k], device);
+        PoolGive(rad[k], device);
+      }
+      for (DeviceBuffer *b : {&hits, &link, &final_rad, &org, &contrib, &slot_dir, &shq, &order, &film_sum, &film_sq,
+                              &film_cnt})
+        PoolGive(*b, device);
+    }
     if (graph) cudaGraphExecDestroy(graph);
     for (EventPair &e : events) {
       if (e.a) cudaEventDestroy(e.a);
@@ -109,21 +127,22 @@ struct MuonScene {
     if (paths <= wave_cap && slots <= slots_cap) return false;
     int64_t p = std::max(paths, wave_cap);
     int s = std::max(slots, slots_cap);
+    // the stream is idle here (every render synchronises before returning)
     for (int k = 0; k < 2; ++k) {
-      ray_o[k].Ensure(p * sizeof(float4));
-      ray_d[k].Ensure(p * sizeof(float4));
-      tp[k].Ensure(p * sizeof(float4));
-      rad[k].Ensure(p * sizeof(float4));
+      EnsurePooled(ray_o[k], p * sizeof(float4), device);
+      EnsurePooled(ray_d[k], p * sizeof(float4), device);
+      EnsurePooled(tp[k], p * sizeof(float4), device);
+      EnsurePooled(rad[k], p * sizeof(float4), device);
     }
-    hits.Ensure(p * sizeof(int2));
-    link.Ensure(p * sizeof(int32_t));
-    final_rad.Ensure(p * sizeof(float4));
-    org.Ensure(p * sizeof(float4));
+    EnsurePooled(hits, p * sizeof(int2), device);
+    EnsurePooled(link, p * sizeof(int32_t), device);
+    EnsurePooled(final_rad, p * sizeof(float4), device);
+    EnsurePooled(org, p * sizeof(float4), device);
     size_t sl = static_cast<size_t>(p) * std::max(s, 1);
-    contrib.Ensure(sl * sizeof(float4));
-    slot_dir.Ensure(sl * sizeof(float4));
-    shq.Ensure(sl * sizeof(uint32_t));
-    order.Ensure(static_cast<size_t>(p) * kNumClasses * sizeof(int32_t));
+    EnsurePooled(contrib, sl * sizeof(float4), device);
+    EnsurePooled(slot_dir, sl * sizeof(float4), device);
+    EnsurePooled(shq, sl * sizeof(uint32_t), device);
+    EnsurePooled(order, static_cast<size_t>(p) * kNumClasses * sizeof(int32_t), device);
     wave_cap = p;
     slots_cap = s;
     return true;
@@ -421,6 +440,7 @@ void RenderDevice(MuonScene *sc, const MuonRenderParams &p, double *d_sum, doubl
   uint64_t launches = 0;
   int timed_pairs = 1;
   // Records the launch sequence of the whole frame on `st`.
+  bool capturing = false;  // event records inside a graph capture become external event nodes
   auto enqueue = [&](bool host_loop) {
     sc->events_used = 1;  // pair 0 brackets the frame
     CUDA_TRY(cudaMemsetAsync(sc->counters.ptr, 0, stride * waves.size() * sizeof(uint32_t), st));
@@ -434,9 +454,11 @@ void RenderDevice(MuonScene *sc, const MuonRenderParams &p, double *d_sum, doubl
         // External event nodes when captured, so they time the kernels
         // inside the replayed graph.
         EventPair *ev = timing ? sc->NextEvent(kind) : nullptr;
-        if (ev) CUDA_TRY(cudaEventRecordWithFlags(ev->a, st, cudaEventRecordExternal));
+        if (ev) CUDA_TRY(capturing ? cudaEventRecordWithFlags(ev->a, st, cudaEventRecordExternal)
+                                   : cudaEventRecord(ev->a, st));
         launch();
-        if (ev) CUDA_TRY(cudaEventRecordWithFlags(ev->b, st, cudaEventRecordExternal));
+        if (ev) CUDA_TRY(capturing ? cudaEventRecordWithFlags(ev->b, st, cudaEventRecordExternal)
+                                   : cudaEventRecord(ev->b, st));
         ++launches;
       };
       if (whitted && bounces > 0) {
@@ -505,14 +527,17 @@ void RenderDevice(MuonScene *sc, const MuonRenderParams &p, double *d_sum, doubl
   const bool use_graph = bounded && !(p.flags & MUON_RENDER_NO_GRAPH);
   if (moved) sc->DropGraph();
   CUDA_TRY(cudaEventRecord(t0, st));
-  if (use_graph) {
-    if (sc->graph_key != keybuf || !sc->graph) {
+  const bool graph_ready = use_graph && sc->graph && sc->graph_key == keybuf;
+  if (graph_ready || (use_graph && sc->seen_key == keybuf)) {
+    if (!graph_ready) {
       sc->DropGraph();
       cudaGraph_t g = nullptr;
       launches = 0;
       CUDA_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
       try {
+        capturing = true;
         enqueue(false);
+        capturing = false;
       } catch (...) {
         cudaGraph_t dummy = nullptr;
         cudaStreamEndCapture(st, &dummy);
@@ -532,6 +557,7 @@ void RenderDevice(MuonScene *sc, const MuonRenderParams &p, double *d_sum, doubl
     timed_pairs = sc->graph_events;
   } else {
     enqueue(!bounded);
+    if (use_graph) sc->seen_key = keybuf;
   }
   CUDA_TRY(cudaEventRecord(t1, st));
   CUDA_TRY(cudaGetLastError());
@@ -592,6 +618,106 @@ void RenderDevice(MuonScene *sc, const MuonRenderParams &p, double *d_sum, doubl
 }  // namespace
 
 namespace muon_gpu {
+
+// ---- device block cache (host_cuda.h) ----------------------------------------------
+namespace {
+
+struct PoolBlock {
+  int device;
+  void *ptr;
+  size_t bytes;
+};
+
+std::mutex g_pool_mu;
+std::vector<PoolBlock> g_pool;  // oldest first
+
+size_t PoolCap(int device) {
+  size_t free_b = 0, total_b = 0;
+  int cur = 0;
+  cudaGetDevice(&cur);
+  if (cur != device) cudaSetDevice(device);
+  if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) total_b = 0;
+  if (cur != device) cudaSetDevice(cur);
+  return total_b / 8;
+}
+
+}  // namespace
+
+void PoolGive(DeviceBuffer &buf, int device) noexcept {
+  if (!buf.ptr) return;
+  std::vector<void *> evict;
+  try {
+    std::lock_guard<std::mutex> lock(g_pool_mu);
+    g_pool.push_back({device, buf.ptr, buf.bytes});
+    size_t held = 0;
+    for (const PoolBlock &b : g_pool)
+      if (b.device == device) held += b.bytes;
+    const size_t cap = PoolCap(device);
+    for (size_t i = 0; i < g_pool.size() && held > cap;) {
+      if (g_pool[i].device == device) {
+        held -= g_pool[i].bytes;
+        evict.push_back(g_pool[i].ptr);
+        g_pool.erase(g_pool.begin() + static_cast<std::ptrdiff_t>(i));
+      } else {
+        ++i;
+      }
+    }
+  } catch (...) {  // no room to remember the block: free it
+    cudaFree(buf.ptr);
+  }
+  buf.ptr = nullptr;
+  buf.bytes = 0;
+  for (void *p : evict) cudaFree(p);
+}
+
+void PoolTrim(int device) noexcept {
+  std::vector<void *> drop;
+  {
+    std::lock_guard<std::mutex> lock(g_pool_mu);
+    for (size_t i = 0; i < g_pool.size();) {
+      if (device < 0 || g_pool[i].device == device) {
+        drop.push_back(g_pool[i].ptr);
+        g_pool.erase(g_pool.begin() + static_cast<std::ptrdiff_t>(i));
+      } else {
+        ++i;
+      }
+    }
+  }
+  for (void *p : drop) cudaFree(p);
+}
+
+void EnsurePooled(DeviceBuffer &buf, size_t want, int device) {
+  if (want <= buf.bytes && buf.ptr) return;
+  PoolGive(buf, device);
+  if (want == 0) return;
+  {
+    std::lock_guard<std::mutex> lock(g_pool_mu);
+    size_t best = g_pool.size();
+    for (size_t i = 0; i < g_pool.size(); ++i) {
+      const PoolBlock &b = g_pool[i];
+      if (b.device == device && b.bytes >= want && b.bytes <= want + want / 2 &&
+          (best == g_pool.size() || b.bytes < g_pool[best].bytes))
+        best = i;
+    }
+    if (best < g_pool.size()) {
+      buf.ptr = g_pool[best].ptr;
+      buf.bytes = g_pool[best].bytes;
+      g_pool.erase(g_pool.begin() + static_cast<std::ptrdiff_t>(best));
+      return;
+    }
+  }
+  cudaError_t e = cudaMalloc(&buf.ptr, want);
+  if (e == cudaErrorMemoryAllocation) {
+    cudaGetLastError();
+    PoolTrim(-1);
+    e = cudaMalloc(&buf.ptr, want);
+  }
+  if (e != cudaSuccess) {
+    buf.ptr = nullptr;
+    throw CudaError{e, "cudaMalloc"};
+  }
+  buf.bytes = want;
+}
 
 void RenderGuided(MuonScene *sc, const MuonRenderParams &p, double *d_sum, double *d_sq, uint32_t *d_cnt,
                   const GuideDev &g) {
@@ -681,6 +807,8 @@ int muon_gpu_scene_create(const MuonSceneDesc *desc, MuonScene **out) {
 
 void muon_gpu_scene_destroy(MuonScene *scene) { delete scene; }
 
+void muon_gpu_release_cached(void) { PoolTrim(-1); }
+
 int muon_gpu_render_device(MuonScene *scene, const MuonRenderParams *params, double *d_sum, double *d_sum_sq,
                            uint32_t *d_count) {
   if (!scene || !params || !d_sum || !d_sum_sq || !d_count) return Fail(MUON_ERR_INVALID_ARG, "null argument");
@@ -713,9 +841,9 @@ int muon_gpu_render(MuonScene *scene, const MuonRenderParams *params, MuonFilm *
   try {
     CUDA_TRY(cudaSetDevice(scene->device));
     const size_t np = static_cast<size_t>(film->width) * film->height;
-    scene->film_sum.Ensure(3 * np * sizeof(double));
-    scene->film_sq.Ensure(3 * np * sizeof(double));
-    scene->film_cnt.Ensure(np * sizeof(uint32_t));
+    EnsurePooled(scene->film_sum, 3 * np * sizeof(double), scene->device);
+    EnsurePooled(scene->film_sq, 3 * np * sizeof(double), scene->device);
+    EnsurePooled(scene->film_cnt, np * sizeof(uint32_t), scene->device);
     cudaStream_t st = scene->stream;
     if (params->flags & MUON_RENDER_ACCUMULATE) {
       CUDA_TRY(cudaMemcpyAsync(scene->film_sum.ptr, film->sum, 3 * np * sizeof(double), cudaMemcpyHostToDevice, st));

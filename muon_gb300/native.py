@@ -136,6 +136,7 @@ SIGNATURES = {
     "muon_film_write": (C.c_int, [C.POINTER(Film), C.c_float, C.c_char_p]),
     "muon_gpu_scene_create": (C.c_int, [C.POINTER(SceneDesc), C.POINTER(C.c_void_p)]),
     "muon_gpu_scene_destroy": (None, [C.c_void_p]),
+    "muon_gpu_release_cached": (None, []),
     "muon_gpu_render": (C.c_int, [C.c_void_p, C.POINTER(RenderParams), C.POINTER(Film)]),
     "muon_gpu_render_device": (C.c_int, [C.c_void_p, C.POINTER(RenderParams), C.c_void_p, C.c_void_p,
                                          C.c_void_p]),

@@ -176,3 +176,37 @@ def test_counted_rays_follow_the_reference_definition(lib):
     gpu_ratio = st["secondary_rays"] / st["primary_rays"]
     print(f"secondary per primary: gpu {gpu_ratio:.4f} reference {ref_ratio:.4f}")
     assert abs(gpu_ratio - ref_ratio) <= 0.01 * ref_ratio
+
+
+@pytest.mark.gpu
+def test_direct_and_graph_renders_are_identical(lib):
+    """A scene's first render of a configuration launches kernel by kernel,
+    the second captures a CUDA graph, the third replays it: same film bits."""
+    fx = np.load(f"{GOLDEN}/pt_cornell.npz")
+    scene = m.Scene.from_string(str(fx["scene"]))
+    films = [scene.render(pixel_samples=64, seed=3) for _ in range(3)]
+    for f in films[1:]:
+        assert np.array_equal(f.sum, films[0].sum) and np.array_equal(f.sum_sq, films[0].sum_sq)
+        assert np.array_equal(f.count, films[0].count)
+
+
+@pytest.mark.gpu
+def test_scenes_reuse_cached_work_arrays(lib):
+    """Destroyed scenes leave their work arrays cached for the next scene;
+    renders are the same with reused arrays, fresh ones, and after the cache
+    is released."""
+    texts = [str(np.load(f"{GOLDEN}/pt_{n}.npz")["scene"]) for n in ("cornell", "feature_mix")]
+
+    def render(text):
+        sc = m.Scene.from_string(text)
+        f = sc.render(pixel_samples=32, seed=5)
+        sc.close()
+        return f
+
+    first = [render(t) for t in texts]
+    again = [render(t) for t in reversed(texts)][::-1]
+    native.load().muon_gpu_release_cached()
+    fresh = [render(t) for t in texts]
+    for a, b, c in zip(first, again, fresh):
+        assert np.array_equal(a.sum, b.sum) and np.array_equal(a.sum, c.sum)
+        assert np.array_equal(a.count, b.count) and np.array_equal(a.count, c.count)

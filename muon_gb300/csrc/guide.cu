@@ -25,7 +25,7 @@ namespace {
 using namespace guide;
 
 constexpr int kThreads = 256;
-constexpr int kChunk = 2048;  // samples per weight-gradient partial
+constexpr int kChunk = 512;  // samples per weight-gradient partial
 
 // ---- packing and initialisation ------------------------------------------------
 // The inference image (guide_mlp.cuh): one thread per 16-byte chunk of a
@@ -102,6 +102,28 @@ __global__ void __launch_bounds__(kTcThreads, 1) ForwardKernel(const void *img, 
   TcEnd(smem, grp, status);
 }
 
+// T consecutive floats of shared memory into registers, as 16- or 8-byte
+// loads where T allows (p is aligned to T floats).
+template <int T>
+__device__ __forceinline__ void LoadRow(const float *p, float (&v)[T]) {
+  if constexpr (T % 4 == 0) {
+#pragma unroll
+    for (int q = 0; q < T / 4; ++q) {
+      const float4 f = reinterpret_cast<const float4 *>(p)[q];
+      v[4 * q] = f.x, v[4 * q + 1] = f.y, v[4 * q + 2] = f.z, v[4 * q + 3] = f.w;
+    }
+  } else if constexpr (T % 2 == 0) {
+#pragma unroll
+    for (int q = 0; q < T / 2; ++q) {
+      const float2 f = reinterpret_cast<const float2 *>(p)[q];
+      v[2 * q] = f.x, v[2 * q + 1] = f.y;
+    }
+  } else {
+#pragma unroll
+    for (int q = 0; q < T; ++q) v[q] = p[q];
+  }
+}
+
 // ---- training: forward ----------------------------------------------------------
 // y[b][n] = act(sum_k x[b][k] w[k][n] + bias[n]) for a tile of 64 samples;
 // with kBlob, x is the one-blob encoding of features (batch x 8).
@@ -109,7 +131,7 @@ template <bool kBlob, bool kRelu>
 __global__ void __launch_bounds__(kThreads) FwdLayerKernel(const float *x, const float *w, const float *bias, int K,
                                                            int N, float *y, int batch) {
   __shared__ float xs[64][33];
-  __shared__ float ws[32][65];
+  __shared__ __align__(16) float ws[32][64];
   const int tid = threadIdx.x, ty = tid >> 4, tx = tid & 15;
   const int b0 = blockIdx.x * 64;
   float acc[4][4] = {};
@@ -132,7 +154,8 @@ __global__ void __launch_bounds__(kThreads) FwdLayerKernel(const float *x, const
     for (int kk = 0; kk < 32; ++kk) {
       float a[4], bb[4];
 #pragma unroll
-      for (int i = 0; i < 4; ++i) a[i] = xs[ty * 4 + i][kk], bb[i] = ws[kk][tx * 4 + i];
+      for (int i = 0; i < 4; ++i) a[i] = xs[ty * 4 + i][kk];
+      LoadRow<4>(&ws[kk][tx * 4], bb);
 #pragma unroll
       for (int i = 0; i < 4; ++i)
 #pragma unroll
@@ -230,20 +253,21 @@ __global__ void __launch_bounds__(kThreads) LossKernel(float *z, const float *di
 __global__ void __launch_bounds__(kThreads) BwdDataKernel(const float *dz, const float *w, const float *h, int N,
                                                           float *dx, int batch) {
   __shared__ float ds[64][65];
-  __shared__ float ws[64][65];
+  __shared__ __align__(16) float wt[64][68];  // wt[n][k] = w[k][n], rows 16-byte aligned
   const int tid = threadIdx.x, ty = tid >> 4, tx = tid & 15;
   const int b0 = blockIdx.x * 64;
   for (int i = tid; i < 64 * 64; i += kThreads) {
     const int r = i >> 6, c = i & 63, b = b0 + r;
     ds[r][c] = (b < batch && c < N) ? dz[static_cast<int64_t>(b) * N + c] : 0.0f;
-    ws[r][c] = c < N ? w[r * N + c] : 0.0f;  // row k, column n
+    wt[c][r] = c < N ? w[r * N + c] : 0.0f;  // w row k = r, column n = c
   }
   __syncthreads();
   float acc[4][4] = {};
   for (int n = 0; n < N; ++n) {
     float a[4], bb[4];
 #pragma unroll
-    for (int i = 0; i < 4; ++i) a[i] = ds[ty * 4 + i][n], bb[i] = ws[tx * 4 + i][n];
+    for (int i = 0; i < 4; ++i) a[i] = ds[ty * 4 + i][n];
+    LoadRow<4>(&wt[n][tx * 4], bb);
 #pragma unroll
     for (int i = 0; i < 4; ++i)
 #pragma unroll
@@ -265,12 +289,17 @@ __global__ void __launch_bounds__(kThreads) BwdDataKernel(const float *dz, const
 // Per chunk of samples: partial[k * N + n] = sum_b x[b][k] dz[b][n] and the
 // bias part partial[K * N + n] = sum_b dz[b][n]. Each thread owns a TK x TN
 // block of outputs.
+// Weight and bias gradients of one layer over one chunk of kChunk samples:
+// partial[chunk][k][n] = sum over the chunk's samples of x[b][k] dz[b][n].
+// Each thread owns a TK x TN tile of the K x N gradient; 32 samples at a time
+// are staged in shared memory (rows of K and N floats, read back as vectors).
 template <bool kBlob, int K, int N, int TK, int TN>
 __global__ void __launch_bounds__(kThreads) WgradKernel(const float *x, const float *dz, int batch, float *partial,
                                                         int stride, int layer_off) {
   static_assert((K / TK) * (N / TN) == kThreads, "thread tiling");
-  __shared__ float xs[32][K + 1];
-  __shared__ float ds[32][N + 1];
+  static_assert(K % 4 == 0 && N % 4 == 0, "rows of whole 16-byte vectors");
+  __shared__ __align__(16) float xs[32][K];
+  __shared__ __align__(16) float ds[32][N];
   const int tid = threadIdx.x;
   const int kg = tid / (N / TN), ng = tid % (N / TN);
   const int b0 = blockIdx.x * kChunk;
@@ -291,12 +320,11 @@ __global__ void __launch_bounds__(kThreads) WgradKernel(const float *x, const fl
       ds[r][n] = b < batch ? dz[static_cast<int64_t>(b) * N + n] : 0.0f;
     }
     __syncthreads();
+#pragma unroll 4
     for (int r = 0; r < 32; ++r) {
       float a[TK], d[TN];
-#pragma unroll
-      for (int i = 0; i < TK; ++i) a[i] = xs[r][kg * TK + i];
-#pragma unroll
-      for (int j = 0; j < TN; ++j) d[j] = ds[r][ng * TN + j];
+      LoadRow<TK>(&xs[r][kg * TK], a);
+      LoadRow<TN>(&ds[r][ng * TN], d);
 #pragma unroll
       for (int i = 0; i < TK; ++i)
 #pragma unroll
@@ -352,19 +380,33 @@ __global__ void GatherKernel(const GuideSample *pool, uint64_t available, uint32
 }
 
 // Divides the weights by their mean (one block; fixed summation order).
-__global__ void __launch_bounds__(1024) NormaliseKernel(float *weights, int batch) {
-  __shared__ double red[1024];
+// Training weights divided by their batch mean, in two deterministic passes:
+// per-block sums in a fixed order, then every block forms the total from them.
+constexpr int kSumBlocks = 256;
+
+__global__ void __launch_bounds__(256) WeightSumKernel(const float *weights, int batch, double *part) {
+  __shared__ double red[256];
   double s = 0.0;
-  for (int i = threadIdx.x; i < batch; i += 1024) s += weights[i];
+  for (int i = blockIdx.x * 256 + threadIdx.x; i < batch; i += kSumBlocks * 256) s += weights[i];
   red[threadIdx.x] = s;
   __syncthreads();
-  for (int o = 512; o > 0; o >>= 1) {
+  for (int o = 128; o > 0; o >>= 1) {
     if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
     __syncthreads();
   }
-  const double mean = red[0] / static_cast<double>(batch);
-  const float inv = mean > 0.0 ? static_cast<float>(1.0 / mean) : 0.0f;
-  for (int i = threadIdx.x; i < batch; i += 1024) weights[i] *= inv;
+  if (threadIdx.x == 0) part[blockIdx.x] = red[0];
+}
+
+__global__ void __launch_bounds__(256) WeightScaleKernel(float *weights, int batch, const double *part) {
+  __shared__ float inv;
+  if (threadIdx.x == 0) {
+    double total = 0.0;
+    for (int b = 0; b < kSumBlocks; ++b) total += part[b];
+    const double mean = total / static_cast<double>(batch);
+    inv = mean > 0.0 ? static_cast<float>(1.0 / mean) : 0.0f;
+  }
+  __syncthreads();
+  for (int i = blockIdx.x * 256 + threadIdx.x; i < batch; i += gridDim.x * 256) weights[i] *= inv;
 }
 
 inline unsigned Grid(int64_t n, int block) { return static_cast<unsigned>((n + block - 1) / block); }
@@ -395,7 +437,7 @@ size_t GuideTrainBytes(int batch) {
   const size_t chunks = (batch + kChunk - 1) / kChunk;
   return sizeof(float) * (4ull * batch * kWidth + static_cast<size_t>(batch) * kOut + 2ull * batch * kWidth +
                           chunks * kParams + kParams) +
-         sizeof(double) * (batch / kThreads + 2) + 256 * 8;
+         sizeof(double) * (batch / kThreads + 2 + kSumBlocks) + 256 * 9;
 }
 
 void GuideTrainCarve(void *base, int batch, GuideTrainBuffers *out) {
@@ -414,6 +456,7 @@ void GuideTrainCarve(void *base, int batch, GuideTrainBuffers *out) {
   out->partial = reinterpret_cast<float *>(take(sizeof(float) * out->chunks * kParams));
   out->grad = reinterpret_cast<float *>(take(sizeof(float) * kParams));
   out->loss = reinterpret_cast<double *>(take(sizeof(double) * (batch / kThreads + 2)));
+  out->wsum = reinterpret_cast<double *>(take(sizeof(double) * kSumBlocks));
 }
 
 void LaunchGuideGradients(const float *params, const float *features, const float *dirs, const float *weights,
@@ -446,9 +489,10 @@ void LaunchGuideGradients(const float *params, const float *features, const floa
 }
 
 void LaunchGuideGather(const GuideSample *pool, uint64_t available, uint32_t cap, int batch, uint64_t seed,
-                       float *features, float *dirs, float *weights, cudaStream_t st) {
+                       float *features, float *dirs, float *weights, double *sums, cudaStream_t st) {
   GatherKernel<<<Grid(batch, 256), 256, 0, st>>>(pool, available, cap, batch, seed, features, dirs, weights);
-  NormaliseKernel<<<1, 1024, 0, st>>>(weights, batch);
+  WeightSumKernel<<<kSumBlocks, 256, 0, st>>>(weights, batch, sums);
+  WeightScaleKernel<<<std::max(1u, std::min(Grid(batch, 256), 1024u)), 256, 0, st>>>(weights, batch, sums);
 }
 
 void LaunchGuideAdam(float *params, float *m, float *v, const float *grad, float lr, int step, cudaStream_t st) {

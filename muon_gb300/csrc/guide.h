@@ -83,6 +83,7 @@ struct GuideTrainBuffers {
   float *partial;   // per chunk: all weight and bias gradients
   float *grad;      // guide::kParams
   double *loss;     // loss sum of every 256 consecutive samples
+  double *wsum;     // partial sums of the training weights (LaunchGuideGather)
   int32_t chunks;
 };
 size_t GuideTrainBytes(int batch);
@@ -92,9 +93,10 @@ void GuideTrainCarve(void *base, int batch, GuideTrainBuffers *out);
 void LaunchGuideGradients(const float *params, const float *features, const float *dirs, const float *weights,
                           int batch, const GuideTrainBuffers &tb, cudaStream_t st);
 // Gathers `batch` samples from the pool at random positions (seeded) into
-// features / dirs / weights (weights normalised by their batch mean).
+// features / dirs / weights (weights normalised by their batch mean; `sums`
+// is scratch of GuideTrainBuffers::wsum).
 void LaunchGuideGather(const GuideSample *pool, uint64_t available, uint32_t cap, int batch, uint64_t seed,
-                       float *features, float *dirs, float *weights, cudaStream_t st);
+                       float *features, float *dirs, float *weights, double *sums, cudaStream_t st);
 void LaunchGuideAdam(float *params, float *m, float *v, const float *grad, float lr, int step, cudaStream_t st);
 
 }  // namespace muon_gpu

@@ -181,7 +181,7 @@ int muon_gpu_guide_train(MuonGuide *guide, int32_t steps, double *loss) {
     for (int s = 0; s < steps; ++s) {
       LaunchGuideGather(guide->pool.as<GuideSample>(), avail, guide->dev.pool_cap, batch,
                         guide->cfg.seed * 0x9E3779B97F4A7C15ull + (++guide->batches), guide->batch_feat.as<float>(),
-                        guide->batch_dir.as<float>(), guide->batch_w.as<float>(), st);
+                        guide->batch_dir.as<float>(), guide->batch_w.as<float>(), tb.wsum, st);
       LaunchGuideGradients(guide->params.as<float>(), guide->batch_feat.as<float>(), guide->batch_dir.as<float>(),
                            guide->batch_w.as<float>(), batch, tb, st);
       LaunchGuideAdam(guide->params.as<float>(), guide->adam_m.as<float>(), guide->adam_v.as<float>(), tb.grad,

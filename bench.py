@@ -160,7 +160,7 @@ def run_batch(args) -> None:
 
     native_build.build()
     import muon_gb300 as m
-    from muon_gb300 import native
+    from muon_gb300 import native, replicas
 
     texts = batch_texts()
     parsed = [m.parse_string(t) for t in texts]
@@ -193,12 +193,7 @@ def run_batch(args) -> None:
             lat += [p["done_ms"] for p in per]
             launches = total["kernel_launches"]
     dev_ms = sum(times)
-    t = torch.tensor([dev_ms, float(counted)], dtype=torch.float64, device="cuda")
-    if world > 1:
-        tmax, tsum = t.clone(), t.clone()
-        torch.distributed.all_reduce(tmax, op=torch.distributed.ReduceOp.MAX)
-        torch.distributed.all_reduce(tsum, op=torch.distributed.ReduceOp.SUM)
-        dev_ms, counted = float(tmax[0]), float(tsum[1])
+    dev_ms, counted = replicas.reduce_step(dev_ms, counted, device="cuda")
     value = counted / (dev_ms * 1e3)
     # end to end: scene uploads (BVH builds), batch merge, render, host films back
     e2e_steps = 2
@@ -388,7 +383,7 @@ def run_ours(args) -> None:
 
     native_build.build()
     import muon_gb300 as m
-    from muon_gb300 import native
+    from muon_gb300 import native, replicas
 
     text = scene_text()
     scene = m.Scene.from_string(text, builder=args.builder)
@@ -437,15 +432,7 @@ def run_ours(args) -> None:
     counted = sum(s["primary_rays"] + s["secondary_rays"] for s in st_steps)
     launches = sum(s["kernel_launches"] for s in st_steps)
 
-    t = torch.tensor([dev_ms, float(counted)], dtype=torch.float64, device="cuda")
-    if world > 1:
-        tmax = t.clone()
-        torch.distributed.all_reduce(tmax, op=torch.distributed.ReduceOp.MAX)
-        tsum = t.clone()
-        torch.distributed.all_reduce(tsum, op=torch.distributed.ReduceOp.SUM)
-        dev_ms_max, counted_all = float(tmax[0]), float(tsum[1])
-    else:
-        dev_ms_max, counted_all = dev_ms, float(counted)
+    dev_ms_max, counted_all = replicas.reduce_step(dev_ms, counted, device="cuda")
     value = counted_all / (dev_ms_max * 1e3)
 
     # end to end through the public API with host buffers

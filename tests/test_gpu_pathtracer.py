@@ -210,3 +210,27 @@ def test_scenes_reuse_cached_work_arrays(lib):
     for a, b, c in zip(first, again, fresh):
         assert np.array_equal(a.sum, b.sum) and np.array_equal(a.sum, c.sum)
         assert np.array_equal(a.count, b.count) and np.array_equal(a.count, c.count)
+
+
+@pytest.mark.gpu
+def test_replica_sample_ranges_add_up_to_one_render(lib):
+    """Multi-GPU replicas (muon_gb300/replicas.py): the films of the ranks'
+    sample ranges, added, are the film of one render of all the samples
+    (rendered here one range after another on one GPU)."""
+    from muon_gb300 import replicas
+
+    fx = np.load(f"{GOLDEN}/pt_feature_mix.npz")
+    scene = m.Scene.from_string(str(fx["scene"]))
+    spp, world = 100, 3
+    whole = scene.render(pixel_samples=spp, seed=17)
+    parts = []
+    for rank in range(world):
+        off, n = replicas.sample_range(rank, world, spp)
+        parts.append(scene.render(pixel_samples=n, sample_offset=off, seed=17))
+    s = sum(f.sum for f in parts)
+    q = sum(f.sum_sq for f in parts)
+    c = sum(f.count.astype(np.int64) for f in parts)
+    assert np.array_equal(c, whole.count.astype(np.int64))
+    ok = np.isfinite(whole.sum)
+    np.testing.assert_allclose(s[ok], whole.sum[ok], rtol=1e-12, atol=1e-12)
+    np.testing.assert_allclose(q[ok], whole.sum_sq[ok], rtol=1e-12, atol=1e-12)

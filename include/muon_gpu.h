@@ -409,7 +409,7 @@ typedef struct MuonGuideConfig {
 } MuonGuideConfig;
 
 /* Number of FP32 network parameters (weights [in][out] then biases, per layer). */
-#define MUON_GUIDE_PARAMS 31528
+#define MUON_GUIDE_PARAMS 33088
 
 int muon_gpu_guide_create(MuonScene *scene, const MuonGuideConfig *config, MuonGuide **out);
 void muon_gpu_guide_destroy(MuonGuide *guide);
@@ -422,7 +422,7 @@ int muon_gpu_guide_render_device(MuonGuide *guide, const MuonRenderParams *param
 /* `steps` Adam steps on batches drawn from the collected samples; the mean
  * loss of the last step goes to *loss when not NULL. */
 int muon_gpu_guide_train(MuonGuide *guide, int32_t steps, double *loss);
-/* Network outputs (n x 40 raw values) for features (n x 8), on the
+/* Network outputs (n x 64 raw values) for features (n x 8), on the
  * tensor-core inference path; host arrays. */
 int muon_gpu_guide_forward(MuonGuide *guide, const float *features, int64_t n, float *out);
 /* Gradients (MUON_GUIDE_PARAMS values) of the mean loss over one batch of n

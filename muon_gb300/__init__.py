@@ -316,7 +316,7 @@ class Guide:
 
     def forward(self, features: np.ndarray) -> np.ndarray:
         f = np.ascontiguousarray(features, dtype=np.float32)
-        out = np.zeros((len(f), 40), dtype=np.float32)
+        out = np.zeros((len(f), 64), dtype=np.float32)
         check(load().muon_gpu_guide_forward(self._h, f.ctypes.data_as(C.POINTER(C.c_float)), len(f),
                                             out.ctypes.data_as(C.POINTER(C.c_float))))
         return out

@@ -179,6 +179,12 @@ __global__ void __launch_bounds__(kThreads) FwdLayerKernel(const float *x, const
 
 // ---- training: loss ---------------------------------------------------------------
 // Replaces z (raw outputs) by d(mean loss)/dz and writes per-block loss sums.
+// Per sample: loss -weight log q(w) and its gradient with respect to the 64
+// raw outputs (written over them), mean over the batch. q = (1 - eps)
+// sum_i pi_i p_i + eps / (4 pi) with the lobes of guide_mlp.cuh; the
+// gradient of log p_i follows oracle/guiding.py (loss_grad), through
+// s = exp(b) (inside the clip range), the tangent projection pu = u - (u.mu) mu
+// and mu = m / |m|.
 __global__ void __launch_bounds__(kThreads) LossKernel(float *z, const float *dirs, const float *weights, int batch,
                                                        double *loss_out) {
   __shared__ double red[kThreads];
@@ -186,57 +192,88 @@ __global__ void __launch_bounds__(kThreads) LossKernel(float *z, const float *di
   double loss = 0.0;
   if (b < batch) {
     float *r = z + static_cast<int64_t>(b) * kOut;
-    const float wx = dirs[3 * b], wy = dirs[3 * b + 1], wz = dirs[3 * b + 2];
+    const float w[3] = {dirs[3 * b], dirs[3 * b + 1], dirs[3 * b + 2]};
     const float wt = weights[b];
-    float pi[kLobes], kap[kLobes], mu[kLobes][3], nrm[kLobes], cosw[kLobes], lpf[kLobes];
     float amax = -INFINITY;
-    for (int i = 0; i < kLobes; ++i) amax = fmaxf(amax, r[5 * i]);
-    float s = 0.0f;
-    for (int i = 0; i < kLobes; ++i) s += expf(r[5 * i] - amax);
-    const float lse = amax + logf(s);
-    float lmax = -INFINITY;
+    for (int i = 0; i < kLobes; ++i) amax = fmaxf(amax, r[kLobeOut * i]);
+    float se = 0.0f;
+    for (int i = 0; i < kLobes; ++i) se += expf(r[kLobeOut * i] - amax);
+    const float lse = amax + logf(se);
+    // pass 1: log of each lobe's share of q (-inf where the lobe is zero)
+    float t[kLobes];
+    const float log_keep = logf(1.0f - kEpsUniform), t_uniform = logf(kEpsUniform * 0.25f / kPi);
+    float tmax = t_uniform;
     for (int i = 0; i < kLobes; ++i) {
-      const float la = r[5 * i] - lse;  // log pi
-      pi[i] = expf(la);
-      float mx = r[5 * i + 1], my = r[5 * i + 2], mz = r[5 * i + 3];
-      float n2 = mx * mx + my * my + mz * mz;
-      nrm[i] = sqrtf(n2);
+      const float *ri = r + kLobeOut * i;
+      t[i] = -INFINITY;
+      const float n2 = ri[1] * ri[1] + ri[2] * ri[2] + ri[3] * ri[3];
+      float mu[3] = {0.0f, 0.0f, 1.0f};
       if (n2 > 1e-24f) {
-        mu[i][0] = mx / nrm[i], mu[i][1] = my / nrm[i], mu[i][2] = mz / nrm[i];
-      } else {
-        mu[i][0] = 0.0f, mu[i][1] = 0.0f, mu[i][2] = 1.0f;
+        const float k = 1.0f / sqrtf(n2);
+        mu[0] = ri[1] * k, mu[1] = ri[2] * k, mu[2] = ri[3] * k;
       }
-      const float bb = fminf(fmaxf(r[5 * i + 4], kBMin), kBMax);
-      kap[i] = expf(bb);
-      cosw[i] = mu[i][0] * wx + mu[i][1] * wy + mu[i][2] * wz;
-      const float logf_i = logf(kap[i]) - logf(2.0f * 3.14159265358979f) - logf(-expm1f(-2.0f * kap[i])) +
-                           kap[i] * (cosw[i] - 1.0f);
-      lpf[i] = la + logf_i;
-      lmax = fmaxf(lmax, lpf[i]);
+      const float c = mu[0] * w[0] + mu[1] * w[1] + mu[2] * w[2];
+      if (!(c > kCMin)) continue;
+      const float s = expf(fminf(fmaxf(ri[4], kBMin), kBMax));
+      const float um = ri[5] * mu[0] + ri[6] * mu[1] + ri[7] * mu[2];
+      float pu[3], v[3], p2 = 0.0f, v2 = 0.0f, d = 0.0f;
+      for (int k = 0; k < 3; ++k) {
+        pu[k] = ri[5 + k] - um * mu[k];
+        v[k] = w[k] / c - mu[k];
+        p2 += pu[k] * pu[k], v2 += v[k] * v[k], d += pu[k] * v[k];
+      }
+      const float logp = 0.5f * logf(s) + 0.5f * logf(s + p2) - logf(2.0f * kPi) - 0.5f * (s * v2 + d * d) -
+                         3.0f * logf(c);
+      t[i] = log_keep + (ri[0] - lse) + logp;
+      tmax = fmaxf(tmax, t[i]);
     }
-    float qs = 0.0f;
-    for (int i = 0; i < kLobes; ++i) qs += expf(lpf[i] - lmax);
-    const float logq = lmax + logf(qs);
+    float qs = expf(t_uniform - tmax);
+    for (int i = 0; i < kLobes; ++i) qs += expf(t[i] - tmax);
+    const float logq = tmax + logf(qs);
     loss = -static_cast<double>(wt) * logq;
     const float coef = -wt / static_cast<float>(batch);
+    float resp[kLobes], rsum = 0.0f;
     for (int i = 0; i < kLobes; ++i) {
-      const float resp = expf(lpf[i] - logq);
-      const float cr = coef * resp;
-      float g[5];
-      g[0] = coef * (resp - pi[i]);
-      if (nrm[i] * nrm[i] > 1e-24f) {
-        for (int c = 0; c < 3; ++c) {
-          const float w_c = c == 0 ? wx : (c == 1 ? wy : wz);
-          g[1 + c] = cr * kap[i] * (w_c - cosw[i] * mu[i][c]) / nrm[i];
+      resp[i] = expf(t[i] - logq);
+      rsum += resp[i];
+    }
+    // pass 2: gradients, written over the raw outputs
+    for (int i = 0; i < kLobes; ++i) {
+      float *ri = r + kLobeOut * i;
+      const float pi = expf(ri[0] - lse);
+      float g[kLobeOut] = {coef * (resp[i] - pi * rsum), 0, 0, 0, 0, 0, 0, 0};
+      const float n2 = ri[1] * ri[1] + ri[2] * ri[2] + ri[3] * ri[3];
+      float mu[3] = {0.0f, 0.0f, 1.0f};
+      const float nrm = sqrtf(n2);
+      if (n2 > 1e-24f) mu[0] = ri[1] / nrm, mu[1] = ri[2] / nrm, mu[2] = ri[3] / nrm;
+      const float c = mu[0] * w[0] + mu[1] * w[1] + mu[2] * w[2];
+      if (resp[i] > 0.0f && c > kCMin) {
+        const float cr = coef * resp[i];
+        const float braw = ri[4];
+        const float s = expf(fminf(fmaxf(braw, kBMin), kBMax));
+        const float um = ri[5] * mu[0] + ri[6] * mu[1] + ri[7] * mu[2];
+        float pu[3], v[3], p2 = 0.0f, v2 = 0.0f, d = 0.0f, vw = 0.0f, pw = 0.0f;
+        for (int k = 0; k < 3; ++k) {
+          pu[k] = ri[5 + k] - um * mu[k];
+          v[k] = w[k] / c - mu[k];
+          p2 += pu[k] * pu[k], v2 += v[k] * v[k], d += pu[k] * v[k];
+          vw += v[k] * w[k], pw += pu[k] * w[k];
         }
-      } else {
-        g[1] = g[2] = g[3] = 0.0f;
+        const float sp2 = s + p2;
+        if (braw > kBMin && braw < kBMax) g[4] = cr * (0.5f + 0.5f * s / sp2 - 0.5f * s * v2);
+        for (int k = 0; k < 3; ++k) g[5 + k] = cr * (pu[k] / sp2 - d * v[k]);
+        if (n2 > 1e-24f) {
+          const float ic2 = 1.0f / (c * c);
+          float gm[3], dot = 0.0f;
+          for (int k = 0; k < 3; ++k) {
+            gm[k] = -um * pu[k] / sp2 + s * (vw * w[k] * ic2 + v[k]) + d * (um * v[k] + pw * w[k] * ic2 + pu[k]) -
+                    3.0f * w[k] / c;
+            dot += gm[k] * mu[k];
+          }
+          for (int k = 0; k < 3; ++k) g[1 + k] = cr * (gm[k] - dot * mu[k]) / nrm;
+        }
       }
-      const float e2 = expf(-2.0f * kap[i]);
-      const float dk = 1.0f / kap[i] - 2.0f * e2 / (-expm1f(-2.0f * kap[i])) + (cosw[i] - 1.0f);
-      const float braw = r[5 * i + 4];
-      g[4] = (braw > kBMin && braw < kBMax) ? cr * dk * kap[i] : 0.0f;
-      for (int c = 0; c < 5; ++c) r[5 * i + c] = g[c];
+      for (int k = 0; k < kLobeOut; ++k) ri[k] = g[k];
     }
   }
   red[threadIdx.x] = loss;
@@ -471,7 +508,7 @@ void LaunchGuideGradients(const float *params, const float *features, const floa
   LossKernel<<<Grid(batch, kThreads), kThreads, 0, st>>>(tb.z, dirs, weights, batch, tb.loss);
   const unsigned chunks = static_cast<unsigned>(tb.chunks);
   // layer 4: 64 x 40
-  WgradKernel<false, kWidth, kOut, 2, 5><<<chunks, kThreads, 0, st>>>(tb.h[4], tb.z, batch, tb.partial, kParams,
+  WgradKernel<false, kWidth, kOut, 4, 4><<<chunks, kThreads, 0, st>>>(tb.h[4], tb.z, batch, tb.partial, kParams,
                                                                        MasterOffset(4));
   BwdDataKernel<<<tiles, kThreads, 0, st>>>(tb.z, W(4), tb.h[4], kOut, tb.dz[0], batch);
   // layers 3..1: 64 x 64

@@ -30,7 +30,7 @@ struct GuideSample {
 struct GuideDev {
   const void *wt;        // the inference image (guide_mlp.cuh): BF16 operands, then FP32 biases
   int32_t *status;       // set to 1 by an inference kernel whose tensor-core wait gave up
-  float4 *mix;           // 10 per queue entry: the processed mixture
+  float4 *mix;           // guide::kMixVec per queue entry: the processed mixture
   float4 *feat;          // 2 per queue entry: the features
   GuideRec *rec;         // rec_bounces x rec_cap
   int32_t rec_cap;       // entries per bounce (the wave's capacity)

@@ -89,7 +89,7 @@ int muon_gpu_guide_create(MuonScene *scene, const MuonGuideConfig *config, MuonG
     g->wt.Ensure(guide::kImgBytes);
     g->status.Ensure(sizeof(int32_t));
     const size_t cap = static_cast<size_t>(c.wave_paths);
-    g->mix.Ensure(cap * 10 * sizeof(float4));
+    g->mix.Ensure(cap * guide::kMixVec * sizeof(float4));
     g->feat.Ensure(cap * 2 * sizeof(float4));
     const bool records = c.targets == MUON_GUIDE_ALL;  // continuation records (guided continuations only)
     if (records) g->rec.Ensure(cap * c.record_bounces * sizeof(GuideRec));

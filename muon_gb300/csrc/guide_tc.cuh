@@ -27,10 +27,10 @@ namespace muon_gpu {
 namespace guide {
 
 // Shared memory of a tcgen05 inference CTA: the weight image (padded to
-// 64 KiB), two operand buffers of 128 rows x 256 BF16, the mbarriers (weight
+// 66 KiB), two operand buffers of 128 rows x 256 BF16, the mbarriers (weight
 // copy, group 0, group 1) and the TMEM address slot.
 constexpr int kTcRows = 128;
-constexpr int kTcImgSmem = 65536;
+constexpr int kTcImgSmem = 66 * 1024;
 constexpr int kTcOperandBytes = kTcRows * kIn * 2;
 constexpr int kTcBarOffset = kTcImgSmem + 2 * kTcOperandBytes;
 constexpr int kTcSmemBytes = kTcBarOffset + 64;
@@ -330,22 +330,24 @@ __device__ __forceinline__ bool TcForward(TcGroup &g, const float (&f)[kFeatures
     TcHidden(g, l - 1);
     if (!TcLayer(g, l)) return false;
   }
-  float v[32], w[16];
-  TmemLoad32(g.tmem + g.lane_off, v);
-  TmemLoad16(g.tmem + g.lane_off + 32, w);
+  static_assert(kOut == 64, "two 32-column loads of the output layer");
   const float *b = g.bias + BiasOffset(kLayers - 1);
 #pragma unroll
-  for (int c = 0; c < 32; ++c) out[c] = v[c] + b[c];
+  for (int half = 0; half < 2; ++half) {
+    float v[32];
+    TmemLoad32(g.tmem + g.lane_off + 32 * half, v);
 #pragma unroll
-  for (int c = 32; c < kOut; ++c) out[c] = w[c - 32] + b[c];
+    for (int c = 0; c < 32; ++c) out[32 * half + c] = v[c] + b[32 * half + c];
+  }
   return true;
 }
 
 // Stages this thread's processed mixture (kMixFloats) in its row of the
 // operand buffer, which the finished network pass no longer needs; rows are
-// 176 bytes apart so that the float4 stores of 8 consecutive rows fall in
-// distinct banks.
-constexpr int kMixRowBytes = 176;
+// 304 bytes (76 words) apart so that the float4 stores of 8 consecutive rows
+// fall in distinct banks.
+constexpr int kMixRowBytes = 304;
+static_assert(kMixRowBytes >= 4 * kMixFloats && kMixRowBytes % 16 == 0, "mixture staging row");
 static_assert(kTcRows * kMixRowBytes <= kTcOperandBytes, "mixture staging larger than the operand buffer");
 
 __device__ __forceinline__ float *TcMixRow(const TcGroup &g) {

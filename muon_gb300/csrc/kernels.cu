@@ -649,7 +649,7 @@ __device__ __forceinline__ void ShadeEntry(const DevScene &s, const WaveInfo &w,
                                            float4 d4, int local, unsigned long long &counted, ShadeOut &out,
                                            const GuideDev *gd) {
     // the vertex's learned mixture when guided
-    const float *mx = gd ? reinterpret_cast<const float *>(gd->mix + 10 * static_cast<int64_t>(jj)) : nullptr;
+    const float *mx = gd ? reinterpret_cast<const float *>(gd->mix + guide::kMixVec * static_cast<int64_t>(jj)) : nullptr;
     const float3 o = f3(o4.x, o4.y, o4.z), d = f3(d4.x, d4.y, d4.z);
     const int2 h = b.hits[jj];
     float4 *contrib = b.contrib + static_cast<int64_t>(jj) * S;

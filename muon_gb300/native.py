@@ -121,7 +121,7 @@ class GuideConfig(C.Structure):
 GUIDE_DIRECT, GUIDE_ALL = 0, 1
 
 
-GUIDE_PARAMS = 31528
+GUIDE_PARAMS = 33088
 
 # Every entry point declared in include/muon_gpu.h: name -> (restype, argtypes)
 SIGNATURES = {

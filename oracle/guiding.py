@@ -11,13 +11,20 @@ reference code:
   encoding   one-blob (Mueller et al., "Neural Importance Sampling", 2019):
              each feature s -> 32 bins, bin k = exp(-(s - (k + 1/2) / 32)^2 /
              (2 sigma^2)), sigma = 1/32; 256 inputs
-  network    256 -> 64 -> 64 -> 64 -> 64 -> 40, ReLU after the first four
+  network    256 -> 64 -> 64 -> 64 -> 64 -> 64, ReLU after the first four
              layers; BF16 weights and activations, FP32 accumulation
-  output     8 von Mises-Fisher lobes, 5 numbers each (a, mx, my, mz, b):
-             weight softmax(a), mean direction normalize(m), concentration
-             kappa = exp(clip(b, -3, 8))
-  density    q(w) = sum_i pi_i kappa_i / (2 pi (1 - exp(-2 kappa_i)))
-                    * exp(kappa_i (mu_i . w - 1))
+  output     8 anisotropic lobes, 8 numbers each (a, mx, my, mz, b, ux, uy,
+             uz): weight softmax(a), mean direction mu = normalize(m),
+             isotropic precision s = exp(clip(b, -3, 8)), and the tangent
+             projection pu = u - (u . mu) mu of an anisotropy vector
+  lobe       a 2D Gaussian in the plane tangent to the sphere at mu, mapped to
+             the sphere by gnomonic projection (w = normalize(mu + x)): with
+             c = mu . w > 0, v = w / c - mu, the precision s I + pu pu^T
+             (eigenvalues s and s + |pu|^2) and Q = s |v|^2 + (pu . v)^2,
+             p(w) = sqrt(s (s + |pu|^2)) / (2 pi) exp(-Q / 2) / c^3
+             (the 1 / c^3 is the projection's area change); 0 where c <= 0
+  density    q(w) = (1 - eps) sum_i pi_i p_i(w) + eps / (4 pi), eps = 0.02: a
+             uniform component keeps q > 0 everywhere
   loss       -weight * log q(w) per sample (the KL-divergence estimator of
              Mueller et al. 2019, weight = target / sampling density), mean
              over the batch; Adam (Kingma and Ba, 2015).
@@ -32,9 +39,12 @@ N_FEATURES = 8
 N_IN = N_FEATURES * BINS
 WIDTH = 64
 LOBES = 8
-N_OUT = 5 * LOBES
+LOBE_OUT = 8  # raw outputs per lobe: a, m (3), b, u (3)
+N_OUT = LOBE_OUT * LOBES
 LAYERS = [(N_IN, WIDTH), (WIDTH, WIDTH), (WIDTH, WIDTH), (WIDTH, WIDTH), (WIDTH, N_OUT)]
 B_MIN, B_MAX = -3.0, 8.0
+EPS_UNIFORM = 0.02   # probability of the uniform component
+C_MIN = 1e-4         # lobes are zero where mu . w <= C_MIN
 
 
 def bf16(x: np.ndarray) -> np.ndarray:
@@ -87,9 +97,11 @@ def forward(params, features: np.ndarray, bf16_round: bool = True):
     return h, acts, zs
 
 
-def mixture(raw: np.ndarray):
-    """raw (N, 40) -> (pi (N,8), mu (N,8,3), kappa (N,8), b_clipped_mask)."""
-    r = raw.reshape(-1, LOBES, 5)
+def mixture(raw: np.ndarray) -> dict:
+    """raw (N, 64) -> lobe weights pi (N,8), unit means mu (N,8,3), isotropic
+    precisions s (N,8), tangent anisotropy pu (N,8,3), and what the gradient
+    needs: the raw u, |m| and the mask of b inside its clip range."""
+    r = raw.reshape(-1, LOBES, LOBE_OUT)
     a = r[:, :, 0]
     a = a - a.max(axis=1, keepdims=True)
     e = np.exp(a)
@@ -99,44 +111,99 @@ def mixture(raw: np.ndarray):
     mu = np.where(norm > 1e-12, m / np.maximum(norm, 1e-30), np.array([0.0, 0.0, 1.0]))
     b = r[:, :, 4]
     inside = (b > B_MIN) & (b < B_MAX)
-    kappa = np.exp(np.clip(b, B_MIN, B_MAX))
-    return pi, mu, kappa, inside
+    s = np.exp(np.clip(b, B_MIN, B_MAX))
+    u = r[:, :, 5:8]
+    pu = u - np.einsum("nlk,nlk->nl", u, mu)[:, :, None] * mu
+    return {"pi": pi, "mu": mu, "s": s, "pu": pu, "u": u, "norm": norm[:, :, 0], "inside": inside}
 
 
-def vmf_log_pdf(mu: np.ndarray, kappa: np.ndarray, w: np.ndarray) -> np.ndarray:
-    """log vMF density for lobes (N, L) at unit directions w (N, 3)."""
-    cos = np.einsum("nlk,nk->nl", mu, w)
-    return (np.log(kappa) - np.log(2.0 * np.pi) - np.log1p(-np.exp(-2.0 * kappa)) + kappa * (cos - 1.0))
+def lobe_terms(mx: dict, w: np.ndarray) -> dict:
+    """Per lobe at unit directions w (N, 3): c, v, |v|^2, pu . v, and log p
+    (-inf where c <= C_MIN)."""
+    mu, s, pu = mx["mu"], mx["s"], mx["pu"]
+    c = np.einsum("nlk,nk->nl", mu, w)
+    valid = c > C_MIN
+    cs = np.where(valid, c, 1.0)
+    v = w[:, None, :] / cs[:, :, None] - mu
+    v2 = np.einsum("nlk,nlk->nl", v, v)
+    d = np.einsum("nlk,nlk->nl", pu, v)
+    p2 = np.einsum("nlk,nlk->nl", pu, pu)
+    q = s * v2 + d * d
+    logp = 0.5 * np.log(s) + 0.5 * np.log(s + p2) - np.log(2.0 * np.pi) - 0.5 * q - 3.0 * np.log(cs)
+    logp = np.where(valid, logp, -np.inf)
+    return {"c": cs, "valid": valid, "v": v, "v2": v2, "d": d, "p2": p2, "logp": logp}
 
 
 def mixture_pdf(raw: np.ndarray, w: np.ndarray) -> np.ndarray:
-    pi, mu, kappa, _ = mixture(raw)
-    return (pi * np.exp(vmf_log_pdf(mu, kappa, w))).sum(axis=1)
+    mx = mixture(raw)
+    t = lobe_terms(mx, w)
+    return (1.0 - EPS_UNIFORM) * (mx["pi"] * np.exp(t["logp"])).sum(axis=1) + EPS_UNIFORM / (4.0 * np.pi)
+
+
+def sample_mixture(raw: np.ndarray, u: np.ndarray) -> np.ndarray:
+    """Directions drawn from the mixture of each row of raw, u (N, 4) uniform
+    in [0, 1): the uniform component with probability eps, else a lobe by
+    weight, then the tangent-plane Gaussian (Box-Muller) projected."""
+    mx = mixture(raw)
+    n = len(raw)
+    out = np.zeros((n, 3))
+    for i in range(n):
+        if u[i, 0] < EPS_UNIFORM:
+            z = 1.0 - 2.0 * u[i, 1]
+            ph = 2.0 * np.pi * u[i, 2]
+            rr = np.sqrt(max(0.0, 1.0 - z * z))
+            out[i] = (rr * np.cos(ph), rr * np.sin(ph), z)
+            continue
+        x = (u[i, 0] - EPS_UNIFORM) / (1.0 - EPS_UNIFORM)
+        lobe = min(int(np.searchsorted(np.cumsum(mx["pi"][i]), x, side="right")), LOBES - 1)
+        mu, s, pu = mx["mu"][i, lobe], mx["s"][i, lobe], mx["pu"][i, lobe]
+        p2 = pu @ pu
+        if p2 > 1e-20:
+            e2 = pu / np.sqrt(p2)
+        else:
+            e2 = np.cross(mu, [1.0, 0.0, 0.0] if abs(mu[0]) < 0.9 else [0.0, 1.0, 0.0])
+            e2 /= np.linalg.norm(e2)
+        e1 = np.cross(mu, e2)
+        r = np.sqrt(-2.0 * np.log(max(u[i, 1], 1e-300)))
+        g1, g2 = r * np.cos(2.0 * np.pi * u[i, 2]), r * np.sin(2.0 * np.pi * u[i, 2])
+        x = g1 / np.sqrt(s) * e1 + g2 / np.sqrt(s + p2) * e2
+        d = mu + x
+        out[i] = d / np.linalg.norm(d)
+    return out
 
 
 def loss_grad(raw: np.ndarray, w: np.ndarray, weight: np.ndarray):
-    """Loss = mean(-weight * log q(w)); returns (loss, dLoss/draw (N, 40))."""
+    """Loss = mean(-weight * log q(w)); returns (loss, dLoss/draw (N, 64))."""
     n = len(raw)
-    r = raw.reshape(n, LOBES, 5)
-    pi, mu, kappa, inside = mixture(raw)
-    logf = vmf_log_pdf(mu, kappa, w)
-    f = np.exp(logf)
-    q = (pi * f).sum(axis=1)
+    mx = mixture(raw)
+    t = lobe_terms(mx, w)
+    p = np.exp(t["logp"])
+    q = (1.0 - EPS_UNIFORM) * (mx["pi"] * p).sum(axis=1) + EPS_UNIFORM / (4.0 * np.pi)
     loss = float(np.mean(-weight * np.log(q)))
-    resp = pi * f / q[:, None]                         # responsibilities
-    coef = (-weight / n)[:, None]                      # d loss / d log q
-    g = np.zeros_like(r)
-    g[:, :, 0] = coef * (resp - pi)                    # softmax
-    m = r[:, :, 1:4]
-    norm = np.maximum(np.linalg.norm(m, axis=2, keepdims=True), 1e-30)
-    cos = np.einsum("nlk,nk->nl", mu, w)
-    dlog_dmu = kappa[:, :, None] * w[:, None, :]       # d(kappa mu.w)/dmu
-    # through mu = m / |m|: (I - mu mu^T) / |m|
-    proj = dlog_dmu - (np.einsum("nlk,nlk->nl", dlog_dmu, mu))[:, :, None] * mu
-    g[:, :, 1:4] = (coef * resp)[:, :, None] * proj / norm
-    e2 = np.exp(-2.0 * kappa)
-    dlog_dkappa = 1.0 / kappa - 2.0 * e2 / (1.0 - e2) + (cos - 1.0)
-    g[:, :, 4] = coef * resp * dlog_dkappa * kappa * inside
+    resp = (1.0 - EPS_UNIFORM) * mx["pi"] * p / q[:, None]       # responsibilities of the lobes
+    coef = (-weight / n)[:, None]                                  # d loss / d log q
+    g = np.zeros((n, LOBES, LOBE_OUT))
+    g[:, :, 0] = coef * (resp - mx["pi"] * resp.sum(axis=1, keepdims=True))
+    mu, s, pu, u = mx["mu"], mx["s"], mx["pu"], mx["u"]
+    c, v, v2, d, p2 = t["c"], t["v"], t["v2"], t["d"], t["p2"]
+    cr = (coef * resp)[:, :, None]
+    sp2 = s + p2
+    # b (through s = exp(b) inside the clip range)
+    g[:, :, 4] = coef * resp * (0.5 + 0.5 * s / sp2 - 0.5 * s * v2) * mx["inside"]
+    # u: d|pu|^2/du = 2 pu, d(pu . v)/du = v (v is tangent)
+    g[:, :, 5:8] = cr * (pu / sp2[:, :, None] - d[:, :, None] * v)
+    # mu: through c = mu . w, v = w / c - mu and pu = u - (u . mu) mu
+    um = np.einsum("nlk,nlk->nl", u, mu)[:, :, None]
+    vw = np.einsum("nlk,nk->nl", v, w)[:, :, None]
+    pw = np.einsum("nlk,nk->nl", pu, w)[:, :, None]
+    wc2 = w[:, None, :] / (c * c)[:, :, None]
+    gmu = (-um * pu / sp2[:, :, None]
+           + s[:, :, None] * (vw * wc2 + v)
+           + d[:, :, None] * (um * v + pw * wc2 + pu)
+           - 3.0 * w[:, None, :] / c[:, :, None])
+    gmu = gmu - np.einsum("nlk,nlk->nl", gmu, mu)[:, :, None] * mu
+    norm = np.maximum(mx["norm"], 1e-30)[:, :, None]
+    g[:, :, 1:4] = cr * gmu / norm * (mx["norm"] > 1e-12)[:, :, None]
     return loss, g.reshape(n, N_OUT)
 
 

@@ -41,6 +41,69 @@ def test_oracle_gradients_match_finite_differences():
         assert abs(fd - grads[li][0][a, b]) <= 1e-5 * max(1.0, abs(fd))
 
 
+def test_oracle_lobe_gradients_match_finite_differences():
+    """The mixture loss gradient of every raw output, with lobes aimed near
+    the sample directions so that every term is exercised."""
+    rng = np.random.default_rng(0)
+    n = 12
+    raw = rng.normal(0, 1, (n, G.N_OUT))
+    w = rng.normal(size=(n, 3))
+    w /= np.linalg.norm(w, axis=1, keepdims=True)
+    raw.reshape(n, G.LOBES, G.LOBE_OUT)[:, :, 1:4] += 2.0 * w[:, None, :]
+    wt = rng.uniform(0.1, 2.0, n)
+    _, g = G.loss_grad(raw, w, wt)
+    eps = 1e-6
+    for i in range(n):
+        for j in range(G.N_OUT):
+            r2, r3 = raw.copy(), raw.copy()
+            r2[i, j] += eps
+            r3[i, j] -= eps
+            fd = (G.loss_grad(r2, w, wt)[0] - G.loss_grad(r3, w, wt)[0]) / (2 * eps)
+            assert abs(fd - g[i, j]) <= 1e-5 * max(1e-2, abs(fd)), (i, j, fd, g[i, j])
+
+
+def _sphere_points(rng, n):
+    z = rng.uniform(-1, 1, n)
+    ph = rng.uniform(0, 2 * np.pi, n)
+    r = np.sqrt(1 - z * z)
+    return np.stack([r * np.cos(ph), r * np.sin(ph), z], 1)
+
+
+def _strong_mixture(rng):
+    raw = rng.normal(0, 1.5, G.N_OUT)
+    raw.reshape(G.LOBES, G.LOBE_OUT)[:, 4] += 2.0      # concentrated
+    raw.reshape(G.LOBES, G.LOBE_OUT)[:, 5:8] *= 8.0    # strongly anisotropic
+    return raw
+
+
+def test_oracle_mixture_density_integrates_to_one():
+    rng = np.random.default_rng(1)
+    for _ in range(3):
+        raw = _strong_mixture(rng)
+        wu = _sphere_points(rng, 1_000_000)
+        q = G.mixture_pdf(np.broadcast_to(raw, (len(wu), G.N_OUT)), wu)
+        total = 4 * np.pi * q.mean()
+        se = 4 * np.pi * q.std() / np.sqrt(len(wu))
+        assert abs(total - 1.0) <= 4 * se + 1e-3, (total, se)
+
+
+def test_oracle_sampler_draws_from_the_density():
+    """Moments of sampled directions against the same moments of the density
+    (uniform sphere points weighted by q): z-scores within 4."""
+    rng = np.random.default_rng(2)
+    for _ in range(2):
+        raw = _strong_mixture(rng)
+        ws = G.sample_mixture(np.broadcast_to(raw, (40000, G.N_OUT)), rng.random((40000, 4)))
+        wu = _sphere_points(rng, 1_000_000)
+        qu = G.mixture_pdf(np.broadcast_to(raw, (len(wu), G.N_OUT)), wu)
+        for f in (lambda v: v[:, 0], lambda v: v[:, 1], lambda v: v[:, 2], lambda v: v[:, 0] * v[:, 1],
+                  lambda v: v[:, 2] ** 2, lambda v: v[:, 0] * v[:, 2]):
+            a, sa = f(ws).mean(), f(ws).std() / np.sqrt(len(ws))
+            b = 4 * np.pi * np.mean(qu * f(wu))
+            sb = 4 * np.pi * np.std(qu * f(wu)) / np.sqrt(len(wu))
+            assert abs(a - b) <= 4 * np.hypot(sa, sb)
+
+
 def test_flat_layout_round_trip():
     p = G.init_params(5)
     flat = G.flatten(p)

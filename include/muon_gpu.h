@@ -401,7 +401,7 @@ typedef struct MuonGuideConfig {
   int32_t pool_capacity;    /* training samples kept, newest first (0: 2^22)       */
   float learning_rate;      /* Adam step size (0: 1e-3)                            */
   float mixture_fraction;   /* probability that a guided ray samples the mixture
-                               rather than the BRDF (0: 0.9 with MUON_GUIDE_DIRECT,
+                               rather than the BRDF (0: 0.95 with MUON_GUIDE_DIRECT,
                                0.5 with MUON_GUIDE_ALL)                            */
   int32_t targets;          /* MUON_GUIDE_DIRECT or MUON_GUIDE_ALL                 */
   int32_t reserved;         /* 0                                                   */

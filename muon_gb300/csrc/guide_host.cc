@@ -38,7 +38,7 @@ void Defaults(MuonGuideConfig *c) {
   if (c->pool_capacity <= 0) c->pool_capacity = 1 << 22;
   if (!(c->learning_rate > 0.0f)) c->learning_rate = 1e-3f;
   if (!(c->mixture_fraction > 0.0f) || c->mixture_fraction > 1.0f)
-    c->mixture_fraction = c->targets == MUON_GUIDE_DIRECT ? 0.9f : 0.5f;
+    c->mixture_fraction = c->targets == MUON_GUIDE_DIRECT ? 0.95f : 0.5f;
 }
 
 // Scene box from the BVH root's two child boxes.

@@ -60,7 +60,7 @@ int CheckInferenceStatus(const MuonGuide *g) {
   int32_t v = 0;
   CUDA_TRY(cudaMemcpyAsync(&v, g->status.ptr, sizeof(v), cudaMemcpyDeviceToHost, g->view.stream));
   CUDA_TRY(cudaStreamSynchronize(g->view.stream));
-  if (v != 0) return Fail(MUON_ERR_CUDA, "guide inference: a tensor-core wait timed out");
+  if (v != 0) return Fail(MUON_ERR_TIMEOUT, "guide inference: a tensor-core wait timed out");
   return MUON_OK;
 }
 

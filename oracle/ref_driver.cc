@@ -22,11 +22,23 @@
 //     generator before tiles and the path tracer are seeded.
 //     Output: int32 w, h, spp, then w*h*3 doubles of sums and of sums of
 //     squares, then uint64 primary, secondary, object tests, bounds tests.
+//
+//   ref_driver pixels scene.muon pixels.bin out.bin spp seed
+//     The scene's integrator (reseeded as by `render`) traced spp times
+//     through each listed pixel (int32 x, y pairs): sample 0 at the pixel
+//     centre, later ones jittered in the pixel (muon/sampling.cc:89-107) with
+//     an mt19937 of `seed` (the jitter sequence is the driver's own: only the
+//     distribution of sample positions matters). For converged values of a
+//     pixel subset of a large frame. Output: int32 n, spp, then n*3 doubles of
+//     sums and n*3 of sums of squares.
+#include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <fstream>
+#include <limits>
 #include <map>
+#include <random>
 #include <string>
 #include <vector>
 
@@ -93,18 +105,61 @@ int Hits(const char *scene, const char *out_path, bool linear) {
   return 0;
 }
 
+// Re-seeds as if the file had said `random_seed <seed>` before the
+// integrator line: a fresh path-tracer RNG and tile seeds.
+void Reseed(muon::SceneConfig &sc, long long seed) {
+  if (seed < 0) return;
+  sc.scene->seedgen = std::make_unique<muon::SeedGenerator>(static_cast<unsigned int>(seed));
+  if (dynamic_cast<muon::PathTracer *>(sc.integrator_prototype.get())) {
+    sc.integrator_prototype = std::make_unique<muon::PathTracer>(*sc.scene, sc.scene->seedgen->Next());
+  }
+}
+
+int Pixels(const char *scene, const char *pix_path, const char *out_path, int spp, long long seed) {
+  std::ifstream pin(pix_path, std::ios::binary);
+  std::vector<int32_t> pix;
+  int32_t v;
+  while (pin.read(reinterpret_cast<char *>(&v), sizeof(v))) pix.push_back(v);
+  const size_t n = pix.size() / 2;
+  muon::Options options = MakeOptions(false);
+  muon::Parser parser(scene, options);
+  muon::SceneConfig sc = parser.Parse();
+  Reseed(sc, seed);
+  std::unique_ptr<muon::Integrator> integrator = sc.integrator_prototype->Clone();
+  integrator->Init();
+  std::mt19937 jitter(static_cast<unsigned int>(seed < 0 ? 0 : seed) ^ 0x9e3779b9u);
+  std::uniform_real_distribution<float> u01(0.0f, 1.0f);
+  std::vector<double> sum(3 * n, 0.0), sq(3 * n, 0.0);
+  for (size_t i = 0; i < n; ++i) {
+    const float px = static_cast<float>(pix[2 * i]), py = static_cast<float>(pix[2 * i + 1]);
+    for (int k = 0; k < spp; ++k) {
+      float x = px + 0.5f, y = py + 0.5f;
+      if (k > 0) {
+        x = px + u01(jitter);
+        y = py + u01(jitter);
+        if (x == px + 1.0f) x = std::nextafter(x, -std::numeric_limits<float>::infinity());
+        if (y == py + 1.0f) y = std::nextafter(y, -std::numeric_limits<float>::infinity());
+      }
+      glm::vec3 c = integrator->Trace(sc.scene->camera->CastRay(x, y));
+      for (int q = 0; q < 3; ++q) {
+        sum[3 * i + q] += c[q];
+        sq[3 * i + q] += static_cast<double>(c[q]) * c[q];
+      }
+    }
+  }
+  std::ofstream out(out_path, std::ios::binary);
+  int32_t head[2] = {static_cast<int32_t>(n), spp};
+  out.write(reinterpret_cast<const char *>(head), sizeof(head));
+  out.write(reinterpret_cast<const char *>(sum.data()), sum.size() * sizeof(double));
+  out.write(reinterpret_cast<const char *>(sq.data()), sq.size() * sizeof(double));
+  return 0;
+}
+
 int Render(const char *scene, const char *out_path, int spp_override, long long seed) {
   muon::Options options = MakeOptions(false);
   muon::Parser parser(scene, options);
   muon::SceneConfig sc = parser.Parse();
-  if (seed >= 0) {
-    // Re-seed as if the file had said `random_seed <seed>` before the
-    // integrator line: a fresh path-tracer RNG and tile seeds.
-    sc.scene->seedgen = std::make_unique<muon::SeedGenerator>(static_cast<unsigned int>(seed));
-    if (dynamic_cast<muon::PathTracer *>(sc.integrator_prototype.get())) {
-      sc.integrator_prototype = std::make_unique<muon::PathTracer>(*sc.scene, sc.scene->seedgen->Next());
-    }
-  }
+  Reseed(sc, seed);
   if (spp_override > 0) sc.scene->pixel_samples = spp_override;
   const int w = sc.scene->width, h = sc.scene->height, spp = sc.scene->pixel_samples;
   std::vector<double> sum(3 * static_cast<size_t>(w) * h, 0.0), sq(sum.size(), 0.0);
@@ -148,6 +203,9 @@ int main(int argc, char **argv) {
     long long seed = argc > 5 ? std::atoll(argv[5]) : -1;
     return Render(argv[2], argv[3], spp, seed);
   }
-  std::fprintf(stderr, "usage: ref_driver hits|render scene.muon out.bin ...\n");
+  if (argc >= 7 && std::string(argv[1]) == "pixels") {
+    return Pixels(argv[2], argv[3], argv[4], std::atoi(argv[5]), std::atoll(argv[6]));
+  }
+  std::fprintf(stderr, "usage: ref_driver hits|render|pixels scene.muon ...\n");
   return 2;
 }

@@ -15,6 +15,13 @@ muon_gb300.scenes and stores small .npz files next to this script:
                    z-tests, free of the correlation between runs that the
                    reference's unseeded first tile (muon/sampling.cc:41-46)
                    puts into pt_<name>.npz
+  pt65k_subset_slit_room.npz
+                   256 seeded pixels of the 1024x1024 guiding scene (slit
+                   room, depth 10) at 65,536 spp each (8 processes of 8,192
+                   with distinct seeds): the converged values that the GPU's
+                   full-frame reference of the guiding benchmark, and guided
+                   renders, are z-tested against; the scene is regenerated
+                   from the stored generator arguments
 
 Usage: python tests/golden/make_fixtures.py [--only NAME ...]
 Requires the reference sources (to build oracle/_ref); the GPU machine only reads
@@ -155,6 +162,42 @@ def pt65k(names: list[str]) -> None:
             print(line, flush=True)
 
 
+SUBSET = {"width": 1024, "height": 1024, "spp": 16, "max_depth": 10, "seed": 1, "pixels": 256, "pixel_seed": 7,
+          "processes": 8, "spp_per_process": 8192}
+
+
+def _subset_run(args) -> tuple[np.ndarray, np.ndarray]:
+    scene_path, pix_path, seed = args
+    with tempfile.TemporaryDirectory() as td:
+        out = os.path.join(td, "o.bin")
+        subprocess.run([DRIVER, "pixels", scene_path, pix_path, out, str(SUBSET["spp_per_process"]), str(seed)],
+                       check=True)
+        raw = open(out, "rb").read()
+    n = int(np.frombuffer(raw, np.int32, 1)[0])
+    vals = np.frombuffer(raw, np.float64, offset=8)
+    return vals[:3 * n].reshape(n, 3), vals[3 * n:6 * n].reshape(n, 3)
+
+
+def pt65k_subset() -> None:
+    c = SUBSET
+    text = scenes.slit_room(c["width"], c["height"], c["spp"], c["max_depth"], seed=c["seed"])
+    rng = np.random.default_rng(c["pixel_seed"])
+    flat = rng.choice(c["width"] * c["height"], size=c["pixels"], replace=False)
+    pix = np.stack([flat % c["width"], flat // c["width"]], 1).astype(np.int32)
+    with tempfile.TemporaryDirectory() as td:
+        sp, pp = os.path.join(td, "s.muon"), os.path.join(td, "p.bin")
+        open(sp, "w").write(text)
+        pix.tofile(pp)
+        with ThreadPoolExecutor(max_workers=c["processes"]) as ex:
+            res = list(ex.map(_subset_run, [(sp, pp, 2000 + i) for i in range(c["processes"])]))
+    sums = sum(r[0] for r in res)
+    sqs = sum(r[1] for r in res)
+    spp = c["processes"] * c["spp_per_process"]
+    np.savez_compressed(os.path.join(HERE, "pt65k_subset_slit_room.npz"), pixels=pix, sum=sums, sum_sq=sqs,
+                        spp=np.int32(spp), generator=np.array(str(c)))
+    print(f"pt65k_subset_slit_room: {len(pix)} px x {spp} spp, mean {np.nanmean(sums) / spp:.6f}")
+
+
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--only", nargs="*")
@@ -170,6 +213,8 @@ def main() -> None:
         if not a.only or ("img_" + name) in a.only:
             img(name)
     pt65k([name for name in PT_SCENES if not a.only or ("pt65k_" + name) in a.only])
+    if not a.only or "pt65k_subset_slit_room" in a.only:
+        pt65k_subset()
 
 
 if __name__ == "__main__":

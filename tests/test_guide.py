@@ -263,3 +263,59 @@ def test_trained_guide_lowers_variance(lib):
           f"plain {mp.mean():.5f} ({(mg.mean() - mp.mean()) / se:+.2f} se)")
     assert ratio < 0.75
     assert abs(mg.mean() - mp.mean()) <= 4 * se
+
+
+@pytest.mark.gpu
+def test_guiding_scene_matches_reference_pixel_subset(lib):
+    """The guiding benchmark's scene (slit room, 1024x1024, depth 10), plain
+    and guided, z-tested per pixel against 256 seeded pixels that the
+    reference build rendered at 65,536 spp each (pt65k_subset_slit_room.npz,
+    make_fixtures.py). The plain render stands for the full-frame image the
+    benchmark measures RMSE against; the guided one is the estimator the
+    benchmark times, on the scene it is timed on."""
+    import ast
+
+    import torch
+    from conftest import GOLDEN
+
+    fx = np.load(f"{GOLDEN}/pt65k_subset_slit_room.npz")
+    gen = ast.literal_eval(str(fx["generator"]))
+    scene = m.Scene.from_string(scenes.slit_room(gen["width"], gen["height"], gen["spp"], gen["max_depth"],
+                                                 seed=gen["seed"]))
+    h, w = scene.height, scene.width
+    px, py = fx["pixels"][:, 0], fx["pixels"][:, 1]
+    n_ref = float(fx["spp"])
+    mean_r = fx["sum"] / n_ref
+    se2_r = np.maximum(fx["sum_sq"] / n_ref - mean_r ** 2, 0) * n_ref / (n_ref - 1) / n_ref
+
+    def film():
+        return [torch.zeros((h, w, 3), dtype=torch.float64, device="cuda"),
+                torch.zeros((h, w, 3), dtype=torch.float64, device="cuda"),
+                torch.zeros((h, w), dtype=torch.int32, device="cuda")]
+
+    def check(f, label):
+        s, q, c = (x.cpu().numpy()[py, px] for x in f)
+        c = c[:, None].astype(np.float64)
+        mean_g = s / c
+        se2_g = np.maximum(q / c - mean_g ** 2, 0) * c / (c - 1) / c
+        z = (mean_g - mean_r) / np.sqrt(se2_g + se2_r + 1e-30)
+        frac = (np.abs(z) > 4).mean()
+        se = 1.6 * np.sqrt(se2_g.sum() + se2_r.sum()) / mean_g.size
+        diff = mean_g.mean() - mean_r.mean()
+        print(f"{label}: |z|>4 on {frac * 100:.2f}% of pixel channels, subset mean gpu {mean_g.mean():.5f} "
+              f"ref {mean_r.mean():.5f} ({diff / se:+.2f} se)")
+        assert frac <= 0.02
+        assert abs(diff) <= 4 * se
+
+    plain = film()
+    scene.render_device(scene.params(pixel_samples=1024, seed=31), *[x.data_ptr() for x in plain])
+    check(plain, "plain")
+    guide = m.Guide(scene, seed=3)
+    warm = film()
+    for it in range(2):
+        guide.render_device(scene.params(pixel_samples=16, seed=40 + it, sample_offset=16 * it,
+                                         flags=native.RENDER_ACCUMULATE if it else 0), *[x.data_ptr() for x in warm])
+        guide.train(48)
+    guided = film()
+    guide.render_device(scene.params(pixel_samples=1024, seed=32), *[x.data_ptr() for x in guided])
+    check(guided, "guided")

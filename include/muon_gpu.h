@@ -425,6 +425,12 @@ int muon_gpu_guide_train(MuonGuide *guide, int32_t steps, double *loss);
 /* Network outputs (n x 64 raw values) for features (n x 8), on the
  * tensor-core inference path; host arrays. */
 int muon_gpu_guide_forward(MuonGuide *guide, const float *features, int64_t n, float *out);
+/* Directions drawn from the network's mixture at features (n x 8), one per
+ * row, with the given uniforms in [0, 1) (n x 3), and the mixture density of
+ * each direction (per steradian): the sampling and density a guided render
+ * uses, for inspecting a trained guide and for tests. Host arrays. */
+int muon_gpu_guide_sample(MuonGuide *guide, const float *features, const float *u, int64_t n, float *dirs,
+                          float *pdf);
 /* Gradients (MUON_GUIDE_PARAMS values) of the mean loss over one batch of n
  * samples (features n x 8, unit directions n x 3, weights n) and the loss;
  * host arrays. */

@@ -321,6 +321,17 @@ class Guide:
                                             out.ctypes.data_as(C.POINTER(C.c_float))))
         return out
 
+    def sample(self, features: np.ndarray, u: np.ndarray) -> tuple[np.ndarray, np.ndarray]:
+        """Directions (n x 3) drawn from the mixture at each feature row with
+        uniforms u (n x 3), and their mixture densities (n)."""
+        f = np.ascontiguousarray(features, dtype=np.float32)
+        uu = np.ascontiguousarray(u, dtype=np.float32)
+        dirs = np.zeros((len(f), 3), dtype=np.float32)
+        pdf = np.zeros(len(f), dtype=np.float32)
+        fp = lambda a: a.ctypes.data_as(C.POINTER(C.c_float))
+        check(load().muon_gpu_guide_sample(self._h, fp(f), fp(uu), len(f), fp(dirs), fp(pdf)))
+        return dirs, pdf
+
     def gradients(self, features: np.ndarray, dirs: np.ndarray, weights: np.ndarray) -> tuple[np.ndarray, float]:
         f = np.ascontiguousarray(features, dtype=np.float32)
         d = np.ascontiguousarray(dirs, dtype=np.float32)

@@ -124,6 +124,22 @@ __device__ __forceinline__ void LoadRow(const float *p, float (&v)[T]) {
   }
 }
 
+// ---- sampling the mixture for given network outputs ------------------------------
+__global__ void MixKernel(const float *raw, int n, float *mix) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) MakeMixture(raw + static_cast<int64_t>(i) * kOut, mix + static_cast<int64_t>(i) * kMixFloats);
+}
+
+__global__ void SampleKernel(const float *mix, int n, const float *u, float *dirs, float *pdf) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float *mx = mix + static_cast<int64_t>(i) * kMixFloats;
+  float wx, wy, wz;
+  SampleMixture(mx, u[3 * i], u[3 * i + 1], u[3 * i + 2], &wx, &wy, &wz);
+  dirs[3 * i] = wx, dirs[3 * i + 1] = wy, dirs[3 * i + 2] = wz;
+  pdf[i] = MixturePdf(mx, wx, wy, wz);
+}
+
 // ---- training: forward ----------------------------------------------------------
 // y[b][n] = act(sum_k x[b][k] w[k][n] + bias[n]) for a tile of 64 samples;
 // with kBlob, x is the one-blob encoding of features (batch x 8).
@@ -468,6 +484,13 @@ void LaunchGuideForward(const void *img, const float *features, int n, float *ou
       1, std::min<int64_t>((static_cast<int64_t>(n) + kTcThreads - 1) / kTcThreads, std::max(sms, 1))));
   cudaFuncSetAttribute(ForwardKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmemBytes);
   ForwardKernel<<<grid, kTcThreads, kTcSmemBytes, st>>>(img, features, n, out, status);
+}
+
+void LaunchGuideSample(const float *raw, int n, const float *u, float *mix, float *dirs, float *pdf,
+                       cudaStream_t st) {
+  if (n <= 0) return;
+  MixKernel<<<Grid(n, 256), 256, 0, st>>>(raw, n, mix);
+  SampleKernel<<<Grid(n, 256), 256, 0, st>>>(mix, n, u, dirs, pdf);
 }
 
 size_t GuideTrainBytes(int batch) {

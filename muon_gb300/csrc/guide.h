@@ -75,6 +75,12 @@ void LaunchGuideInit(float *params, uint64_t seed, cudaStream_t st);
 void LaunchGuideForward(const void *img, const float *features, int n, float *out, int32_t *status,
                         cudaStream_t st);
 
+// Directions drawn from the mixtures of network outputs raw (n x 64) with
+// uniforms u (n x 3), and the mixture density of each (guide_mlp.cuh,
+// SampleMixture / MixturePdf); mix is scratch of n x kMixFloats.
+void LaunchGuideSample(const float *raw, int n, const float *u, float *mix, float *dirs, float *pdf,
+                       cudaStream_t st);
+
 // Working memory of one training step over `batch` samples.
 struct GuideTrainBuffers {
   float *h[5];      // inputs of layers 1..4 (h[0] unused: the one-blob input is recomputed), batch x 64

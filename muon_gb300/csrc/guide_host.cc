@@ -22,7 +22,7 @@ struct MuonGuide {
   SceneView view{};
   MuonGuideConfig cfg{};
   DeviceBuffer params, adam_m, adam_v, wt, status, mix, feat, rec, pool, pool_count, train, batch_feat, batch_dir,
-      batch_w, io_in, io_dir, io_w, io_out;
+      batch_w, io_in, io_dir, io_w, io_out, io_mix, io_u, io_pdf;
   GuideDev dev{};
   int step = 0;
   uint64_t batches = 0;
@@ -226,6 +226,37 @@ int muon_gpu_guide_forward(MuonGuide *guide, const float *features, int64_t n, f
     return FailCuda(e);
   }
   return MUON_OK;
+}
+
+int muon_gpu_guide_sample(MuonGuide *guide, const float *features, const float *u, int64_t n, float *dirs,
+                          float *pdf) {
+  if (!guide || n < 0 || (n > 0 && (!features || !u || !dirs || !pdf)) || n > (int64_t(1) << 26))
+    return Fail(MUON_ERR_INVALID_ARG, "bad argument");
+  if (n == 0) return MUON_OK;
+  try {
+    CUDA_TRY(cudaSetDevice(guide->view.device));
+    cudaStream_t st = guide->view.stream;
+    guide->io_in.Ensure(sizeof(float) * n * guide::kFeatures);
+    guide->io_out.Ensure(sizeof(float) * n * guide::kOut);
+    guide->io_mix.Ensure(sizeof(float) * n * guide::kMixFloats);
+    guide->io_u.Ensure(sizeof(float) * n * 3);
+    guide->io_dir.Ensure(sizeof(float) * n * 3);
+    guide->io_pdf.Ensure(sizeof(float) * n);
+    CUDA_TRY(cudaMemcpyAsync(guide->io_in.ptr, features, sizeof(float) * n * guide::kFeatures,
+                             cudaMemcpyHostToDevice, st));
+    CUDA_TRY(cudaMemcpyAsync(guide->io_u.ptr, u, sizeof(float) * n * 3, cudaMemcpyHostToDevice, st));
+    LaunchGuideForward(guide->wt.ptr, guide->io_in.as<float>(), static_cast<int>(n), guide->io_out.as<float>(),
+                       guide->status.as<int32_t>(), st);
+    LaunchGuideSample(guide->io_out.as<float>(), static_cast<int>(n), guide->io_u.as<float>(),
+                      guide->io_mix.as<float>(), guide->io_dir.as<float>(), guide->io_pdf.as<float>(), st);
+    CUDA_TRY(cudaGetLastError());
+    CUDA_TRY(cudaMemcpyAsync(dirs, guide->io_dir.ptr, sizeof(float) * n * 3, cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaMemcpyAsync(pdf, guide->io_pdf.ptr, sizeof(float) * n, cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaStreamSynchronize(st));
+    return CheckInferenceStatus(guide);
+  } catch (const CudaError &e) {
+    return FailCuda(e);
+  }
 }
 
 int muon_gpu_guide_gradients(MuonGuide *guide, const float *features, const float *dirs, const float *weights,

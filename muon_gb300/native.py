@@ -163,6 +163,8 @@ SIGNATURES = {
                                                C.c_void_p]),
     "muon_gpu_guide_train": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_double)]),
     "muon_gpu_guide_forward": (C.c_int, [C.c_void_p, C.POINTER(C.c_float), C.c_int64, C.POINTER(C.c_float)]),
+    "muon_gpu_guide_sample": (C.c_int, [C.c_void_p, C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_int64,
+                                         C.POINTER(C.c_float), C.POINTER(C.c_float)]),
     "muon_gpu_guide_gradients": (C.c_int, [C.c_void_p, C.POINTER(C.c_float), C.POINTER(C.c_float),
                                            C.POINTER(C.c_float), C.c_int32, C.POINTER(C.c_float),
                                            C.POINTER(C.c_double)]),

@@ -319,3 +319,37 @@ def test_guiding_scene_matches_reference_pixel_subset(lib):
     guided = film()
     guide.render_device(scene.params(pixel_samples=1024, seed=32), *[x.data_ptr() for x in guided])
     check(guided, "guided")
+
+
+@pytest.mark.gpu
+def test_gpu_mixture_sampler_and_density_match_oracle(lib):
+    """The GPU's lobe sampling and density (the functions guided renders use,
+    through muon_gpu_guide_sample): with the output layer's weights zeroed
+    and its bias set to a chosen raw vector, every row's mixture is known.
+    The densities the GPU returns match the oracle's at the same directions,
+    and the sampled directions have the oracle density's moments."""
+    guide = m.Guide(tiny_scene(), seed=21)
+    rng = np.random.default_rng(9)
+    for _ in range(2):
+        raw = _strong_mixture(rng)
+        params = G.unflatten(guide.params())
+        params[-1] = (np.zeros_like(params[-1][0]), raw)
+        guide.set_params(G.flatten(params))
+        raw = raw.astype(np.float32).astype(np.float64)
+        n = 200000
+        feat = rng.uniform(0, 1, (n, 8)).astype(np.float32)
+        dirs, pdf = guide.sample(feat, rng.random((n, 3)).astype(np.float32))
+        assert np.allclose(np.linalg.norm(dirs, axis=1), 1.0, atol=1e-5)
+        ref = G.mixture_pdf(np.broadcast_to(raw, (n, G.N_OUT)), dirs.astype(np.float64))
+        rel = np.abs(pdf - ref) / ref
+        print(f"density: median relative error {np.median(rel):.2e}, max {rel.max():.2e}")
+        assert np.median(rel) < 1e-4 and rel.max() < 1e-2
+        wu = _sphere_points(rng, 1_000_000)
+        qu = G.mixture_pdf(np.broadcast_to(raw, (len(wu), G.N_OUT)), wu)
+        d = dirs.astype(np.float64)
+        for f in (lambda v: v[:, 0], lambda v: v[:, 1], lambda v: v[:, 2], lambda v: v[:, 0] * v[:, 1],
+                  lambda v: v[:, 2] ** 2, lambda v: v[:, 0] * v[:, 2]):
+            a, sa = f(d).mean(), f(d).std() / np.sqrt(n)
+            b = 4 * np.pi * np.mean(qu * f(wu))
+            sb = 4 * np.pi * np.std(qu * f(wu)) / np.sqrt(len(wu))
+            assert abs(a - b) <= 4 * np.hypot(sa, sb)

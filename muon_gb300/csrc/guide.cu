@@ -353,17 +353,25 @@ __global__ void __launch_bounds__(kThreads) WgradKernel(const float *x, const fl
   static_assert(K % 4 == 0 && N % 4 == 0, "rows of whole 16-byte vectors");
   __shared__ __align__(16) float xs[32][K];
   __shared__ __align__(16) float ds[32][N];
+  __shared__ float fs[32][kFeatures];  // one-blob input: the slab's features
   const int tid = threadIdx.x;
   const int kg = tid / (N / TN), ng = tid % (N / TN);
   const int b0 = blockIdx.x * kChunk;
   float acc[TK][TN] = {};
   float bacc = 0.0f;
   for (int s0 = b0; s0 < b0 + kChunk && s0 < batch; s0 += 32) {
+    if (kBlob) {
+      for (int i = tid; i < 32 * kFeatures; i += kThreads) {
+        const int r = i / kFeatures, b = s0 + r;
+        fs[r][i % kFeatures] = b < batch ? x[static_cast<int64_t>(b) * kFeatures + i % kFeatures] : 0.0f;
+      }
+      __syncthreads();
+    }
     for (int i = tid; i < 32 * K; i += kThreads) {
       const int r = i / K, k = i % K, b = s0 + r;
       float v = 0.0f;
       if (b < batch) {
-        if (kBlob) v = Blob(x[static_cast<int64_t>(b) * kFeatures + k / kBins], k % kBins);
+        if (kBlob) v = Blob(fs[r][k / kBins], k % kBins);
         else v = x[static_cast<int64_t>(b) * K + k];
       }
       xs[r][k] = v;

@@ -47,6 +47,12 @@ struct GuideDev {
   int32_t mis_slot;
   int32_t direct_only;   // MUON_GUIDE_DIRECT: only the light-hit (MIS) ray is guided and
                          // only light samples train; continuations sample the BRDF
+  // ordered appends of light-sample training samples (per queue entry: its
+  // count and the exclusive scan of the counts; scan scratch)
+  uint32_t *sample_count;
+  uint32_t *sample_off;
+  void *scan_tmp;
+  size_t scan_bytes;
 };
 
 // A path-traced render with guiding (render.cc): the single-scene wavefront
@@ -60,8 +66,13 @@ void LaunchGuideInfer(const DevScene &s, const PathBuffers &b, WaveCounters wc, 
                       const GuideDev &g, cudaStream_t st);
 void LaunchShadePathGuided(const DevScene &s, const WaveInfo &w, const ShadeParams &sp, const PathBuffers &b,
                            WaveCounters wc, int bounce, int bound, const GuideDev &g, cudaStream_t st);
+// The guided fold; on bounces that collect training samples it also appends
+// them to the pool in entry order (a scan of per-entry counts). Throws
+// CudaError.
 void LaunchFoldGuided(const PathBuffers &b, WaveCounters wc, int bounce, int slots, int bound, const GuideDev &g,
                       cudaStream_t st);
+// Scratch bytes of the scan over `capacity` entries.
+size_t GuideScanBytes(int capacity);
 void LaunchGuideCollect(const PathBuffers &b, WaveCounters wc, int bounces, int bound, const GuideDev &g,
                         cudaStream_t st);
 

@@ -22,7 +22,7 @@ struct MuonGuide {
   SceneView view{};
   MuonGuideConfig cfg{};
   DeviceBuffer params, adam_m, adam_v, wt, status, mix, feat, rec, pool, pool_count, train, batch_feat, batch_dir,
-      batch_w, io_in, io_dir, io_w, io_out, io_mix, io_u, io_pdf;
+      batch_w, io_in, io_dir, io_w, io_out, io_mix, io_u, io_pdf, sample_count, sample_off, scan_tmp;
   GuideDev dev{};
   int step = 0;
   uint64_t batches = 0;
@@ -95,6 +95,10 @@ int muon_gpu_guide_create(MuonScene *scene, const MuonGuideConfig *config, MuonG
     if (records) g->rec.Ensure(cap * c.record_bounces * sizeof(GuideRec));
     g->pool.Ensure(static_cast<size_t>(c.pool_capacity) * sizeof(GuideSample));
     g->pool_count.Ensure(sizeof(unsigned long long));
+    g->sample_count.Ensure(cap * sizeof(uint32_t));
+    g->sample_off.Ensure(cap * sizeof(uint32_t));
+    const size_t scan_bytes = GuideScanBytes(c.wave_paths);
+    g->scan_tmp.Ensure(std::max<size_t>(scan_bytes, 16));
     g->train.Ensure(GuideTrainBytes(c.batch));
     g->batch_feat.Ensure(sizeof(float) * c.batch * guide::kFeatures);
     g->batch_dir.Ensure(sizeof(float) * c.batch * 3);
@@ -126,6 +130,10 @@ int muon_gpu_guide_create(MuonScene *scene, const MuonGuideConfig *config, MuonG
     d.pool = g->pool.as<GuideSample>();
     d.pool_count = g->pool_count.as<unsigned long long>();
     d.pool_cap = static_cast<uint32_t>(c.pool_capacity);
+    d.sample_count = g->sample_count.as<uint32_t>();
+    d.sample_off = g->sample_off.as<uint32_t>();
+    d.scan_tmp = g->scan_tmp.ptr;
+    d.scan_bytes = scan_bytes;
     CUDA_TRY(cudaStreamSynchronize(st));
   } catch (const CudaError &e) {
     return FailCuda(e);

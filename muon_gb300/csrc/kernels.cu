@@ -16,7 +16,10 @@
 // reserves the block's range with a single atomicAdd.
 #include <cuda_runtime.h>
 
+#include <cub/device/device_scan.cuh>
+
 #include <algorithm>
+#include <numeric>
 #include <type_traits>
 
 #include "dev_shade.cuh"
@@ -25,6 +28,7 @@
 #include "guide.h"
 #include "guide_mlp.cuh"
 #include "guide_tc.cuh"
+#include "host_cuda.h"
 
 namespace muon_gpu {
 
@@ -905,59 +909,73 @@ __global__ void __launch_bounds__(kBlock, MUON_SHADE_MIN_BLOCKS)
 // weight = luminance of its contribution / throughput, i.e. f cos L_e times
 // the MIS weight over the density it was drawn from. Together with the
 // continuation records (indirect light) these estimate the full incident
-// radiance the mixture learns. Called by whole warps.
-__device__ __forceinline__ void GuideDirectSamples(const PathBuffers &b, const GuideDev &g, int bounce, int slots,
-                                                   int j, bool valid) {
-  const int lane = threadIdx.x & 31;
-  const bool shaded = valid && b.hits[j].y >= 0;
+// radiance the mixture learns. They enter the pool at positions fixed by the
+// bounce, the path and the slot (the fold stores each path's count at
+// Mix(path), an exclusive scan over the wave's paths gives the offsets, then
+// GuideAppendKernel writes), so the pool, and training, are reproducible
+// whatever order the queues hold the paths in. Mix is a fixed permutation of
+// the wave's path indices (p -> a p mod n, a coprime to n, near 0.618 n): the
+// pool keeps the latest samples, and in path (pixel) order those would all
+// come from the bottom of the image.
+__device__ __forceinline__ uint32_t Mix(uint32_t path, uint32_t a, uint32_t n) {
+  return static_cast<uint32_t>((static_cast<uint64_t>(path) * a) % n);
+}
+__device__ __forceinline__ bool GuideSlotKept(const GuideDev &g, const float4 *c, int k) {
+  if (k >= g.area_slots && k != g.mis_slot) return false;
+  const float4 v = c[k];
+  return v.x != 0.0f || v.y != 0.0f || v.z != 0.0f;
+}
+
+__device__ __forceinline__ uint32_t GuideSampleCount(const PathBuffers &b, const GuideDev &g, int slots, int j) {
+  if (b.hits[j].y < 0) return 0;
   const float4 *c = b.contrib + static_cast<int64_t>(j) * slots;
   uint32_t count = 0;
-  if (shaded) {
+  for (int k = 0; k < slots; ++k) count += GuideSlotKept(g, c, k) ? 1u : 0u;
+  return count;
+}
+
+// Writes entry j's training samples from pool position base + off[path of j].
+__global__ void __launch_bounds__(kBlock) GuideAppendKernel(PathBuffers b, WaveCounters wc, int bounce, int slots,
+                                                            GuideDev g, uint32_t mix_a, uint32_t paths) {
+  const int n = static_cast<int>(*wc.count(bounce));
+  const unsigned long long base = *g.pool_count;
+  for (int j = blockIdx.x * kBlock + threadIdx.x; j < n; j += gridDim.x * kBlock) {
+    const uint32_t key = Mix(PathOf(Pick(b.ray_o, bounce & 1)[j].w), mix_a, paths);
+    if (g.sample_count[key] == 0) continue;
+    unsigned long long idx = base + g.sample_off[key];
+    const float4 *c = b.contrib + static_cast<int64_t>(j) * slots;
+    const float4 tp = Pick(b.tp, bounce & 1)[j];
+    const float4 f0 = g.feat[2 * static_cast<int64_t>(j)], f1 = g.feat[2 * static_cast<int64_t>(j) + 1];
+    const float tpc[3] = {tp.x, tp.y, tp.z};
+    const float lum[3] = {0.2126f, 0.7152f, 0.0722f};
     for (int k = 0; k < slots; ++k) {
-      if (k >= g.area_slots && k != g.mis_slot) continue;
+      if (!GuideSlotKept(g, c, k)) continue;
       const float4 v = c[k];
-      if (v.x != 0.0f || v.y != 0.0f || v.z != 0.0f) ++count;
+      const float vc[3] = {v.x, v.y, v.z};
+      float wgt = 0.0f;
+      for (int q = 0; q < 3; ++q)
+        if (tpc[q] > 0.0f) wgt += lum[q] * fmaxf(vc[q], 0.0f) / tpc[q];
+      const float4 dir = b.slot_dir[static_cast<int64_t>(j) * slots + k];
+      GuideSample smp;
+      smp.f0 = f0;
+      smp.f1 = f1;
+      // a non-finite weight becomes 0, which training ignores
+      smp.dir_w = make_float4(dir.x, dir.y, dir.z, isfinite(wgt) ? wgt : 0.0f);
+      g.pool[idx % g.pool_cap] = smp;
+      ++idx;
     }
   }
-  // warp-wide exclusive scan of the counts, one atomic per warp
-  uint32_t incl = count;
-  for (int o = 1; o < 32; o <<= 1) {
-    const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
-    if (lane >= o) incl += y;
-  }
-  const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
-  if (total == 0) return;
-  unsigned long long base = 0;
-  if (lane == 31) base = atomicAdd(g.pool_count, static_cast<unsigned long long>(total));
-  base = __shfl_sync(0xffffffffu, base, 31);
-  if (!count) return;
-  unsigned long long idx = base + (incl - count);
-  const float4 tp = Pick(b.tp, bounce & 1)[j];
-  const float4 f0 = g.feat[2 * static_cast<int64_t>(j)], f1 = g.feat[2 * static_cast<int64_t>(j) + 1];
-  const float tpc[3] = {tp.x, tp.y, tp.z};
-  const float lum[3] = {0.2126f, 0.7152f, 0.0722f};
-  for (int k = 0; k < slots; ++k) {
-    if (k >= g.area_slots && k != g.mis_slot) continue;
-    const float4 v = c[k];
-    if (!(v.x != 0.0f || v.y != 0.0f || v.z != 0.0f)) continue;
-    const float vc[3] = {v.x, v.y, v.z};
-    float wgt = 0.0f;
-    for (int q = 0; q < 3; ++q)
-      if (tpc[q] > 0.0f) wgt += lum[q] * fmaxf(vc[q], 0.0f) / tpc[q];
-    const float4 dir = b.slot_dir[static_cast<int64_t>(j) * slots + k];
-    GuideSample smp;
-    smp.f0 = f0;
-    smp.f1 = f1;
-    // a non-finite weight becomes 0, which training ignores
-    smp.dir_w = make_float4(dir.x, dir.y, dir.z, isfinite(wgt) ? wgt : 0.0f);
-    g.pool[idx % g.pool_cap] = smp;
-    ++idx;
-  }
+}
+
+// Samples ever appended += this bounce's total over the wave's `paths` paths
+// (one thread, after the append).
+__global__ void GuideAdvanceKernel(int paths, GuideDev g) {
+  *g.pool_count += static_cast<unsigned long long>(g.sample_off[paths - 1]) + g.sample_count[paths - 1];
 }
 
 template <bool kGuide>
 __global__ void __launch_bounds__(kBlock) FoldKernel(PathBuffers b, WaveCounters wc, int bounce, int slots,
-                                                     GuideDev g) {
+                                                     GuideDev g, uint32_t mix_a = 1, uint32_t paths = 1) {
   const int n = static_cast<int>(*wc.count(bounce));
   const int cur = bounce & 1, nxt = cur ^ 1;
   for (int base = blockIdx.x * kBlock; base < n; base += gridDim.x * kBlock) {
@@ -981,7 +999,8 @@ __global__ void __launch_bounds__(kBlock) FoldKernel(PathBuffers b, WaveCounters
       if (next >= 0) Pick(b.rad, nxt)[next] = r;
       else b.final_rad[PathOf(Pick(b.ray_o, cur)[j].w)] = r;
     }
-    if (kGuide && bounce < g.rec_bounces) GuideDirectSamples(b, g, bounce, slots, j, j < n);
+    if (kGuide && bounce < g.rec_bounces && j < n)
+      g.sample_count[Mix(PathOf(Pick(b.ray_o, cur)[j].w), mix_a, paths)] = GuideSampleCount(b, g, slots, j);
   }
 }
 
@@ -1357,7 +1376,26 @@ void LaunchShadePathGuided(const DevScene &s, const WaveInfo &w, const ShadePara
 void LaunchFoldGuided(const PathBuffers &b, WaveCounters wc, int bounce, int slots, int bound, const GuideDev &g,
                       cudaStream_t st) {
   if (bound <= 0) return;
-  FoldKernel<true><<<CountedBlocks(bound), kBlock, 0, st>>>(b, wc, bounce, slots, g);
+  // `bound` is the wave's path count: sample counts are kept per path index
+  // (paths without a vertex at this bounce count none)
+  const bool sampling = bounce < g.rec_bounces;
+  const uint32_t paths = static_cast<uint32_t>(bound);
+  uint32_t mix_a = std::max<uint32_t>(1u, static_cast<uint32_t>(0.6180339887 * paths));
+  while (std::gcd(mix_a, paths) != 1u) ++mix_a;
+  if (sampling) CUDA_TRY(cudaMemsetAsync(g.sample_count, 0, sizeof(uint32_t) * bound, st));
+  FoldKernel<true><<<CountedBlocks(bound), kBlock, 0, st>>>(b, wc, bounce, slots, g, mix_a, paths);
+  if (!sampling) return;
+  size_t tmp = g.scan_bytes;
+  CUDA_TRY(cub::DeviceScan::ExclusiveSum(g.scan_tmp, tmp, g.sample_count, g.sample_off, bound, st));
+  GuideAppendKernel<<<CountedBlocks(bound), kBlock, 0, st>>>(b, wc, bounce, slots, g, mix_a, paths);
+  GuideAdvanceKernel<<<1, 1, 0, st>>>(bound, g);
+}
+
+size_t GuideScanBytes(int capacity) {
+  size_t bytes = 0;
+  cub::DeviceScan::ExclusiveSum(nullptr, bytes, static_cast<const uint32_t *>(nullptr), static_cast<uint32_t *>(nullptr),
+                                capacity);
+  return bytes;
 }
 
 void LaunchGuideCollect(const PathBuffers &b, WaveCounters wc, int bounces, int bound, const GuideDev &g,

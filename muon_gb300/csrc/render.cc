@@ -496,6 +496,7 @@ void RenderDevice(MuonScene *sc, const MuonRenderParams &p, double *d_sum, doubl
           if (guided) LaunchFoldGuided(b, wc, k, slots, w.n, guide_local, st);
           else LaunchFold(b, wc, k, slots, w.n, st);
         });
+        if (guided) launches += 2;  // the ordered append of training samples
         if (host_loop) {
           CUDA_TRY(cudaMemcpyAsync(sc->h_counters, wc.count(k + 1), sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
           CUDA_TRY(cudaStreamSynchronize(st));

@@ -378,14 +378,15 @@ int muon_gpu_scene_stream(const MuonScene *scene, void **stream);
 
 /* ---- learned path guiding --------------------------------------------
  * No counterpart in the reference (which has no learned component): a small
- * MLP predicts, per shading point, a mixture of 8 von Mises-Fisher lobes over
- * directions; the path tracer samples it with probability mixture_fraction
- * and its own sampler otherwise, weighting every sample by the combined
- * density, so the estimate stays unbiased whatever the network predicts. The
- * network (one-blob encoded position, normal, outgoing direction and
- * roughness -> 5 layers of 64 -> 40 outputs; BF16 tensor-core inference,
- * FP32 training with Adam) learns online from the radiance samples of the
- * guide's own renders. */
+ * MLP predicts, per shading point, a mixture of 8 anisotropic lobes over
+ * directions (2D Gaussians in the tangent plane of each lobe's mean, projected
+ * to the sphere, plus a small uniform part); the path tracer samples it with
+ * probability mixture_fraction and its own sampler otherwise, weighting every
+ * sample by the combined density, so the estimate stays unbiased whatever the
+ * network predicts. The network (one-blob encoded position, normal, outgoing
+ * direction and roughness -> 5 layers of 64 -> 64 outputs; BF16 tcgen05
+ * tensor-core inference, FP32 training with Adam) learns online from the
+ * radiance samples of the guide's own renders. */
 typedef struct MuonGuide MuonGuide;
 
 /* What the network learns and which rays it guides (MuonGuideConfig.targets). */

@@ -538,7 +538,7 @@ void LaunchGuideGradients(const float *params, const float *features, const floa
   FwdLayerKernel<false, false><<<tiles, kThreads, 0, st>>>(tb.h[4], W(4), B(4), kWidth, kOut, tb.z, batch);
   LossKernel<<<Grid(batch, kThreads), kThreads, 0, st>>>(tb.z, dirs, weights, batch, tb.loss);
   const unsigned chunks = static_cast<unsigned>(tb.chunks);
-  // layer 4: 64 x 40
+  // layer 4: 64 x 64
   WgradKernel<false, kWidth, kOut, 4, 4><<<chunks, kThreads, 0, st>>>(tb.h[4], tb.z, batch, tb.partial, kParams,
                                                                        MasterOffset(4));
   BwdDataKernel<<<tiles, kThreads, 0, st>>>(tb.z, W(4), tb.h[4], kOut, tb.dz[0], batch);

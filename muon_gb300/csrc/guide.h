@@ -81,7 +81,7 @@ void LaunchGuideCollect(const PathBuffers &b, WaveCounters wc, int bounces, int 
 // Writes the inference image (guide_mlp.cuh) of the master copy.
 void LaunchGuidePack(const float *params, void *img, cudaStream_t st);
 void LaunchGuideInit(float *params, uint64_t seed, cudaStream_t st);
-// Network outputs (n x 40) for features (n x 8) on the tensor-core path;
+// Network outputs (n x 64) for features (n x 8) on the tensor-core path;
 // `status` as in GuideDev.
 void LaunchGuideForward(const void *img, const float *features, int n, float *out, int32_t *status,
                         cudaStream_t st);
@@ -95,7 +95,7 @@ void LaunchGuideSample(const float *raw, int n, const float *u, float *mix, floa
 // Working memory of one training step over `batch` samples.
 struct GuideTrainBuffers {
   float *h[5];      // inputs of layers 1..4 (h[0] unused: the one-blob input is recomputed), batch x 64
-  float *z;         // batch x 40 outputs, then their gradients
+  float *z;         // batch x 64 outputs, then their gradients
   float *dz[2];     // batch x 64 gradients (ping-pong)
   float *partial;   // per chunk: all weight and bias gradients
   float *grad;      // guide::kParams

@@ -320,7 +320,7 @@ __device__ __forceinline__ void TcHidden(const TcGroup &g, int l) {
   }
 }
 
-// The network's 40 raw outputs for this thread's features. Every thread of
+// The network's 64 raw outputs for this thread's features. Every thread of
 // the group calls it together; false (on all of them) if a wait gave up.
 __device__ __forceinline__ bool TcForward(TcGroup &g, const float (&f)[kFeatures], float (&out)[kOut]) {
   TcEncode(g, f);

@@ -40,6 +40,18 @@ def test_errors_are_status_codes(lib):
     assert native.MUON_OK == 0
 
 
+def test_guide_and_cache_entry_points_without_a_device(lib):
+    """Null handles are argument errors (no device needed), and releasing the
+    work-array cache is safe when nothing was ever cached."""
+    import ctypes as C
+
+    assert lib.muon_gpu_guide_create(None, None, C.byref(C.c_void_p())) == 1
+    assert lib.muon_gpu_guide_sample(None, None, None, 4, None, None) == 1
+    assert lib.muon_gpu_guide_forward(None, None, 4, None) == 1
+    assert lib.muon_gpu_guide_train(None, 1, None) == 1
+    lib.muon_gpu_release_cached()
+
+
 def test_scene_without_camera_is_a_parse_error(lib):
     import pytest
 

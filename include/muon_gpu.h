@@ -417,7 +417,10 @@ void muon_gpu_guide_destroy(MuonGuide *guide);
 /* Path-traced render of the guide's scene (device film, as
  * muon_gpu_render_device) sampling with the current network; its path
  * vertices become training samples. params->integrator must be the path
- * tracer; params->wave_paths is the guide's. */
+ * tracer; params->wave_paths is the guide's. The tensor-core inference waits
+ * for its matrix units with a bound: if a wait gives up, this call (and
+ * every later render, forward or sample call of the same guide) returns
+ * MUON_ERR_TIMEOUT; destroy the guide. */
 int muon_gpu_guide_render_device(MuonGuide *guide, const MuonRenderParams *params, double *d_sum, double *d_sum_sq,
                                  uint32_t *d_count);
 /* `steps` Adam steps on batches drawn from the collected samples; the mean

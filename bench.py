@@ -49,7 +49,7 @@ WORKLOADS = {
     # learned path guiding: time to RMSE 1e-2 against a converged plain render, guided vs plain
     "guiding": {"workload": "slit_room", "triangles": 1320756 + 10000 + 14, "width": 1024, "height": 1024,
                 "max_depth": 10, "nee": "mis", "importance_sampling": "brdf", "seed": 1, "target_rmse": 1e-2,
-                "reference_spp": 8192, "pass_spp": 16, "train_steps_per_pass": 96, "train_passes": 4,
+                "reference_spp": 8192, "pass_spp": 16, "train_steps_per_pass": 128, "train_passes": 2,
                 "batch": 1 << 18, "guide_targets": "direct", "mixture_fraction": 0.95, "guided_bounces": 4},
     # 64 seeded scenes of uneven size in one batched wavefront
     "batch64": {"workload": "batch64", "scenes": 64, "triangles": "log-uniform 1k-500k per scene",

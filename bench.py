@@ -47,7 +47,7 @@ WORKLOADS = {
     "dense_mesh": {"workload": "dense_mesh", "triangles": 1320756, "width": 1024, "height": 1024, "spp": 256,
                    "max_depth": 10, "nee": "mis", "importance_sampling": "brdf", "seed": 1},
     # learned path guiding: time to RMSE 1e-2 against a converged plain render, guided vs plain
-    "guiding": {"workload": "slit_room", "triangles": 1320756 + 10000 + 14, "width": 1024, "height": 1024,
+    "guiding": {"workload": "slit_room", "triangles": 1310720 + 10000 + 14 + 2, "width": 1024, "height": 1024,
                 "max_depth": 10, "nee": "mis", "importance_sampling": "brdf", "seed": 1, "target_rmse": 1e-2,
                 "reference_spp": 8192, "pass_spp": 16, "train_steps_per_pass": 128, "train_passes": 2,
                 "batch": 1 << 18, "guide_targets": "direct", "mixture_fraction": 0.95, "guided_bounces": 4},

@@ -101,3 +101,16 @@ def test_synthetic_scenes_parse(lib, name):
     ids = sorted([p.desc.triangles[i].prim_id for i in range(p.desc.num_triangles)] +
                  [p.desc.spheres[i].prim_id for i in range(p.desc.num_spheres)])
     assert ids == list(range(len(ids)))
+
+
+def test_benchmark_scenes_have_their_stated_sizes(lib):
+    """The dense-mesh and guiding workloads as bench.py builds them contain
+    the triangle counts its JSON line reports (a level-8 icosphere of
+    1,310,720 triangles plus 10,000 clutter triangles, in the box or the
+    slit room) and one quad light each."""
+    import bench
+
+    for name, make in [("dense_mesh", scenes.dense_mesh), ("guiding", scenes.slit_room)]:
+        p = parse(make(64, 64, 1, 10))
+        assert p.desc.num_triangles == bench.WORKLOADS[name]["triangles"], name
+        assert p.desc.num_spheres == 0 and p.desc.num_lights == 1

@@ -114,3 +114,7 @@ def test_benchmark_scenes_have_their_stated_sizes(lib):
         p = parse(make(64, 64, 1, 10))
         assert p.desc.num_triangles == bench.WORKLOADS[name]["triangles"], name
         assert p.desc.num_spheres == 0 and p.desc.num_lights == 1
+    # the headline: 512 spheres, a ground quad and the 2x2 quad light (2 triangles each)
+    p = parse(scenes.sphere_field(64, 64, 1, 8))
+    assert p.desc.num_spheres == bench.WORKLOADS["sphere_field"]["spheres"] == 512
+    assert p.desc.num_triangles == 4 and p.desc.num_lights == 1

@@ -118,3 +118,18 @@ def test_benchmark_scenes_have_their_stated_sizes(lib):
     p = parse(scenes.sphere_field(64, 64, 1, 8))
     assert p.desc.num_spheres == bench.WORKLOADS["sphere_field"]["spheres"] == 512
     assert p.desc.num_triangles == 4 and p.desc.num_lights == 1
+
+
+def test_batch_scenes_follow_their_distribution(lib):
+    """Every 8th scene of the 64-scene batch: triangle count within
+    [1000, 500000] beyond the Cornell box's 36, a square resolution from
+    {128, 256, 512, 1024}, spp in 4..64, max depth in 4..10 (what bench.py
+    reports for the batch workload)."""
+    import bench
+
+    for i in range(0, bench.WORKLOADS["batch64"]["scenes"], 8):
+        p = parse(scenes.batch_scene(i, bench.WORKLOADS["batch64"]["seed"]))
+        d, r = p.desc, p.params
+        assert 1000 <= d.num_triangles - 36 <= 500_000, (i, d.num_triangles)
+        assert d.width == d.height and d.width in (128, 256, 512, 1024)
+        assert 4 <= r.pixel_samples <= 64 and 4 <= r.max_depth <= 10

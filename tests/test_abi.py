@@ -60,3 +60,45 @@ def test_scene_without_camera_is_a_parse_error(lib):
     with pytest.raises(m.MuonError) as e:
         m.parse_string("film_size 4 4\nsphere 0 0 0 1\n")
     assert e.value.code == 5
+
+
+def test_header_compiles_and_links_as_c(lib, tmp_path):
+    """include/muon_gpu.h is a C ABI: a C99 program includes it, links
+    against libmuon_gpu.so and runs the host-only parsing calls."""
+    import os
+    import shutil
+    import subprocess
+
+    if shutil.which("gcc") is None:
+        import pytest
+        pytest.skip("no C compiler")
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    libdir = os.path.join(root, "muon_gb300", "lib")
+    src = tmp_path / "t.c"
+    src.write_text(r"""
+#include <stdio.h>
+#include <string.h>
+#include "muon_gpu.h"
+int main(void) {
+  const char *text = "film_size 8 4\nintegrator pathtracer\ncamera 0 0 5  0 0 0  0 1 0  45\n"
+                     "quad_light -1 3 -1  0 0 2  2 0 0  5 5 5\nsphere 0 0 0 1\n";
+  MuonParsedScene *ps = NULL;
+  MuonSceneDesc desc;
+  MuonRenderParams params;
+  if (muon_parse_scene_string(text, ".", &ps) != MUON_OK) return 1;
+  if (muon_parsed_scene_desc(ps, &desc, &params) != MUON_OK) return 2;
+  if (desc.width != 8 || desc.height != 4 || desc.num_spheres != 1 || desc.num_lights != 1) return 3;
+  if (params.integrator != MUON_INTEGRATOR_PATHTRACER) return 4;
+  muon_parsed_scene_free(ps);
+  if (muon_gpu_render(NULL, NULL, NULL) != MUON_ERR_INVALID_ARG) return 5;
+  if (strlen(muon_gpu_last_error()) == 0) return 6;
+  puts("ok");
+  return 0;
+}
+""")
+    exe = tmp_path / "t"
+    subprocess.run(["gcc", "-std=c99", "-Wall", "-Werror", str(src), "-I", os.path.join(root, "include"),
+                    "-L", libdir, "-lmuon_gpu", "-Wl,-rpath," + libdir, "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], capture_output=True, text=True)
+    assert out.returncode == 0, out.returncode
+    assert out.stdout.strip() == "ok"

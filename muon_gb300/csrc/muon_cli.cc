@@ -13,6 +13,12 @@
 
 namespace {
 
+const char kUsage[] =
+    "usage: muon --scene=FILE [--output=FILE] [--acceleration=bvh|linear]\n"
+    "            [--partition_strategy=sah|midpoint|uniform] [--parallelism=N] [--stats[=true|false]]\n"
+    "            [--samples=N] [--seed=N] [--intersect_mode=exact|fast|watertight]\n"
+    "Renders a .muon scene on the GPU and writes its film (PNG or PPM).\n";
+
 bool Flag(const char *arg, const char *name, std::string *value) {
   size_t n = std::strlen(name);
   if (std::strncmp(arg, name, n) != 0) return false;
@@ -42,13 +48,20 @@ int main(int argc, char **argv) {
     else if (Flag(argv[i], "--samples", &v)) samples = v;
     else if (Flag(argv[i], "--seed", &v)) seed = v;
     else if (Flag(argv[i], "--intersect_mode", &v)) tri = v;
-    else {
-      std::fprintf(stderr, "unknown flag %s\n", argv[i]);
+    else if (Flag(argv[i], "--help", &v) || Flag(argv[i], "-h", &v)) {
+      std::fputs(kUsage, stdout);
+      return 0;
+    } else {
+      std::fprintf(stderr, "unknown flag %s\n%s", argv[i], kUsage);
       return 1;
     }
   }
   if (scene.empty()) {
-    std::fprintf(stderr, "A scene file is required\n");
+    std::fprintf(stderr, "A scene file is required\n%s", kUsage);
+    return 1;
+  }
+  if (tri != "exact" && tri != "fast" && tri != "watertight") {
+    std::fprintf(stderr, "unknown value for intersect_mode\n");
     return 1;
   }
   auto t_start = std::chrono::steady_clock::now();

@@ -133,3 +133,29 @@ def test_batch_scenes_follow_their_distribution(lib):
         assert 1000 <= d.num_triangles - 36 <= 500_000, (i, d.num_triangles)
         assert d.width == d.height and d.width in (128, 256, 512, 1024)
         assert 4 <= r.pixel_samples <= 64 and 4 <= r.max_depth <= 10
+
+
+def test_cli_arguments(tmp_path):
+    """The `muon` CLI (the reference's flags): usage, and the errors it
+    reports before touching the GPU."""
+    import os
+    import subprocess
+
+    cli = os.path.join(os.path.dirname(m.__file__), "lib", "muon")
+    run = lambda *a: subprocess.run([cli, *a], capture_output=True, text=True)
+    r = run("--help")
+    assert r.returncode == 0 and "usage: muon --scene=FILE" in r.stdout
+    r = run()
+    assert r.returncode == 1 and "scene file is required" in r.stderr
+    r = run("--bogus")
+    assert r.returncode == 1 and "unknown flag --bogus" in r.stderr
+    r = run("--scene=" + str(tmp_path / "missing.muon"))
+    assert r.returncode == 1 and "parse failed" in r.stderr
+    scene = tmp_path / "s.muon"
+    scene.write_text(scenes.cornell(8, 8, 1, 2, 1))
+    r = run("--scene=" + str(scene), "--acceleration=octree")
+    assert r.returncode == 1 and "unknown value for acceleration" in r.stderr
+    r = run("--scene=" + str(scene), "--partition_strategy=random")
+    assert r.returncode == 1 and "unknown value for partition_strategy" in r.stderr
+    r = run("--scene=" + str(scene), "--intersect_mode=approximate")
+    assert r.returncode == 1 and "unknown value for intersect_mode" in r.stderr

@@ -159,3 +159,27 @@ def test_cli_arguments(tmp_path):
     assert r.returncode == 1 and "unknown value for partition_strategy" in r.stderr
     r = run("--scene=" + str(scene), "--intersect_mode=approximate")
     assert r.returncode == 1 and "unknown value for intersect_mode" in r.stderr
+
+
+def test_film_tonemap_and_files(tmp_path):
+    """Film::WriteOutput's tone map (mean, pow(1/gamma), clamp to [0, 1], x255
+    truncated) on a synthetic film, and the PNG and PPM files it writes
+    decode to the same bytes."""
+    from muon_gb300 import imageio
+
+    rng = np.random.default_rng(3)
+    h, w = 7, 9
+    count = rng.integers(1, 50, (h, w)).astype(np.uint32)
+    mean = rng.uniform(0, 1.3, (h, w, 3))
+    film = m.FilmResult(mean * count[..., None], mean * mean * count[..., None], count)
+    got = film.tonemap(1.0)
+    want = (np.clip((film.sum / count[..., None]).astype(np.float32), 0, 1) * np.float32(255)).astype(np.uint8)
+    assert np.array_equal(got, want)
+    g22 = film.tonemap(2.2).astype(int)
+    ref = np.clip(np.power((film.sum / count[..., None]).astype(np.float32), np.float32(1 / 2.2)), 0, 1)
+    ref = (ref * np.float32(255)).astype(int)
+    assert np.abs(g22 - ref).max() <= 1 and (g22 != ref).mean() < 0.01  # powf may differ from numpy by an ulp
+    for name in ("f.png", "f.ppm"):
+        path = str(tmp_path / name)
+        film.write(path, 2.2)
+        assert np.array_equal(imageio.read_image(path), film.tonemap(2.2))

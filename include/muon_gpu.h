@@ -311,15 +311,18 @@ int muon_gpu_occluded(MuonScene *scene, const MuonRay *rays, const float *max_di
  * after initialisation: renders like muon_gpu_render_device (path tracer or
  * normals/albedo/depth; same film layout and flags) but takes every byte of
  * working memory from one fixed buffer of MUON_NOALLOC_SCRATCH_BYTES that the
- * library declares statically on each GPU it is loaded on, and calls no
- * cudaMalloc/cudaFree, pinned-host allocation, CUDA graph or event API. The
- * scene must already exist (muon_gpu_scene_create, which does allocate).
+ * library declares statically, and calls no cudaMalloc/cudaFree, pinned-host
+ * allocation, CUDA graph or event API. The scene must already exist
+ * (muon_gpu_scene_create, which does allocate). The buffer is placed on a GPU
+ * when the first scene is created there (CUDA loads the library's modules
+ * lazily; scene creation loads this one) and stays until the process exits;
+ * every call looks up its device address with the scene's device current.
  * Paths in flight per wavefront are limited to what fits in the buffer
  * (about MUON_NOALLOC_SCRATCH_BYTES / (196 + 36 * shadow slots per path));
- * a larger wave_paths is rejected with MUON_ERR_INVALID_ARG. The first call
- * on a device looks up the buffer's device address. All calls share the one
- * buffer: calls whose GPU work overlaps (other streams, scenes or threads)
- * race and corrupt each other's results. muon_gpu_stats is not updated. */
+ * a larger wave_paths is rejected with MUON_ERR_INVALID_ARG. All calls share
+ * the one buffer and find the previous call's data in it: calls whose GPU
+ * work overlaps (other streams, scenes or threads) race and corrupt each
+ * other's results. muon_gpu_stats is not updated. */
 #define MUON_NOALLOC_SCRATCH_BYTES (64u << 20)
 int muon_gpu_render_noalloc(MuonScene *scene, const MuonRenderParams *params, double *d_sum, double *d_sum_sq,
                             uint32_t *d_count);
@@ -444,6 +447,12 @@ int muon_gpu_guide_get_params(const MuonGuide *guide, float *params);
 int muon_gpu_guide_set_params(MuonGuide *guide, const float *params);
 /* Training samples collected so far. */
 int muon_gpu_guide_samples(const MuonGuide *guide, uint64_t *count);
+/* No counterpart in the reference (which has no device waits). Writes the
+ * guide's wait-status word from the host: 1 is what an inference kernel
+ * leaves when one of its tensor-core waits gives up, 0 clears it. Lets a
+ * host (or a test) exercise its MUON_ERR_TIMEOUT handling without making a
+ * device wait run out. */
+int muon_gpu_guide_set_status(MuonGuide *guide, int32_t status);
 
 /* Thread-local description of the last failure on this thread. */
 const char *muon_gpu_last_error(void);

@@ -351,6 +351,11 @@ class Guide:
         v = np.ascontiguousarray(values, dtype=np.float32)
         check(load().muon_gpu_guide_set_params(self._h, v.ctypes.data_as(C.POINTER(C.c_float))))
 
+    def set_status(self, status: int) -> None:
+        """Writes the device wait-status word (1: as a timed-out tensor-core
+        wait leaves it; 0: cleared)."""
+        check(load().muon_gpu_guide_set_status(self._h, status))
+
     def samples(self) -> int:
         n = C.c_uint64()
         check(load().muon_gpu_guide_samples(self._h, C.byref(n)))

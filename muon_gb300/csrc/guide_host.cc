@@ -331,6 +331,18 @@ int muon_gpu_guide_set_params(MuonGuide *guide, const float *params) {
   return MUON_OK;
 }
 
+int muon_gpu_guide_set_status(MuonGuide *guide, int32_t status) {
+  if (!guide) return Fail(MUON_ERR_INVALID_ARG, "null argument");
+  try {
+    CUDA_TRY(cudaSetDevice(guide->view.device));
+    CUDA_TRY(cudaMemcpyAsync(guide->status.ptr, &status, sizeof(status), cudaMemcpyHostToDevice, guide->view.stream));
+    CUDA_TRY(cudaStreamSynchronize(guide->view.stream));
+  } catch (const CudaError &e) {
+    return FailCuda(e);
+  }
+  return MUON_OK;
+}
+
 int muon_gpu_guide_samples(const MuonGuide *guide, uint64_t *count) {
   if (!guide || !count) return Fail(MUON_ERR_INVALID_ARG, "null argument");
   try {

@@ -101,4 +101,59 @@ void BuildLightTris(const std::vector<DevLight> &lights, std::vector<PrimRecord>
 // ShadeParams of a render; returns the shadow slots per path vertex.
 int SetupShade(const MuonRenderParams &p, int num_quad_lights, int num_other_lights, ShadeParams *out);
 
+// How a render cuts the film's samples into wavefronts: pixels in groups of
+// `pix_per_wave`, each group's samples in runs of at most `ns`; wave i is
+// pixel group i / SampleGroups(), sample run i % SampleGroups(). No storage:
+// callers that may not allocate enumerate the waves with At().
+struct WavePlan {
+  int width = 0;
+  int64_t npix = 0;
+  int spp = 1, ns = 1;
+  int64_t pix_per_wave = 1;
+  uint32_t sample_offset = 0;
+  uint64_t seed = 0;
+  int64_t PixelGroups() const { return (npix + pix_per_wave - 1) / pix_per_wave; }
+  int64_t SampleGroups() const { return (spp + ns - 1) / ns; }
+  size_t Count() const { return static_cast<size_t>(PixelGroups() * SampleGroups()); }
+  WaveInfo At(size_t i) const {
+    const int64_t pg = static_cast<int64_t>(i) / SampleGroups(), sg = static_cast<int64_t>(i) % SampleGroups();
+    WaveInfo w{};
+    w.width = width;
+    w.p0 = static_cast<int32_t>(pg * pix_per_wave);
+    w.npix = static_cast<int>(std::min<int64_t>(pix_per_wave, npix - pg * pix_per_wave));
+    w.s0 = static_cast<int>(sg * ns);
+    w.ns = std::min(ns, spp - w.s0);
+    w.n = w.npix * w.ns;
+    w.sample_offset = sample_offset;
+    w.seed = seed;
+    return w;
+  }
+};
+// Wavefronts of at most `budget` paths for a width x height film.
+WavePlan PlanWaves(int width, int height, const MuonRenderParams &p, int64_t budget);
+
+// Bounces a wavefront runs: `traces` is false when Integrator::Trace casts no
+// ray at all (max_depth 0 with lights sampled); `bounded` when the depth is
+// bounded (or the integrator is not the path tracer), so that the launch
+// sequence is fixed; `bounces` is the number of extend passes.
+struct BouncePlan {
+  bool traces = false, bounded = true;
+  int bounces = 0;
+};
+BouncePlan PlanBounces(const MuonRenderParams &p, const ShadeParams &sp);
+
+// Places the static scratch buffer of muon_gpu_render_noalloc on the current
+// device (loading its module) and checks that its address can be taken
+// (noalloc.cu). Scene creation calls it, so that the buffer is taken then and
+// not during a render.
+cudaError_t NoAllocPrepare();
+
+// Bytes of per-wavefront path state per path with `slots` shadow slots (the
+// arrays of PathBuffers, unpadded).
+inline int64_t WorkBytesPerPath(int slots) {
+  return 8 * 16 /* ray_o, ray_d, tp, rad (double-buffered) */ + 8 /* hits */ + 4 /* link */ +
+         16 /* final_rad */ + 16 /* org */ + int64_t(kNumClasses) * 4 /* order */ +
+         int64_t(std::max(slots, 1)) * (16 + 16 + 4) /* contrib, slot_dir, shq */;
+}
+
 }  // namespace muon_gpu

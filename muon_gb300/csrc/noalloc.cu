@@ -11,13 +11,17 @@
 //
 // All working memory of a render (path queues, per-path state, shadow slots,
 // queue counters, counters of work done) is carved out of `g_scratch`, a
-// file-scope device array of kScratchBytes. Every GPU that loads the library
-// holds it until the process exits. Host code cannot use the array's name as
-// a device address, so the first call on each device looks the address up with
-// cudaGetSymbolAddress while that device is current, and caches it.
+// file-scope device array of kScratchBytes. This file is its own module, and
+// CUDA loads modules lazily, so the array is placed on a device when its
+// address is first looked up there: muon_gpu_scene_create does that
+// (NoAllocPrepare), so the 64 MiB is taken when the first scene is created on
+// a device, not during a render, and held until the process exits. Host code
+// cannot use the array's name as a device address, so every call looks the
+// address up with cudaGetSymbolAddress while the scene's device is current
+// (cheap once the module is loaded, and never stale after a context reset).
 //
 // Limits and rules:
-//  * Paths in flight per wavefront are capped by the buffer: at most
+//  * Paths in flight per wavefront are capped by the buffer: at most about
 //    kScratchBytes / (196 + 36 * S) paths, S = shadow slots per path. A
 //    requested wave_paths above that, or a scene whose S leaves room for fewer
 //    than 256 paths, is rejected with MUON_ERR_INVALID_ARG.
@@ -25,16 +29,16 @@
 //    parts that must start at zero are cleared at the start of each call.
 //    Two calls whose work overlaps on the GPU (different streams or scenes,
 //    or other host threads) race on the buffer and corrupt each other.
-//  * No CUDA graph and no CUDA events are used, and counters are read back
-//    into host stack memory, so the call creates no runtime objects.
+//  * No CUDA graph and no CUDA events are used, counters are read back into
+//    host stack memory and the waves are enumerated without storage, so the
+//    call creates no runtime objects and allocates nothing on the host heap.
 #include <cuda_runtime.h>
 
 #include <algorithm>
-#include <cmath>
 #include <cstdint>
-#include <mutex>
 #include <string>
 
+#include "host_cuda.h"
 #include "host_scene.h"
 #include "kernels.cuh"
 #include "scene_access.h"
@@ -43,30 +47,16 @@ namespace muon_gpu {
 namespace {
 
 constexpr size_t kScratchBytes = size_t(64) << 20;  // MUON_NOALLOC_SCRATCH_BYTES
-constexpr int kNoAllocMaxBounces = 256;
-constexpr int kMaxDevices = 64;
+static_assert(kScratchBytes == MUON_NOALLOC_SCRATCH_BYTES, "scratch size of the public header");
 
 static __device__ __align__(256) unsigned char g_scratch[kScratchBytes];
 
-std::mutex g_setup_mutex;
-void *g_scratch_addr[kMaxDevices] = {nullptr};
-
-int Fail(int code, const std::string &msg) {
-  SetLastError(msg);
-  return code;
-}
-
-// Device address of g_scratch on the current device (set-up on first use).
-cudaError_t ScratchAddress(int device, unsigned char **out) {
-  std::lock_guard<std::mutex> lock(g_setup_mutex);
-  if (device < 0 || device >= kMaxDevices) return cudaErrorInvalidDevice;
-  if (!g_scratch_addr[device]) {
-    void *p = nullptr;
-    cudaError_t e = cudaGetSymbolAddress(&p, g_scratch);
-    if (e != cudaSuccess) return e;
-    g_scratch_addr[device] = p;
-  }
-  *out = static_cast<unsigned char *>(g_scratch_addr[device]);
+// Device address of g_scratch on the current device.
+cudaError_t ScratchAddress(unsigned char **out) {
+  void *p = nullptr;
+  cudaError_t e = cudaGetSymbolAddress(&p, g_scratch);
+  if (e != cudaSuccess) return e;
+  *out = static_cast<unsigned char *>(p);
   return cudaSuccess;
 }
 
@@ -84,24 +74,52 @@ struct Carver {
   }
 };
 
-size_t BytesFor(int64_t paths, int slots, int bounces) {
-  Carver c{nullptr};
-  for (int k = 0; k < 8; ++k) c.Take<float4>(paths);  // ray_o, ray_d, tp, rad (x2)
-  c.Take<int2>(paths);
-  c.Take<int32_t>(paths);
-  c.Take<float4>(paths);  // final_rad
-  c.Take<float4>(paths);  // org
+// Lays out every working array of a render of `paths` paths per wave in the
+// buffer at `base` (null: only measures). Returns the bytes used.
+size_t Carve(unsigned char *base, int64_t paths, int slots, int bounces, PathBuffers *b, uint32_t **counters) {
+  Carver c{base};
+  PathBuffers pb{};
+  for (int k = 0; k < 2; ++k) pb.ray_o[k] = c.Take<float4>(paths);
+  for (int k = 0; k < 2; ++k) pb.ray_d[k] = c.Take<float4>(paths);
+  for (int k = 0; k < 2; ++k) pb.tp[k] = c.Take<float4>(paths);
+  for (int k = 0; k < 2; ++k) pb.rad[k] = c.Take<float4>(paths);
+  pb.hits = c.Take<int2>(paths);
+  pb.link = c.Take<int32_t>(paths);
+  pb.final_rad = c.Take<float4>(paths);
+  pb.org = c.Take<float4>(paths);
   const size_t sl = static_cast<size_t>(paths) * std::max(slots, 1);
-  c.Take<float4>(sl);
-  c.Take<float4>(sl);
-  c.Take<uint32_t>(sl);
-  c.Take<int32_t>(static_cast<size_t>(paths) * kNumClasses);
-  c.Take<uint32_t>(WaveCounterWords(bounces));
-  c.Take<unsigned long long>(kNumStats);
+  pb.contrib = c.Take<float4>(sl);
+  pb.slot_dir = c.Take<float4>(sl);
+  pb.shq = c.Take<uint32_t>(sl);
+  pb.order = c.Take<int32_t>(static_cast<size_t>(paths) * kNumClasses);
+  pb.order_cap = static_cast<int32_t>(paths);
+  uint32_t *ctr = c.Take<uint32_t>(WaveCounterWords(bounces));
+  pb.stats = c.Take<unsigned long long>(kNumStats);
+  if (b) *b = pb;
+  if (counters) *counters = ctr;
   return c.used;
 }
 
+// Largest multiple of 256 paths whose arrays fit the buffer (0 if none).
+int64_t Capacity(int slots, int bounces) {
+  int64_t lo = 0, hi = static_cast<int64_t>(kScratchBytes / WorkBytesPerPath(slots)) / 256 + 1;
+  while (lo + 1 < hi) {  // Carve(lo * 256) fits, Carve(hi * 256) does not
+    const int64_t mid = (lo + hi) / 2;
+    if (Carve(nullptr, mid * 256, slots, bounces, nullptr, nullptr) <= kScratchBytes) lo = mid;
+    else hi = mid;
+  }
+  return std::min<int64_t>(lo * 256, kMaxWavePaths);
+}
+
 }  // namespace
+
+// Places the scratch array on the current device (loads this module) and
+// checks that its address can be taken; called when a scene is created.
+cudaError_t NoAllocPrepare() {
+  unsigned char *base = nullptr;
+  return ScratchAddress(&base);
+}
+
 }  // namespace muon_gpu
 
 using namespace muon_gpu;
@@ -112,46 +130,18 @@ extern "C" int muon_gpu_render_noalloc(MuonScene *scene, const MuonRenderParams 
   if (!GetSceneView(scene, &v) || !params || !d_sum || !d_sum_sq || !d_count)
     return Fail(MUON_ERR_INVALID_ARG, "null argument");
   const MuonRenderParams &p = *params;
+  int rc = ValidateParams(p);
+  if (rc != MUON_OK) return rc;
   if (p.integrator != MUON_INTEGRATOR_PATHTRACER && p.integrator != MUON_INTEGRATOR_NORMALS &&
       p.integrator != MUON_INTEGRATOR_ALBEDO && p.integrator != MUON_INTEGRATOR_DEPTH)
-    return Fail(MUON_ERR_INVALID_ARG, "integrator not available on the GPU path");
-  if (p.pixel_samples < 1 || p.max_depth < -1 || p.wave_paths < 0 || p.next_event_estimation < MUON_NEE_OFF ||
-      p.next_event_estimation > MUON_NEE_MIS || p.importance_sampling < MUON_IS_HEMISPHERE ||
-      p.importance_sampling > MUON_IS_BRDF || p.intersect_mode < MUON_ISECT_FAST ||
-      p.intersect_mode > MUON_ISECT_EXACT)
-    return Fail(MUON_ERR_INVALID_ARG, "render parameters out of range");
+    return Fail(MUON_ERR_INVALID_ARG, "integrator not available on the no-allocation path");
   const bool pt = p.integrator == MUON_INTEGRATOR_PATHTRACER;
-  if (pt && p.next_event_estimation != MUON_NEE_OFF && p.light_samples < 1)
-    return Fail(MUON_ERR_INVALID_ARG, "light_samples must be >= 1");
-
-  ShadeParams sp{};
-  sp.integrator = p.integrator;
-  sp.nee = p.next_event_estimation;
-  sp.is_mode = p.importance_sampling;
-  sp.rr = p.russian_roulette;
-  sp.min_depth = p.min_depth;
-  sp.max_trace_depth = p.max_depth < 0 ? -1 : (p.next_event_estimation != MUON_NEE_OFF ? p.max_depth - 1 : p.max_depth);
-  sp.strata = p.light_stratify ? static_cast<int>(std::sqrt(static_cast<double>(p.light_samples))) : 1;
-  sp.per_section = p.light_stratify ? 1 : p.light_samples;
-  sp.per_light = sp.strata * sp.strata * sp.per_section;
-  sp.light_samples = std::max(1, p.light_samples);
-  sp.isect = p.intersect_mode;
-  sp.max_bounces = kNoAllocMaxBounces;
-  int slots = 0;
-  sp.mis_slot = -1;
-  if (pt && p.next_event_estimation != MUON_NEE_OFF) {
-    slots = v.dev->num_lights * sp.per_light + v.dev->num_other_lights;
-    if (p.next_event_estimation == MUON_NEE_MIS) sp.mis_slot = slots++;
-  }
-  sp.slots = slots;
-  const bool traces = !(p.max_depth >= 0 && sp.max_trace_depth < 0);
-  const bool bounded = !pt || sp.max_trace_depth >= 0;
-  const int bounces = !traces ? 0 : (!pt ? 1 : (bounded ? sp.max_trace_depth + 1 : kNoAllocMaxBounces));
+  ShadeParams sp;
+  const int slots = SetupShade(p, v.dev->num_lights, v.dev->num_other_lights, &sp);
+  const BouncePlan bp = PlanBounces(p, sp);
 
   // Paths per wavefront that fit the buffer.
-  int64_t capacity = static_cast<int64_t>(kScratchBytes / (196 + 36 * static_cast<size_t>(std::max(slots, 1))));
-  capacity &= ~int64_t(255);
-  while (capacity > 0 && BytesFor(capacity, slots, bounces) > kScratchBytes) capacity -= 256;
+  const int64_t capacity = Capacity(slots, bp.bounces);
   if (capacity < 256)
     return Fail(MUON_ERR_INVALID_ARG, "scene needs too many shadow slots per path for the fixed scratch buffer");
   if (p.wave_paths > capacity)
@@ -161,35 +151,15 @@ extern "C" int muon_gpu_render_noalloc(MuonScene *scene, const MuonRenderParams 
 
   cudaError_t e = cudaSetDevice(v.device);
   unsigned char *base = nullptr;
-  if (e == cudaSuccess) e = ScratchAddress(v.device, &base);
+  if (e == cudaSuccess) e = ScratchAddress(&base);
   if (e != cudaSuccess) return Fail(MUON_ERR_CUDA, std::string("scratch set-up: ") + cudaGetErrorString(e));
-
-  Carver c{base};
   PathBuffers b{};
-  b.ray_o[0] = c.Take<float4>(budget), b.ray_o[1] = c.Take<float4>(budget);
-  b.ray_d[0] = c.Take<float4>(budget), b.ray_d[1] = c.Take<float4>(budget);
-  b.tp[0] = c.Take<float4>(budget), b.tp[1] = c.Take<float4>(budget);
-  b.rad[0] = c.Take<float4>(budget), b.rad[1] = c.Take<float4>(budget);
-  b.hits = c.Take<int2>(budget);
-  b.link = c.Take<int32_t>(budget);
-  b.final_rad = c.Take<float4>(budget);
-  b.org = c.Take<float4>(budget);
-  const size_t sl = static_cast<size_t>(budget) * std::max(slots, 1);
-  b.contrib = c.Take<float4>(sl);
-  b.slot_dir = c.Take<float4>(sl);
-  b.shq = c.Take<uint32_t>(sl);
-  b.order = c.Take<int32_t>(static_cast<size_t>(budget) * kNumClasses);
-  b.order_cap = static_cast<int32_t>(budget);
-  const size_t stride = WaveCounterWords(bounces);
-  uint32_t *counters = c.Take<uint32_t>(stride);
-  b.stats = c.Take<unsigned long long>(kNumStats);
+  uint32_t *counters = nullptr;
+  Carve(base, budget, slots, bp.bounces, &b, &counters);
 
   cudaStream_t st = v.stream;
-  const int W = v.width, H = v.height;
-  const int64_t npix_total = static_cast<int64_t>(W) * H;
-  const int spp = p.pixel_samples;
-  const int ns = static_cast<int>(std::min<int64_t>(spp, budget));
-  const int64_t pix_per_wave = std::max<int64_t>(1, budget / ns);
+  const WavePlan plan = PlanWaves(v.width, v.height, p, budget);
+  const int64_t npix_total = plan.npix;
   if (!(p.flags & MUON_RENDER_ACCUMULATE)) {
     e = cudaMemsetAsync(d_sum, 0, 3 * npix_total * sizeof(double), st);
     if (e == cudaSuccess) e = cudaMemsetAsync(d_sum_sq, 0, 3 * npix_total * sizeof(double), st);
@@ -200,43 +170,35 @@ extern "C" int muon_gpu_render_noalloc(MuonScene *scene, const MuonRenderParams 
   e = cudaMemsetAsync(b.stats, 0, kNumStats * sizeof(unsigned long long), st);
   if (e != cudaSuccess) return Fail(MUON_ERR_CUDA, std::string("scratch clear: ") + cudaGetErrorString(e));
   const bool stats_on = (p.flags & MUON_RENDER_STATS) != 0;
-  for (int64_t p0 = 0; p0 < npix_total; p0 += pix_per_wave) {
-    for (int s0 = 0; s0 < spp; s0 += ns) {
-      WaveInfo w{};
-      w.width = W;
-      w.p0 = static_cast<int32_t>(p0);
-      w.npix = static_cast<int>(std::min<int64_t>(pix_per_wave, npix_total - p0));
-      w.s0 = s0;
-      w.ns = std::min(ns, spp - s0);
-      w.n = w.npix * w.ns;
-      w.sample_offset = static_cast<uint32_t>(p.sample_offset);
-      w.seed = p.seed;
-      // Queue counters of this wavefront start at zero.
-      e = cudaMemsetAsync(counters, 0, stride * sizeof(uint32_t), st);
-      if (e != cudaSuccess) return Fail(MUON_ERR_CUDA, std::string("scratch clear: ") + cudaGetErrorString(e));
-      WaveCounters wc{counters};
-      LaunchCamera(*v.cam, w, b, wc, st);
-      for (int k = 0; k < bounces; ++k) {
-        LaunchExtend(*v.dev, b, wc, k, w.n, p.intersect_mode, stats_on, st);
-        if (!pt) {
-          LaunchShadeDebug(*v.dev, b, wc, p.integrator, w.n, p.intersect_mode, st);
-          break;
-        }
-        LaunchShadePath(*v.dev, w, sp, b, wc, k, w.n, st);
-        if (slots > 0)
-          LaunchOcclude(*v.dev, b, wc, k, slots, static_cast<int>(std::min<int64_t>(int64_t(w.n) * slots, INT32_MAX)),
-                        p.intersect_mode, stats_on, st);
-        LaunchFold(b, wc, k, slots, w.n, st);
-        if (!bounded) {
-          uint32_t next = 0;  // host stack memory: no pinned allocation
-          e = cudaMemcpyAsync(&next, wc.count(k + 1), sizeof(uint32_t), cudaMemcpyDeviceToHost, st);
-          if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-          if (e != cudaSuccess) return Fail(MUON_ERR_CUDA, cudaGetErrorString(e));
-          if (next == 0) break;
-        }
+  const size_t stride = WaveCounterWords(bp.bounces);
+  const size_t nwaves = plan.Count();
+  for (size_t wi = 0; wi < nwaves; ++wi) {
+    const WaveInfo w = plan.At(wi);
+    // Queue counters of this wavefront start at zero.
+    e = cudaMemsetAsync(counters, 0, stride * sizeof(uint32_t), st);
+    if (e != cudaSuccess) return Fail(MUON_ERR_CUDA, std::string("scratch clear: ") + cudaGetErrorString(e));
+    WaveCounters wc{counters};
+    LaunchCamera(*v.cam, w, b, wc, st);
+    for (int k = 0; k < bp.bounces; ++k) {
+      LaunchExtend(*v.dev, b, wc, k, w.n, p.intersect_mode, stats_on, st);
+      if (!pt) {
+        LaunchShadeDebug(*v.dev, b, wc, p.integrator, w.n, p.intersect_mode, st);
+        break;
       }
-      LaunchFilm(w, b, d_sum, d_sum_sq, d_count, st);
+      LaunchShadePath(*v.dev, w, sp, b, wc, k, w.n, st);
+      if (slots > 0)
+        LaunchOcclude(*v.dev, b, wc, k, slots, static_cast<int>(std::min<int64_t>(int64_t(w.n) * slots, INT32_MAX)),
+                      p.intersect_mode, stats_on, st);
+      LaunchFold(b, wc, k, slots, w.n, st);
+      if (!bp.bounded) {
+        uint32_t next = 0;  // host stack memory: no pinned allocation
+        e = cudaMemcpyAsync(&next, wc.count(k + 1), sizeof(uint32_t), cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) return Fail(MUON_ERR_CUDA, cudaGetErrorString(e));
+        if (next == 0) break;
+      }
     }
+    LaunchFilm(w, b, d_sum, d_sum_sq, d_count, st);
   }
   e = cudaGetLastError();
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);

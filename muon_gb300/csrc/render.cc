@@ -355,6 +355,29 @@ void BuildLightTris(const std::vector<DevLight> &lights, std::vector<PrimRecord>
   }
 }
 
+WavePlan PlanWaves(int width, int height, const MuonRenderParams &p, int64_t budget) {
+  WavePlan wp;
+  wp.width = width;
+  wp.npix = static_cast<int64_t>(width) * height;
+  wp.spp = p.pixel_samples;
+  wp.ns = static_cast<int>(std::min<int64_t>(wp.spp, std::max<int64_t>(budget, 1)));
+  wp.pix_per_wave = std::max<int64_t>(1, budget / wp.ns);
+  wp.sample_offset = static_cast<uint32_t>(p.sample_offset);
+  wp.seed = p.seed;
+  return wp;
+}
+
+BouncePlan PlanBounces(const MuonRenderParams &p, const ShadeParams &sp) {
+  const bool pt = p.integrator == MUON_INTEGRATOR_PATHTRACER;
+  BouncePlan b;
+  // A path traces at depths 0..max_trace_depth; with max_depth 0 and lights
+  // sampled, Trace() casts no ray at all.
+  b.traces = !(p.max_depth >= 0 && sp.max_trace_depth < 0);
+  b.bounded = !pt || sp.max_trace_depth >= 0;  // (the ray tracer runs in one launch)
+  b.bounces = !b.traces ? 0 : (!pt ? 1 : (b.bounded ? sp.max_trace_depth + 1 : sp.max_bounces));
+  return b;
+}
+
 int ValidateParams(const MuonRenderParams &p) {
   if (p.integrator < MUON_INTEGRATOR_NORMALS || p.integrator > MUON_INTEGRATOR_PATHTRACER)
     return Fail(MUON_ERR_INVALID_ARG, "unknown integrator");
@@ -406,33 +429,16 @@ void RenderDevice(MuonScene *sc, const MuonRenderParams &p, double *d_sum, doubl
   const int spp = p.pixel_samples;
   int64_t budget = p.wave_paths > 0 ? p.wave_paths : kDefaultWavePaths;
   // Keep per-wave path state within ~8 GiB.
-  const int64_t per_path = 200 + 36 * static_cast<int64_t>(std::max(slots, 1));
-  budget = std::max<int64_t>(1, std::min<int64_t>(budget, (int64_t(8) << 30) / per_path));
+  budget = std::max<int64_t>(1, std::min<int64_t>(budget, (int64_t(8) << 30) / WorkBytesPerPath(slots)));
   budget = std::min<int64_t>(budget, kMaxWavePaths);
-  const int ns = static_cast<int>(std::min<int64_t>(spp, budget));
-  const int64_t pix_per_wave = std::max<int64_t>(1, budget / ns);
-  std::vector<WaveInfo> waves;
-  for (int64_t p0 = 0; p0 < npix_total; p0 += pix_per_wave) {
-    for (int s0 = 0; s0 < spp; s0 += ns) {
-      WaveInfo w{};
-      w.width = W;
-      w.p0 = static_cast<int32_t>(p0);
-      w.npix = static_cast<int>(std::min<int64_t>(pix_per_wave, npix_total - p0));
-      w.s0 = s0;
-      w.ns = std::min(ns, spp - s0);
-      w.n = w.npix * w.ns;
-      w.sample_offset = static_cast<uint32_t>(p.sample_offset);
-      w.seed = p.seed;
-      waves.push_back(w);
-    }
-  }
-  // A path traces at depths 0..max_trace_depth; with max_depth 0 and lights
-  // sampled, Trace() casts no ray at all.
-  const bool traces = !(p.max_depth >= 0 && sp.max_trace_depth < 0);
-  const bool bounded = !pt || sp.max_trace_depth >= 0;  // (the ray tracer runs in one launch)
-  const int bounces = !traces ? 0 : (!pt ? 1 : (bounded ? sp.max_trace_depth + 1 : kMaxBounces));
+  const WavePlan plan = PlanWaves(W, H, p, budget);
+  std::vector<WaveInfo> waves(plan.Count());
+  for (size_t i = 0; i < waves.size(); ++i) waves[i] = plan.At(i);
+  const BouncePlan bp = PlanBounces(p, sp);
+  const bool traces = bp.traces, bounded = bp.bounded;
+  const int bounces = bp.bounces;
   const size_t stride = WaveCounterWords(bounces);
-  bool moved = sc->EnsureWork(std::min<int64_t>(pix_per_wave, npix_total) * ns, slots);
+  bool moved = sc->EnsureWork(std::min<int64_t>(plan.pix_per_wave, npix_total) * plan.ns, slots);
   moved |= sc->EnsureCounters(stride * waves.size());
   sc->stats.Ensure(sizeof(unsigned long long) * kNumStats);
   PathBuffers b = sc->Buffers();
@@ -747,6 +753,14 @@ int muon_gpu_scene_create(const MuonSceneDesc *desc, MuonScene **out) {
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return Fail(MUON_ERR_CUDA, "no CUDA device available");
     CUDA_TRY(cudaGetDevice(&sc->device));
+    {
+      // muon_gpu_render_noalloc's buffer is taken now, not during its renders
+      const cudaError_t e = NoAllocPrepare();
+      if (e != cudaSuccess) {
+        cudaGetLastError();
+        return Fail(MUON_ERR_CUDA, std::string("no-allocation scratch set-up: ") + cudaGetErrorString(e));
+      }
+    }
     int sms = 0;
     CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, sc->device));
     SetPersistentGrid(sms * 8);

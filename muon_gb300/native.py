@@ -171,6 +171,7 @@ SIGNATURES = {
     "muon_gpu_guide_get_params": (C.c_int, [C.c_void_p, C.POINTER(C.c_float)]),
     "muon_gpu_guide_set_params": (C.c_int, [C.c_void_p, C.POINTER(C.c_float)]),
     "muon_gpu_guide_samples": (C.c_int, [C.c_void_p, C.POINTER(C.c_uint64)]),
+    "muon_gpu_guide_set_status": (C.c_int, [C.c_void_p, C.c_int32]),
 }
 
 _lib = None

@@ -8,7 +8,8 @@ if ROOT not in sys.path:
     sys.path.insert(0, ROOT)
 
 GOLDEN = os.path.join(ROOT, "tests", "golden")
-REFERENCE = "/root/reference"
+# the reference checkout (read by fixture generators only; absent on GPU machines)
+REFERENCE = os.environ.get("MUON_REFERENCE_DIR", "/root/reference")
 
 
 def pytest_configure(config):

@@ -391,3 +391,37 @@ def test_guided_training_is_reproducible(lib):
     assert np.array_equal(p1, p2)
     for a, b in zip(f1, f2):
         assert np.array_equal(a, b)
+
+
+@pytest.mark.gpu
+def test_inference_timeout_status_reaches_the_host(lib):
+    """The host side of a device wait that gave up: the status word an
+    inference kernel sets is written here from the host (no device wait is
+    made to run out). Guided renders and forward passes of that guide then
+    return MUON_ERR_TIMEOUT, destroying it succeeds, and the scene renders
+    with a fresh guide afterwards (the context stays usable)."""
+    import torch
+
+    scene = tiny_scene()
+    h, w = scene.height, scene.width
+    film = [torch.zeros((h, w, 3), dtype=torch.float64, device="cuda"),
+            torch.zeros((h, w, 3), dtype=torch.float64, device="cuda"),
+            torch.zeros((h, w), dtype=torch.int32, device="cuda")]
+    ptrs = [x.data_ptr() for x in film]
+    params = scene.params(pixel_samples=4, seed=3)
+    guide = m.Guide(scene, seed=2, batch=1 << 12, pool_capacity=1 << 16)
+    guide.render_device(params, *ptrs)
+    guide.set_status(1)
+    with pytest.raises(m.MuonError) as e:
+        guide.render_device(params, *ptrs)
+    assert e.value.code == 4 and "timed out" in str(e.value)
+    feat, _, _ = random_batch(256, 9)
+    with pytest.raises(m.MuonError) as e:
+        guide.forward(feat)
+    assert e.value.code == 4
+    guide.close()
+    fresh = m.Guide(scene, seed=2, batch=1 << 12, pool_capacity=1 << 16)
+    fresh.render_device(params, *ptrs)
+    torch.cuda.synchronize()
+    assert np.isfinite(film[0].cpu().numpy()).all() and (film[2].cpu().numpy() == 4).all()
+    fresh.close()

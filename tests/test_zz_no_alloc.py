@@ -48,6 +48,33 @@ def test_noalloc_render_matches_the_allocating_entry_point(lib, integrator):
 
 
 @pytest.mark.gpu
+def test_noalloc_render_leaves_free_device_memory_unchanged(lib):
+    """The property the entry point exists for: once the scene exists (its
+    creation placed the static buffer on the device) and the kernels have
+    run once, rendering through it changes the device's free memory by
+    nothing, on the first call and on the next."""
+    torch = pytest.importorskip("torch")
+    fx = np.load(f"{GOLDEN}/pt_cornell.npz")
+    scene = m.Scene.from_string(str(fx["scene"]))
+    h, w = scene.height, scene.width
+    params = scene.params(pixel_samples=16, seed=5)
+    films = [_device_film(h, w) for _ in range(3)]
+    # loads the rendering kernels (the allocating entry point, its own film)
+    _render(load().muon_gpu_render_device, scene, params, films[0])
+    torch.cuda.synchronize()
+    free_before = torch.cuda.mem_get_info()[0]
+    fn = load().muon_gpu_render_noalloc
+    for s, q, n in films[1:]:
+        check(fn(scene._h, C.byref(params), C.c_void_p(s.data_ptr()), C.c_void_p(q.data_ptr()),
+                 C.c_void_p(n.data_ptr())))
+    torch.cuda.synchronize()
+    assert torch.cuda.mem_get_info()[0] == free_before
+    assert torch.equal(films[1][2], films[0][2]) and torch.equal(films[2][2], films[0][2])
+    assert torch.allclose(films[1][0], films[0][0], rtol=1e-12, atol=0)
+    assert torch.allclose(films[2][0], films[0][0], rtol=1e-12, atol=0)
+
+
+@pytest.mark.gpu
 def test_noalloc_rejects_waves_beyond_its_buffer(lib):
     fx = np.load(f"{GOLDEN}/pt_cornell.npz")
     scene = m.Scene.from_string(str(fx["scene"]))

@@ -330,6 +330,56 @@ int muon_gpu_render_noalloc(MuonScene *scene, const MuonRenderParams *params, do
 /* Counters and device timings of the last render (muon/stats.h:11-44). */
 int muon_gpu_stats(const MuonScene *scene, MuonStats *stats);
 
+/* ---- traversal work measured on the host ------------------------------------
+ * What the reference's TraceStats counts (bounds tests and object tests,
+ * muon/stats.h:11-44, incremented in muon/acceleration.cc:65-202), counted by
+ * walking the flattened BVH that the GPU traverses on the host, in the GPU's
+ * visiting order (nearer hit child first, farther one deferred). These counts
+ * are the measure of work behind a roofline's algorithmic bytes, independent
+ * of the GPU kernels' own counters. */
+typedef struct MuonWalkCounts {
+  uint64_t rays;
+  uint64_t box_tests;  /* child boxes tested: 2 per interior node visited */
+  uint64_t prim_tests; /* primitive records tested                        */
+  uint64_t hits;       /* rays that hit something                         */
+} MuonWalkCounts;
+
+/* Walks n rays (tmax per ray, or NULL for no limit) through the BVH that
+ * muon_gpu_scene_create builds from desc with the host builder: closest hit
+ * (any_hit 0) or any hit. hit_ids (optional) receives per ray the parse-order
+ * id of the primitive hit, or -1. intersect_mode: MUON_ISECT_EXACT or
+ * MUON_ISECT_FAST. Host only: needs no GPU. */
+int muon_walk_rays(const MuonSceneDesc *desc, const MuonRay *rays, const float *tmax, int64_t n, int32_t any_hit,
+                   int32_t intersect_mode, int32_t *hit_ids, MuonWalkCounts *out);
+
+typedef struct MuonTraversalProbe {
+  MuonWalkCounts extend_walked;  /* host walk of the sampled closest-hit rays  */
+  MuonWalkCounts occlude_walked; /* host walk of the sampled shadow rays       */
+  uint64_t extend_rays;          /* rays in every extend queue of the render   */
+  uint64_t occlude_rays;         /* rays in every shadow queue of the render   */
+  /* Estimates for all rays of the render: per (wavefront, bounce) queue, its
+   * length times the mean count of its walked sample. */
+  double extend_box_tests, extend_prim_tests;
+  double occlude_box_tests, occlude_prim_tests;
+} MuonTraversalProbe;
+
+/* Renders as muon_gpu_render does (film discarded, MUON_RENDER_STATS on,
+ * kernel by kernel), copies up to rays_per_queue evenly spaced rays out of
+ * every closest-hit and shadow queue of the render as the traversal kernels
+ * receive them, and walks them on the host through the scene's own BVH and
+ * primitive records (the arrays on the device). Afterwards muon_gpu_stats
+ * holds the GPU kernels' counters of the same render, for comparison.
+ * Path tracer with bounded depth; exact or fast intersection mode. */
+int muon_gpu_probe_traversal(MuonScene *scene, const MuonRenderParams *params, int32_t rays_per_queue,
+                             MuonTraversalProbe *out);
+
+/* Read-bandwidth ceilings of the current device for a roofline, measured by
+ * one kernel: level 0 reads a buffer of `bytes` (at most 64 KiB) from every
+ * block through L1; level 1 reads a buffer of `bytes` that fits in L2 across
+ * the grid, bypassing L1; level 2 reads a buffer larger than L2 across the
+ * grid (DRAM). `passes` repeats inside the launch; GB/s of bytes delivered. */
+int muon_gpu_measure_read_bandwidth(int32_t level, int64_t bytes, int32_t passes, double *gb_per_s);
+
 /* ---- batched rendering -------------------------------------------------
  * Many scenes of uneven size, resolution and sample count rendered by one
  * wavefront: every kernel launch covers paths of all the scenes at once, and

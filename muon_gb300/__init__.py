@@ -59,6 +59,35 @@ class ParsedScene:
             pass
 
 
+def walk_rays(parsed: ParsedScene, origins: np.ndarray, directions: np.ndarray, tmax: np.ndarray | None = None,
+              any_hit: bool = False, intersect_mode: int = native.ISECT_EXACT) -> tuple[np.ndarray, dict]:
+    """Host walk of the scene's BVH (muon_walk_rays, no GPU): per ray the
+    parse-order id of the primitive hit (-1: none), and the traversal counts."""
+    n = len(origins)
+    rays = np.zeros((n, 6), dtype=np.float32)
+    rays[:, :3] = origins
+    rays[:, 3:] = directions
+    tm = None if tmax is None else np.ascontiguousarray(tmax, dtype=np.float32)
+    ids = np.zeros(n, dtype=np.int32)
+    cnt = native.WalkCounts()
+    desc = parsed.desc
+    # the BVH a Scene builds by default: binned SAH on the host
+    desc.acceleration, desc.builder = native.ACCEL_BVH, 0
+    desc.partition_strategy, desc.max_leaf_size = native.PARTITION["sah"], 0
+    check(load().muon_walk_rays(C.byref(desc), rays.ctypes.data_as(C.POINTER(native.Ray)),
+                                None if tm is None else tm.ctypes.data_as(C.POINTER(C.c_float)), n, int(any_hit),
+                                intersect_mode, ids.ctypes.data_as(C.POINTER(C.c_int32)), C.byref(cnt)))
+    return ids, {k: getattr(cnt, k) for k, _ in native.WalkCounts._fields_}
+
+
+def measure_read_bandwidth(level: int, nbytes: int, passes: int) -> float:
+    """GB/s of a read-bandwidth ceiling on the current device: level 0 L1,
+    1 L2, 2 DRAM (muon_gpu_measure_read_bandwidth)."""
+    v = C.c_double()
+    check(load().muon_gpu_measure_read_bandwidth(level, nbytes, passes, C.byref(v)))
+    return v.value
+
+
 def parse_file(path: str) -> ParsedScene:
     h = C.c_void_p()
     check(load().muon_parse_scene_file(path.encode(), C.byref(h)))
@@ -215,6 +244,18 @@ class Scene:
                                        md.ctypes.data_as(C.POINTER(C.c_float)), n, intersect_mode,
                                        out.ctypes.data_as(C.POINTER(C.c_uint8))))
         return out.astype(bool)
+
+    def probe_traversal(self, params: native.RenderParams, rays_per_queue: int = 4096) -> dict:
+        """Traversal work of a render counted by the host walk of sampled
+        queue rays (muon_gpu_probe_traversal); stats() then holds the GPU
+        kernels' own counters of the same render."""
+        pr = native.TraversalProbe()
+        check(load().muon_gpu_probe_traversal(self._h, C.byref(params), rays_per_queue, C.byref(pr)))
+        walked = lambda w: {k: getattr(w, k) for k, _ in native.WalkCounts._fields_}
+        out = {k: getattr(pr, k) for k, _ in native.TraversalProbe._fields_ if not k.endswith("_walked")}
+        out["extend_walked"] = walked(pr.extend_walked)
+        out["occlude_walked"] = walked(pr.occlude_walked)
+        return out
 
     def stats(self) -> dict:
         s = native.Stats()

@@ -23,7 +23,7 @@ CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
 CUDA_UNITS = ["kernels.cu", "noalloc.cu", "guide.cu", "bvh_build.cu"]
 HOST_UNITS = ["scene_parser.cc", "mesh_io.cc", "scene_build.cc", "host_api.cc", "render.cc", "batch.cc",
-              "guide_host.cc"]
+              "guide_host.cc", "bvh_walk.cc"]
 CXXFLAGS = ["-std=c++17", "-O2", "-fPIC", "-ffp-contract=off", "-Wall", "-Wno-unused-function"] + \
     os.environ.get("MUON_CXX_EXTRA", "").split()
 NVFLAGS = [ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off",

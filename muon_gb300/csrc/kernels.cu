@@ -1249,6 +1249,66 @@ void WithMode(int mode, F &&f) {
   else f(std::integral_constant<int, MUON_ISECT_FAST>());
 }
 
+// ---- measurement ---------------------------------------------------------------
+// A sample of one bounce's traversal queue, copied for the host walk that
+// counts traversal work: kind 0 the closest-hit queue, kind 1 the shadow
+// queue. out[0] = (sampled, queue length) as int bits; ray i of the sample
+// (queue entry i * length / sampled) follows as (origin, root), (direction,
+// tmax), i.e. exactly what the traversal kernels load for it.
+__global__ void __launch_bounds__(kBlock) SampleQueueKernel(PathBuffers b, WaveCounters wc, int bounce, int kind,
+                                                            int slots, int m, float4 *out) {
+  const int n = static_cast<int>(kind == 0 ? *wc.count(bounce) : *wc.shadow(bounce));
+  const int taken = min(m, n);
+  if (blockIdx.x == 0 && threadIdx.x == 0) out[0] = make_float4(__int_as_float(taken), __int_as_float(n), 0.0f, 0.0f);
+  for (int i = blockIdx.x * kBlock + threadIdx.x; i < taken; i += gridDim.x * kBlock) {
+    const int j = static_cast<int>((static_cast<int64_t>(i) * n) / taken);
+    float4 o, d;
+    if (kind == 0) {
+      o = Pick(b.ray_o, bounce & 1)[j];
+      d = Pick(b.ray_d, bounce & 1)[j];
+      o.w = d.w;  // root
+      d.w = INFINITY;
+    } else {
+      const uint32_t slot = b.shq[j];
+      o = b.org[slot / slots];  // w: root
+      d = b.slot_dir[slot];     // w: distance to the light sample
+    }
+    out[1 + 2 * static_cast<int64_t>(i)] = o;
+    out[2 + 2 * static_cast<int64_t>(i)] = d;
+  }
+}
+
+// Read-bandwidth ceiling: each pass reads the buffer (n4 float4s) once per
+// block through L1 (level 0), or once across the grid bypassing L1 (levels 1
+// and 2). Four independent accumulators keep loads in flight; the sum is
+// stored only if it equals an impossible value, so the loads stay.
+__global__ void __launch_bounds__(kBlock) ReadBandwidthKernel(const float4 *buf, int64_t n4, int passes, int level,
+                                                              float *sink) {
+  float4 a0 = make_float4(0, 0, 0, 0), a1 = a0, a2 = a0, a3 = a0;
+  const int64_t start = level == 0 ? threadIdx.x : static_cast<int64_t>(blockIdx.x) * kBlock + threadIdx.x;
+  const int64_t step = level == 0 ? kBlock : static_cast<int64_t>(gridDim.x) * kBlock;
+  for (int p = 0; p < passes; ++p) {
+    int64_t i = start;
+    for (; i + 3 * step < n4; i += 4 * step) {
+      const float4 v0 = level == 0 ? __ldg(buf + i) : __ldcg(buf + i);
+      const float4 v1 = level == 0 ? __ldg(buf + i + step) : __ldcg(buf + i + step);
+      const float4 v2 = level == 0 ? __ldg(buf + i + 2 * step) : __ldcg(buf + i + 2 * step);
+      const float4 v3 = level == 0 ? __ldg(buf + i + 3 * step) : __ldcg(buf + i + 3 * step);
+      a0.x += v0.x, a0.y += v0.y, a0.z += v0.z, a0.w += v0.w;
+      a1.x += v1.x, a1.y += v1.y, a1.z += v1.z, a1.w += v1.w;
+      a2.x += v2.x, a2.y += v2.y, a2.z += v2.z, a2.w += v2.w;
+      a3.x += v3.x, a3.y += v3.y, a3.z += v3.z, a3.w += v3.w;
+    }
+    for (; i < n4; i += step) {
+      const float4 v = level == 0 ? __ldg(buf + i) : __ldcg(buf + i);
+      a0.x += v.x, a0.y += v.y, a0.z += v.z, a0.w += v.w;
+    }
+  }
+  const float t = (a0.x + a0.y + a0.z + a0.w) + (a1.x + a1.y + a1.z + a1.w) + (a2.x + a2.y + a2.z + a2.w) +
+                  (a3.x + a3.y + a3.z + a3.w);
+  if (t == 1.2345e-37f) sink[0] = t;
+}
+
 }  // namespace
 
 void SetPersistentGrid(int blocks) { g_persistent_blocks = std::max(1, blocks); }
@@ -1265,6 +1325,16 @@ void SetTraversalGrid(int sms) {
     per_sm = 4;
   g_traversal_blocks = std::max(1, sms * per_sm);
   g_sms = std::max(1, sms);
+}
+
+void LaunchSampleQueue(const PathBuffers &b, WaveCounters wc, int bounce, int kind, int slots, int m, float4 *out,
+                       cudaStream_t st) {
+  SampleQueueKernel<<<Blocks(std::max(m, 1)), kBlock, 0, st>>>(b, wc, bounce, kind, std::max(slots, 1), m, out);
+}
+
+void LaunchReadBandwidth(const float4 *buf, int64_t n4, int passes, int level, int blocks, float *sink,
+                         cudaStream_t st) {
+  ReadBandwidthKernel<<<static_cast<unsigned>(std::max(blocks, 1)), kBlock, 0, st>>>(buf, n4, passes, level, sink);
 }
 
 void LaunchCamera(const DevCamera &cam, const WaveInfo &w, const PathBuffers &b, WaveCounters wc, cudaStream_t st) {

@@ -161,4 +161,13 @@ void LaunchIntersectRays(const DevScene &s, const float *rays, int64_t n, int is
 void LaunchOccludedRays(const DevScene &s, const float *rays, const float *maxd, int64_t n, int isect,
                         uint8_t *out, cudaStream_t st);
 
+// Measurement: a sample of bounce `bounce`'s closest-hit (kind 0) or shadow
+// (kind 1) queue, up to m rays, into out (1 + 2m float4s; see SampleQueueKernel).
+void LaunchSampleQueue(const PathBuffers &b, WaveCounters wc, int bounce, int kind, int slots, int m, float4 *out,
+                       cudaStream_t st);
+// Read-bandwidth kernel of `blocks` blocks of 256 threads over n4 float4s,
+// `passes` times; level as in muon_gpu_measure_read_bandwidth.
+void LaunchReadBandwidth(const float4 *buf, int64_t n4, int passes, int level, int blocks, float *sink,
+                         cudaStream_t st);
+
 }  // namespace muon_gpu

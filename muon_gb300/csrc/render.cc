@@ -18,6 +18,7 @@
 #include <vector>
 
 #include "bvh_build.h"
+#include "bvh_walk.h"
 #include "guide.h"
 #include "host_cuda.h"
 #include "host_scene.h"
@@ -399,6 +400,20 @@ int ValidateParams(const MuonRenderParams &p) {
 
 namespace {
 
+// Queue samples of a probed render (muon_gpu_probe_traversal): per wave,
+// bounce and kind (0 closest hit, 1 shadow) a block of 1 + 2m float4s as
+// SampleQueueKernel writes them.
+struct QueueProbe {
+  int m = 0;
+  DeviceBuffer buf;
+  size_t waves = 0;
+  int bounces = 0;
+  size_t BlockFloat4s() const { return 1 + 2 * static_cast<size_t>(m); }
+  size_t Offset(size_t wave, int bounce, int kind) const {
+    return ((wave * bounces + bounce) * 2 + kind) * BlockFloat4s();
+  }
+};
+
 // Renders into a device film. Throws CudaError.
 //
 // Bounded depth: every wavefront is a fixed launch sequence (camera; per
@@ -408,7 +423,7 @@ namespace {
 // depth (max_depth -1): the host reads the queue length after every bounce and
 // stops when no path continues.
 void RenderDevice(MuonScene *sc, const MuonRenderParams &p, double *d_sum, double *d_sq, uint32_t *d_cnt,
-                  const GuideDev *guide = nullptr) {
+                  const GuideDev *guide = nullptr, QueueProbe *probe = nullptr) {
   cudaStream_t st = sc->stream;
   const bool pt = p.integrator == MUON_INTEGRATOR_PATHTRACER;
   // Raytracer / AnalyticDirect: one kernel follows each path to its end.
@@ -442,6 +457,17 @@ void RenderDevice(MuonScene *sc, const MuonRenderParams &p, double *d_sum, doubl
   moved |= sc->EnsureCounters(stride * waves.size());
   sc->stats.Ensure(sizeof(unsigned long long) * kNumStats);
   PathBuffers b = sc->Buffers();
+  if (probe) {
+    probe->waves = waves.size();
+    probe->bounces = bounces;
+    const size_t bytes = std::max<size_t>(16, waves.size() * bounces * 2 * probe->BlockFloat4s() * sizeof(float4));
+    probe->buf.Ensure(bytes);
+    CUDA_TRY(cudaMemsetAsync(probe->buf.ptr, 0, bytes, st));
+  }
+  auto sample_queue = [&](size_t wi, WaveCounters wc, int k, int kind) {
+    if (probe)
+      LaunchSampleQueue(b, wc, k, kind, slots, probe->m, probe->buf.as<float4>() + probe->Offset(wi, k, kind), st);
+  };
 
   uint64_t launches = 0;
   int timed_pairs = 1;
@@ -475,6 +501,7 @@ void RenderDevice(MuonScene *sc, const MuonRenderParams &p, double *d_sum, doubl
         timed(2, [&] { LaunchWhitted(sc->dev, b, w, p.integrator, max_d, p.intersect_mode, stats_on, st); });
       }
       for (int k = 0; k < (whitted ? 0 : bounces); ++k) {
+        sample_queue(wi, wc, k, 0);
         timed(0, [&] { LaunchExtend(sc->dev, b, wc, k, w.n, p.intersect_mode, stats_on, st); });
         // Guiding covers the first rec_bounces vertices of a path (where the
         // network is trained); deeper vertices sample the BRDF alone.
@@ -493,6 +520,7 @@ void RenderDevice(MuonScene *sc, const MuonRenderParams &p, double *d_sum, doubl
           else LaunchShadePath(sc->dev, w, sp, b, wc, k, w.n, st);
         });
         if (slots > 0) {
+          sample_queue(wi, wc, k, 1);
           timed(1, [&] {
             LaunchOcclude(sc->dev, b, wc, k, slots, static_cast<int>(std::min<int64_t>(int64_t(w.n) * slots, INT32_MAX)),
                           p.intersect_mode, stats_on, st);
@@ -531,7 +559,7 @@ void RenderDevice(MuonScene *sc, const MuonRenderParams &p, double *d_sum, doubl
     std::snprintf(keybuf + klen, sizeof(keybuf) - klen, " guide %p %p %p %p %d %d %.9g %.9g %.9g %.9g", guide->wt,
                   (void *)guide->mix, (void *)guide->rec, (void *)guide->pool, guide->rec_cap, guide->rec_bounces,
                   guide->alpha, guide->lo[0], guide->lo[1], guide->inv_ext[0]);
-  const bool use_graph = bounded && !(p.flags & MUON_RENDER_NO_GRAPH);
+  const bool use_graph = bounded && !(p.flags & MUON_RENDER_NO_GRAPH) && !probe;
   if (moved) sc->DropGraph();
   CUDA_TRY(cudaEventRecord(t0, st));
   const bool graph_ready = use_graph && sc->graph && sc->graph_key == keybuf;
@@ -929,6 +957,120 @@ int muon_gpu_occluded(MuonScene *scene, const MuonRay *rays, const float *max_di
     return FailCuda(e);
   }
   return MUON_OK;
+}
+
+int muon_gpu_probe_traversal(MuonScene *scene, const MuonRenderParams *params, int32_t rays_per_queue,
+                             MuonTraversalProbe *out) {
+  if (!scene || !params || !out || rays_per_queue < 1) return Fail(MUON_ERR_INVALID_ARG, "bad argument");
+  int rc = ValidateParams(*params);
+  if (rc != MUON_OK) return rc;
+  if (params->integrator != MUON_INTEGRATOR_PATHTRACER || params->max_depth < 0)
+    return Fail(MUON_ERR_INVALID_ARG, "traversal probes need the path tracer with a bounded depth");
+  if (params->intersect_mode != MUON_ISECT_EXACT && params->intersect_mode != MUON_ISECT_FAST)
+    return Fail(MUON_ERR_INVALID_ARG, "the host walk supports the exact and fast intersection modes");
+  *out = MuonTraversalProbe{};
+  try {
+    CUDA_TRY(cudaSetDevice(scene->device));
+    const size_t np = static_cast<size_t>(scene->img.width) * scene->img.height;
+    EnsurePooled(scene->film_sum, 3 * np * sizeof(double), scene->device);
+    EnsurePooled(scene->film_sq, 3 * np * sizeof(double), scene->device);
+    EnsurePooled(scene->film_cnt, np * sizeof(uint32_t), scene->device);
+    cudaStream_t st = scene->stream;
+    CUDA_TRY(cudaMemsetAsync(scene->film_sum.ptr, 0, 3 * np * sizeof(double), st));
+    CUDA_TRY(cudaMemsetAsync(scene->film_sq.ptr, 0, 3 * np * sizeof(double), st));
+    CUDA_TRY(cudaMemsetAsync(scene->film_cnt.ptr, 0, np * sizeof(uint32_t), st));
+    MuonRenderParams p = *params;
+    p.flags = (p.flags | MUON_RENDER_STATS | MUON_RENDER_NO_GRAPH) & ~MUON_RENDER_ACCUMULATE;
+    QueueProbe probe;
+    probe.m = rays_per_queue;
+    RenderDevice(scene, p, scene->film_sum.as<double>(), scene->film_sq.as<double>(), scene->film_cnt.as<uint32_t>(),
+                 nullptr, &probe);
+    const size_t blocks = probe.waves * probe.bounces * 2;
+    std::vector<float4> h(blocks * probe.BlockFloat4s());
+    if (!h.empty())
+      CUDA_TRY(cudaMemcpy(h.data(), probe.buf.ptr, h.size() * sizeof(float4), cudaMemcpyDeviceToHost));
+    std::vector<WalkRayIn> rays;
+    for (size_t wi = 0; wi < probe.waves; ++wi) {
+      for (int k = 0; k < probe.bounces; ++k) {
+        for (int kind = 0; kind < 2; ++kind) {
+          const float4 *blk = h.data() + probe.Offset(wi, k, kind);
+          int32_t taken, n;
+          std::memcpy(&taken, &blk[0].x, 4);
+          std::memcpy(&n, &blk[0].y, 4);
+          if (taken <= 0 || n <= 0) continue;
+          rays.resize(static_cast<size_t>(taken));
+          for (int i = 0; i < taken; ++i) {
+            const float4 o = blk[1 + 2 * i], d = blk[2 + 2 * i];
+            WalkRayIn &r = rays[i];
+            r.o[0] = o.x, r.o[1] = o.y, r.o[2] = o.z;
+            r.d[0] = d.x, r.d[1] = d.y, r.d[2] = d.z;
+            r.tmax = d.w;
+            std::memcpy(&r.root, &o.w, 4);
+          }
+          MuonWalkCounts c{0, 0, 0, 0};
+          WalkMany(scene->img, rays.data(), taken, kind == 1, p.intersect_mode, nullptr, &c);
+          const double scale = static_cast<double>(n) / taken;
+          MuonWalkCounts &tot = kind == 0 ? out->extend_walked : out->occlude_walked;
+          tot.rays += c.rays, tot.box_tests += c.box_tests, tot.prim_tests += c.prim_tests, tot.hits += c.hits;
+          if (kind == 0) {
+            out->extend_rays += static_cast<uint64_t>(n);
+            out->extend_box_tests += scale * static_cast<double>(c.box_tests);
+            out->extend_prim_tests += scale * static_cast<double>(c.prim_tests);
+          } else {
+            out->occlude_rays += static_cast<uint64_t>(n);
+            out->occlude_box_tests += scale * static_cast<double>(c.box_tests);
+            out->occlude_prim_tests += scale * static_cast<double>(c.prim_tests);
+          }
+        }
+      }
+    }
+  } catch (const CudaError &e) {
+    return FailCuda(e);
+  } catch (const std::bad_alloc &) {
+    return Fail(MUON_ERR_OOM, "host allocation failed");
+  }
+  return MUON_OK;
+}
+
+int muon_gpu_measure_read_bandwidth(int32_t level, int64_t bytes, int32_t passes, double *gb_per_s) {
+  if (!gb_per_s || level < 0 || level > 2 || bytes < 4096 || passes < 1)
+    return Fail(MUON_ERR_INVALID_ARG, "bad argument");
+  if (level == 0 && bytes > (int64_t(64) << 10)) return Fail(MUON_ERR_INVALID_ARG, "level 0 reads at most 64 KiB");
+  cudaStream_t st = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  int rc = MUON_OK;
+  try {
+    int dev = 0, sms = 0;
+    CUDA_TRY(cudaGetDevice(&dev));
+    CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    const int64_t n4 = bytes / 16;
+    DeviceBuffer buf, sink;
+    buf.Ensure(static_cast<size_t>(n4) * 16);
+    sink.Ensure(16);
+    CUDA_TRY(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    CUDA_TRY(cudaEventCreate(&e0));
+    CUDA_TRY(cudaEventCreate(&e1));
+    CUDA_TRY(cudaMemsetAsync(buf.ptr, 0, static_cast<size_t>(n4) * 16, st));
+    // level 0: two blocks per SM, each reading the whole buffer; else eight
+    // blocks per SM (full occupancy) reading it once between them
+    const int blocks = level == 0 ? 2 * sms : 8 * sms;
+    LaunchReadBandwidth(buf.as<float4>(), n4, 1, level, blocks, sink.as<float>(), st);  // warm
+    CUDA_TRY(cudaEventRecord(e0, st));
+    LaunchReadBandwidth(buf.as<float4>(), n4, passes, level, blocks, sink.as<float>(), st);
+    CUDA_TRY(cudaEventRecord(e1, st));
+    CUDA_TRY(cudaGetLastError());
+    CUDA_TRY(cudaEventSynchronize(e1));
+    float ms = 0.0f;
+    CUDA_TRY(cudaEventElapsedTime(&ms, e0, e1));
+    const double delivered = static_cast<double>(n4) * 16.0 * passes * (level == 0 ? blocks : 1);
+    *gb_per_s = delivered / (static_cast<double>(ms) * 1e6);
+  } catch (const CudaError &e) {
+    rc = FailCuda(e);
+  }
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  if (st) cudaStreamDestroy(st);
+  return rc;
 }
 
 int muon_gpu_stats(const MuonScene *scene, MuonStats *stats) {

@@ -112,6 +112,16 @@ class BatchTuning(C.Structure):
                 ("pad", C.c_int32), ("best_ms", C.c_double)]
 
 
+class WalkCounts(C.Structure):
+    _fields_ = [("rays", C.c_uint64), ("box_tests", C.c_uint64), ("prim_tests", C.c_uint64), ("hits", C.c_uint64)]
+
+
+class TraversalProbe(C.Structure):
+    _fields_ = [("extend_walked", WalkCounts), ("occlude_walked", WalkCounts), ("extend_rays", C.c_uint64),
+                ("occlude_rays", C.c_uint64), ("extend_box_tests", C.c_double), ("extend_prim_tests", C.c_double),
+                ("occlude_box_tests", C.c_double), ("occlude_prim_tests", C.c_double)]
+
+
 class GuideConfig(C.Structure):
     _fields_ = [("batch", C.c_int32), ("wave_paths", C.c_int32), ("record_bounces", C.c_int32),
                 ("pool_capacity", C.c_int32), ("learning_rate", C.c_float), ("mixture_fraction", C.c_float),
@@ -146,6 +156,11 @@ SIGNATURES = {
     "muon_gpu_occluded": (C.c_int, [C.c_void_p, C.POINTER(Ray), C.POINTER(C.c_float), C.c_int64, C.c_int32,
                                     C.POINTER(C.c_uint8)]),
     "muon_gpu_stats": (C.c_int, [C.c_void_p, C.POINTER(Stats)]),
+    "muon_walk_rays": (C.c_int, [C.POINTER(SceneDesc), C.POINTER(Ray), C.POINTER(C.c_float), C.c_int64, C.c_int32,
+                                 C.c_int32, C.POINTER(C.c_int32), C.POINTER(WalkCounts)]),
+    "muon_gpu_probe_traversal": (C.c_int, [C.c_void_p, C.POINTER(RenderParams), C.c_int32,
+                                           C.POINTER(TraversalProbe)]),
+    "muon_gpu_measure_read_bandwidth": (C.c_int, [C.c_int32, C.c_int64, C.c_int32, C.POINTER(C.c_double)]),
     "muon_gpu_scene_stream": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p)]),
     "muon_gpu_last_error": (C.c_char_p, []),
     "muon_gpu_batch_create": (C.c_int, [C.POINTER(C.c_void_p), C.c_int32, C.POINTER(C.c_void_p)]),

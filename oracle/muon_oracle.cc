@@ -24,6 +24,7 @@
 // Build: oracle/build.py (g++ -O2 -ffp-contract=off) -> oracle/lib/.
 #include <algorithm>
 #include <atomic>
+#include <chrono>
 #include <cmath>
 #include <cstdint>
 #include <cstring>
@@ -1314,15 +1315,20 @@ int oracle_scene_info(const char *text, int32_t *out) {
 // Renders with the reference algorithm. spp > 0 overrides pixel_samples;
 // seed >= 0 re-seeds the scene's seed generator (tiles and path tracer) as
 // `random_seed <seed>` would. Outputs: sum, sum_sq (3*W*H doubles), film32
-// (3*W*H floats, may be null), counters[6] (primary, secondary, object tests,
-// object hits, bounds tests, bounds hits).
+// (3*W*H floats, may be null), counters[8] (primary, secondary, object tests,
+// object hits, bounds tests, bounds hits, build ns, render ns).
 int oracle_render(const char *text, int precision_bits, int parallelism, int spp, long long seed, int linear,
                   double *sum, double *sum_sq, float *film32, uint64_t *counters) {
   auto run = [&](auto tag) -> int {
     using T = decltype(tag);
     oracle::Scene<T> s;
+    // Build time (parse + acceleration structure) and render time are
+    // measured apart, as the reference's Stats reports them
+    // (muon/stats.cc:9-22, 41-55).
+    const auto t0 = std::chrono::steady_clock::now();
     int rc = LoadScene(text, linear, s);
     if (rc) return rc;
+    const auto t1 = std::chrono::steady_clock::now();
     if (seed >= 0) {
       s.seedgen.seed(static_cast<unsigned int>(seed));
       if (s.integ == oracle::Integ::kPath) s.path_seed = s.seedgen();
@@ -1330,17 +1336,73 @@ int oracle_render(const char *text, int precision_bits, int parallelism, int spp
     if (spp > 0) s.pixel_samples = spp;
     oracle::RenderOut<T> out;
     oracle::Render(s, parallelism, out);
+    const auto t2 = std::chrono::steady_clock::now();
     std::memcpy(sum, out.sum.data(), out.sum.size() * sizeof(double));
     std::memcpy(sum_sq, out.sum_sq.data(), out.sum_sq.size() * sizeof(double));
     if (film32) std::memcpy(film32, out.film32.data(), out.film32.size() * sizeof(float));
     if (counters) {
       counters[0] = out.st.primary, counters[1] = out.st.secondary, counters[2] = out.st.obj_tests;
       counters[3] = out.st.obj_hits, counters[4] = out.st.bounds_tests, counters[5] = out.st.bounds_hits;
+      counters[6] = static_cast<uint64_t>(std::chrono::duration_cast<std::chrono::nanoseconds>(t1 - t0).count());
+      counters[7] = static_cast<uint64_t>(std::chrono::duration_cast<std::chrono::nanoseconds>(t2 - t1).count());
     }
     return 0;
   };
   return precision_bits == 64 ? run(double()) : run(float());
 }
+
+// A scene parsed and built once and rendered many times in float (for
+// timing the reference algorithm on a large scene without re-parsing it per
+// run). oracle_scene_render takes the same spp / seed overrides as
+// oracle_render (seed < 0: the file's own seeds, restored every time) and
+// fills sum, sum_sq (3*W*H doubles, may be null) and counters[8].
+struct LoadedScene {
+  oracle::Scene<float> s;
+  std::mt19937 seedgen0;
+  unsigned int path_seed0 = 0;
+  int spp0 = 1;
+};
+
+void *oracle_scene_load(const char *text, int linear) {
+  auto *h = new LoadedScene();
+  if (LoadScene(text, linear, h->s)) {
+    delete h;
+    return nullptr;
+  }
+  h->seedgen0 = h->s.seedgen;
+  h->path_seed0 = h->s.path_seed;
+  h->spp0 = h->s.pixel_samples;
+  return h;
+}
+
+int oracle_scene_render(void *handle, int parallelism, int spp, long long seed, double *sum, double *sum_sq,
+                        uint64_t *counters) {
+  auto *h = static_cast<LoadedScene *>(handle);
+  if (!h) return 1;
+  oracle::Scene<float> &s = h->s;
+  s.seedgen = h->seedgen0;
+  s.path_seed = h->path_seed0;
+  if (seed >= 0) {
+    s.seedgen.seed(static_cast<unsigned int>(seed));
+    if (s.integ == oracle::Integ::kPath) s.path_seed = s.seedgen();
+  }
+  s.pixel_samples = spp > 0 ? spp : h->spp0;
+  const auto t1 = std::chrono::steady_clock::now();
+  oracle::RenderOut<float> out;
+  oracle::Render(s, parallelism, out);
+  const auto t2 = std::chrono::steady_clock::now();
+  if (sum) std::memcpy(sum, out.sum.data(), out.sum.size() * sizeof(double));
+  if (sum_sq) std::memcpy(sum_sq, out.sum_sq.data(), out.sum_sq.size() * sizeof(double));
+  if (counters) {
+    counters[0] = out.st.primary, counters[1] = out.st.secondary, counters[2] = out.st.obj_tests;
+    counters[3] = out.st.obj_hits, counters[4] = out.st.bounds_tests, counters[5] = out.st.bounds_hits;
+    counters[6] = 0;
+    counters[7] = static_cast<uint64_t>(std::chrono::duration_cast<std::chrono::nanoseconds>(t2 - t1).count());
+  }
+  return 0;
+}
+
+void oracle_scene_free(void *handle) { delete static_cast<LoadedScene *>(handle); }
 
 // Closest hits of caller-given rays (n x 6 floats) in float or double;
 // out: n x 8 doubles (distance, prim id, position, normal), id -1 = miss.

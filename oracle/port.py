@@ -30,6 +30,11 @@ def lib() -> C.CDLL:
         l.oracle_intersect.argtypes = [C.c_char_p, C.c_int, C.c_int, C.POINTER(C.c_float), C.c_longlong,
                                        C.POINTER(C.c_double)]
         l.oracle_camera_rays.argtypes = [C.c_char_p, C.POINTER(C.c_float)]
+        l.oracle_scene_load.restype = C.c_void_p
+        l.oracle_scene_load.argtypes = [C.c_char_p, C.c_int]
+        l.oracle_scene_render.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_longlong, C.POINTER(C.c_double),
+                                          C.POINTER(C.c_double), C.POINTER(C.c_uint64)]
+        l.oracle_scene_free.argtypes = [C.c_void_p]
         l.oracle_tonemap.argtypes = [C.POINTER(C.c_float), C.c_longlong, C.c_int, C.c_float, C.POINTER(C.c_uint8)]
         _lib = l
     return _lib
@@ -66,11 +71,12 @@ def render(text: str, spp: int = 0, seed: int = -1, threads: int = 1, precision:
     s = np.zeros((h, w, 3))
     q = np.zeros((h, w, 3))
     f32 = np.zeros((h, w, 3), dtype=np.float32)
-    cnt = (C.c_uint64 * 6)()
+    cnt = (C.c_uint64 * 8)()
     _check(lib().oracle_render(text.encode(), precision, threads, spp, seed, int(linear),
                                s.ctypes.data_as(C.POINTER(C.c_double)), q.ctypes.data_as(C.POINTER(C.c_double)),
                                f32.ctypes.data_as(C.POINTER(C.c_float)), cnt))
-    names = ["primary", "secondary", "object_tests", "object_hits", "bounds_tests", "bounds_hits"]
+    names = ["primary", "secondary", "object_tests", "object_hits", "bounds_tests", "bounds_hits", "build_ns",
+             "render_ns"]
     return OracleFilm(s, q, np.full((h, w), n, dtype=np.uint32), f32, dict(zip(names, list(cnt))))
 
 
@@ -97,3 +103,43 @@ def camera_rays(text: str) -> np.ndarray:
     rays = np.zeros((h * w, 6), dtype=np.float32)
     _check(lib().oracle_camera_rays(text.encode(), rays.ctypes.data_as(C.POINTER(C.c_float))))
     return rays
+
+
+class LoadedScene:
+    """A scene parsed and built once by the oracle, rendered many times (FP32,
+    the reference's precision): for timing the reference algorithm without
+    re-parsing a large scene per run."""
+
+    def __init__(self, text: str, linear: bool = False):
+        self.width, self.height, self.spp, _ = scene_info(text)
+        self._h = lib().oracle_scene_load(text.encode(), int(linear))
+        if not self._h:
+            raise RuntimeError(f"oracle error: {lib().oracle_last_error().decode()}")
+
+    def render(self, spp: int = 0, seed: int = -1, threads: int = 1, film: bool = False) -> dict:
+        """Renders; returns the counters (render_ns: the render alone) and,
+        with film=True, the FP64 sums under "sum" / "sum_sq"."""
+        cnt = (C.c_uint64 * 8)()
+        s = q = None
+        if film:
+            s = np.zeros((self.height, self.width, 3))
+            q = np.zeros((self.height, self.width, 3))
+        dp = lambda a: None if a is None else a.ctypes.data_as(C.POINTER(C.c_double))
+        _check(lib().oracle_scene_render(self._h, threads, spp, seed, dp(s), dp(q), cnt))
+        names = ["primary", "secondary", "object_tests", "object_hits", "bounds_tests", "bounds_hits", "build_ns",
+                 "render_ns"]
+        out = dict(zip(names, list(cnt)))
+        if film:
+            out["sum"], out["sum_sq"] = s, q
+        return out
+
+    def close(self) -> None:
+        if self._h:
+            lib().oracle_scene_free(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -450,6 +450,16 @@ def measure_batch(w: dict, steps: int, warmup: int, builder: str, with_cpu: bool
             launches += total["kernel_launches"]
     dev_ms, counted = replicas.reduce_step(sum(times), counted, device="cuda")
     value = counted / (dev_ms * 1e3)
+    # the same scenes rendered one at a time (each its own graph, device
+    # time): what batching them into one wavefront buys, and what it costs a
+    # scene in latency
+    alone = []
+    for s_, p_, f_ in zip(sc, params, films):
+        s_.render_device(p_, *[x.data_ptr() for x in f_])  # first render of a configuration: no graph yet
+        s_.render_device(p_, *[x.data_ptr() for x in f_])
+        s_.render_device(p_, *[x.data_ptr() for x in f_])
+        alone.append(s_.stats()["render_ms"])
+    torch.cuda.synchronize()
     # end to end: scene uploads (BVH builds), batch merge, render, host films back
     e2e_steps = 2
     h2d = sum(p.desc.num_triangles * 80 + p.desc.num_spheres * 32 + p.desc.num_materials * 56 +
@@ -475,6 +485,10 @@ def measure_batch(w: dict, steps: int, warmup: int, builder: str, with_cpu: bool
         "paths_per_step": int(total["paths"]),
         "latency_ms": {"p50": round(pct(0.50), 3), "p99": round(pct(0.99), 3), "max": round(lat_sorted[-1], 3),
                        "note": "per scene: batch start to its film complete"},
+        "alone_ms": {"sum": round(sum(alone), 1), "p50": round(sorted(alone)[len(alone) // 2], 3),
+                     "p99": round(sorted(alone)[min(len(alone) - 1, int(0.99 * len(alone)))], 3),
+                     "max": round(max(alone), 3),
+                     "note": "each scene rendered by itself (its own CUDA graph), device time"},
         "autotune": dict(tune, seconds=round(t_tune, 2)),
         "e2e": {"value": round(e2e_value, 2), "unit": METRIC, "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h),

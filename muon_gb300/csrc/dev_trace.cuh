@@ -12,6 +12,14 @@ namespace muon_gpu {
 
 constexpr int kStackSize = 64;
 
+// Exact mode: keep the ray in the object space of the last transform a
+// primitive test used, so that the primitives of one transformed mesh (which
+// share their transform) do not each load the transform and re-transform the
+// ray. The values are the ones the test would compute, so hits are unchanged.
+#ifndef MUON_XF_CACHE
+#define MUON_XF_CACHE 1
+#endif
+
 struct RayPre {
   float3 o, d, idir, ood;
   // watertight-test shear
@@ -20,7 +28,34 @@ struct RayPre {
   // exact mode: the direction as the reference carries it into the object
   // space of an untransformed primitive, normalize(I * (d, 0))
   mm::v3 dn;
+  // exact mode: transform index of the cached object-space ray (co, cd)
+  int cxf;
+  mm::v3 co, cd;
 };
+
+// Three-input min / max of the slab test as single instructions (same
+// values: no operand is NaN, SafeInv keeps 1/d finite).
+#ifndef MUON_MINMAX3
+#define MUON_MINMAX3 1
+#endif
+__device__ __forceinline__ float Max3(float a, float b, float c) {
+#if MUON_MINMAX3
+  float r;
+  asm("max.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+  return r;
+#else
+  return fmaxf(fmaxf(a, b), c);
+#endif
+}
+__device__ __forceinline__ float Min3(float a, float b, float c) {
+#if MUON_MINMAX3
+  float r;
+  asm("min.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+  return r;
+#else
+  return fminf(fminf(a, b), c);
+#endif
+}
 
 __device__ __forceinline__ float SafeInv(float x) {
   const float tiny = 1e-30f;
@@ -51,7 +86,10 @@ __device__ __forceinline__ RayPre Prepare(float3 o, float3 d) {
     r.sy = dy / dz;
     r.sz = 1.0f / dz;
   }
-  if (kTriTest == MUON_ISECT_EXACT) r.dn = mm::normalize(mm::make3(d.x, d.y, d.z));
+  if (kTriTest == MUON_ISECT_EXACT) {
+    r.dn = mm::normalize(mm::make3(d.x, d.y, d.z));
+    r.cxf = -1;  // nothing cached (-1 is the identity, which needs no cache)
+  }
   return r;
 }
 
@@ -152,20 +190,28 @@ __device__ __forceinline__ mm::v3 V(const F4 &v) { return mm::make3(v.x, v.y, v.
 __device__ __forceinline__ mm::v3 V(float3 v) { return mm::make3(v.x, v.y, v.z); }
 
 // The ray in a primitive's object space (Ray::Transform, muon/camera.cc:7-11).
-__device__ __forceinline__ void ObjectRay(const DevScene &s, const RayPre &r, int xf, mm::v3 *o, mm::v3 *d) {
+__device__ __forceinline__ void ObjectRay(const DevScene &s, RayPre &r, int xf, mm::v3 *o, mm::v3 *d) {
   if (xf < 0) {
     *o = V(r.o);
     *d = r.dn;
+  } else if (MUON_XF_CACHE && xf == r.cxf) {
+    *o = r.co;
+    *d = r.cd;
   } else {
     const DevTransform &T = s.transforms[xf];
     *o = XPointExact(T.w2o, V(r.o));
     *d = XDirExact(T.w2o, V(r.d));
+    if (MUON_XF_CACHE) {
+      r.cxf = xf;
+      r.co = *o;
+      r.cd = *d;
+    }
   }
 }
 
 // Object-space test with the reference's operations; returns the world
 // distance |M p - o| (muon/objects.cc:38-43) or -1, and the object-space t.
-__device__ __forceinline__ float PrimTestExact(const DevScene &s, const RayPre &r, const PrimRecord &p, uint32_t flags,
+__device__ __forceinline__ float PrimTestExact(const DevScene &s, RayPre &r, const PrimRecord &p, uint32_t flags,
                                                float *t_obj) {
   using namespace mm;
   const int xf = __float_as_int((flags & kPrimSphere) ? p.p1.y : p.p1.w);
@@ -202,7 +248,7 @@ __device__ __forceinline__ float PrimTestExact(const DevScene &s, const RayPre &
 }
 
 template <int kTriTest>
-__device__ __forceinline__ float PrimTest(const DevScene &s, const RayPre &r, const PrimRecord &p, uint32_t flags,
+__device__ __forceinline__ float PrimTest(const DevScene &s, RayPre &r, const PrimRecord &p, uint32_t flags,
                                           float *t_obj) {
   if (kTriTest == MUON_ISECT_EXACT) return PrimTestExact(s, r, p, flags, t_obj);
   if (flags & kPrimSphere) return SphereTest(s, r, p);
@@ -232,7 +278,7 @@ __device__ __forceinline__ int Trace(const DevScene &s, float3 o, float3 d, floa
                                      TraceCounters *cnt, bool *overflow, float *t_obj_hit = nullptr) {
   int hit = -1;
   if (s.num_nodes == 0) return -1;
-  const RayPre r = Prepare<kTriTest>(o, d);
+  RayPre r = Prepare<kTriTest>(o, d);
   int stack[kStackSize];
   int sp = 0;
   int node = 0;
@@ -249,10 +295,10 @@ __device__ __forceinline__ int Trace(const DevScene &s, float3 o, float3 d, floa
       float c1lox = n1.x * r.idir.x - r.ood.x, c1hix = n1.y * r.idir.x - r.ood.x;
       float c1loy = n1.z * r.idir.y - r.ood.y, c1hiy = n1.w * r.idir.y - r.ood.y;
       float c1loz = n2.z * r.idir.z - r.ood.z, c1hiz = n2.w * r.idir.z - r.ood.z;
-      float c0min = fmaxf(fmaxf(fminf(c0lox, c0hix), fminf(c0loy, c0hiy)), fmaxf(fminf(c0loz, c0hiz), 0.0f));
-      float c0max = fminf(fminf(fmaxf(c0lox, c0hix), fmaxf(c0loy, c0hiy)), fminf(fmaxf(c0loz, c0hiz), tmax));
-      float c1min = fmaxf(fmaxf(fminf(c1lox, c1hix), fminf(c1loy, c1hiy)), fmaxf(fminf(c1loz, c1hiz), 0.0f));
-      float c1max = fminf(fminf(fmaxf(c1lox, c1hix), fmaxf(c1loy, c1hiy)), fminf(fmaxf(c1loz, c1hiz), tmax));
+      float c0min = Max3(fminf(c0lox, c0hix), fminf(c0loy, c0hiy), fmaxf(fminf(c0loz, c0hiz), 0.0f));
+      float c0max = Min3(fmaxf(c0lox, c0hix), fmaxf(c0loy, c0hiy), fminf(fmaxf(c0loz, c0hiz), tmax));
+      float c1min = Max3(fminf(c1lox, c1hix), fminf(c1loy, c1hiy), fmaxf(fminf(c1loz, c1hiz), 0.0f));
+      float c1max = Min3(fmaxf(c1lox, c1hix), fmaxf(c1loy, c1hiy), fminf(fmaxf(c1loz, c1hiz), tmax));
       bool h0 = c0min <= c0max, h1 = c1min <= c1max;
       if (kStats) {
         cnt->box_tests += 2;
@@ -312,13 +358,45 @@ __device__ __forceinline__ int Trace(const DevScene &s, float3 o, float3 d, floa
 }
 
 // ---- resumable traversal for persistent kernels ---------------------------
+// The top kShortStack entries of a traversal stack live in shared memory
+// (a column of `stride` ints per thread, slot-major so a warp's accesses hit
+// distinct banks), as a ring over the stack positions; deeper entries spill
+// to local memory. 0 keeps the whole stack in local memory.
+#ifndef MUON_SHORT_STACK
+#define MUON_SHORT_STACK 8
+#endif
+constexpr int kShortStack = MUON_SHORT_STACK;
+static_assert((kShortStack & (kShortStack - 1)) == 0, "short stack size must be a power of two");
+
 // The state of one ray's traversal, kept across the refill points of a
 // persistent kernel.
 struct TravState {
   int node, sp, hit;
   float tmax, t_obj;
-  int stack[kStackSize];
+  int *sh;      // this thread's shared-memory column (short stack) or null
+  int stride;   // ints between consecutive slots of the column
+  int stack[kStackSize - kShortStack];
 };
+
+__device__ __forceinline__ void StackPush(TravState &t, int v) {
+  if (kShortStack == 0) {
+    t.stack[t.sp++] = v;
+    return;
+  }
+  int *slot = t.sh + (t.sp & (kShortStack - 1)) * t.stride;
+  if (t.sp >= kShortStack) t.stack[t.sp - kShortStack] = *slot;  // spill the entry the ring overwrites
+  *slot = v;
+  ++t.sp;
+}
+
+__device__ __forceinline__ int StackPop(TravState &t) {
+  --t.sp;
+  if (kShortStack == 0) return t.stack[t.sp];
+  int *slot = t.sh + (t.sp & (kShortStack - 1)) * t.stride;
+  const int v = *slot;
+  if (t.sp >= kShortStack) *slot = t.stack[t.sp - kShortStack];  // refill the ring from the spill
+  return v;
+}
 
 __device__ __forceinline__ void TravBegin(TravState &t, float tmax, int root) {
   t.node = root;
@@ -333,7 +411,7 @@ __device__ __forceinline__ void TravBegin(TravState &t, float tmax, int root) {
 // fewer than `min_active` lanes of the warp are still traversing, so that the
 // finished lanes can take new rays.
 template <bool kAnyHit, bool kStats, int kTriTest>
-__device__ __forceinline__ bool TravRun(const DevScene &s, const RayPre &r, TravState &t, TraceCounters *cnt,
+__device__ __forceinline__ bool TravRun(const DevScene &s, RayPre &r, TravState &t, TraceCounters *cnt,
                                         bool *overflow, int min_active) {
   if (s.num_nodes == 0) return true;
   while (true) {
@@ -347,10 +425,10 @@ __device__ __forceinline__ bool TravRun(const DevScene &s, const RayPre &r, Trav
       float c1lox = n1.x * r.idir.x - r.ood.x, c1hix = n1.y * r.idir.x - r.ood.x;
       float c1loy = n1.z * r.idir.y - r.ood.y, c1hiy = n1.w * r.idir.y - r.ood.y;
       float c1loz = n2.z * r.idir.z - r.ood.z, c1hiz = n2.w * r.idir.z - r.ood.z;
-      float c0min = fmaxf(fmaxf(fminf(c0lox, c0hix), fminf(c0loy, c0hiy)), fmaxf(fminf(c0loz, c0hiz), 0.0f));
-      float c0max = fminf(fminf(fmaxf(c0lox, c0hix), fmaxf(c0loy, c0hiy)), fminf(fmaxf(c0loz, c0hiz), t.tmax));
-      float c1min = fmaxf(fmaxf(fminf(c1lox, c1hix), fminf(c1loy, c1hiy)), fmaxf(fminf(c1loz, c1hiz), 0.0f));
-      float c1max = fminf(fminf(fmaxf(c1lox, c1hix), fmaxf(c1loy, c1hiy)), fminf(fmaxf(c1loz, c1hiz), t.tmax));
+      float c0min = Max3(fminf(c0lox, c0hix), fminf(c0loy, c0hiy), fmaxf(fminf(c0loz, c0hiz), 0.0f));
+      float c0max = Min3(fmaxf(c0lox, c0hix), fmaxf(c0loy, c0hiy), fminf(fmaxf(c0loz, c0hiz), t.tmax));
+      float c1min = Max3(fminf(c1lox, c1hix), fminf(c1loy, c1hiy), fmaxf(fminf(c1loz, c1hiz), 0.0f));
+      float c1max = Min3(fmaxf(c1lox, c1hix), fmaxf(c1loy, c1hiy), fminf(fmaxf(c1loz, c1hiz), t.tmax));
       bool h0 = c0min <= c0max, h1 = c1min <= c1max;
       if (kStats) {
         cnt->box_tests += 2;
@@ -361,7 +439,7 @@ __device__ __forceinline__ bool TravRun(const DevScene &s, const RayPre &r, Trav
           t.node = kEmptyLink;
           break;
         }
-        t.node = t.stack[--t.sp];
+        t.node = StackPop(t);
       } else {
         int near = h0 ? n3.x : n3.y;
         if (h0 && h1) {
@@ -370,7 +448,7 @@ __device__ __forceinline__ bool TravRun(const DevScene &s, const RayPre &r, Trav
             near = n3.y;
             far = n3.x;
           }
-          if (t.sp < kStackSize) t.stack[t.sp++] = far;
+          if (t.sp < kStackSize) StackPush(t, far);
           else *overflow = true;
         }
         t.node = near;
@@ -396,7 +474,7 @@ __device__ __forceinline__ bool TravRun(const DevScene &s, const RayPre &r, Trav
       ++i;
     }
     if (t.sp == 0) return true;
-    t.node = t.stack[--t.sp];
+    t.node = StackPop(t);
     if (__popc(__activemask()) < min_active) return false;
   }
 }

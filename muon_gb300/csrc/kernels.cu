@@ -289,7 +289,7 @@ __global__ void __launch_bounds__(kBlock) CameraBatchKernel(const BatchScene *sc
 constexpr int kRefillThreshold = MUON_REFILL_THRESHOLD;
 // Minimum resident blocks per SM the traversal kernels are compiled for.
 #ifndef MUON_TRAVERSAL_MIN_BLOCKS
-#define MUON_TRAVERSAL_MIN_BLOCKS 1
+#define MUON_TRAVERSAL_MIN_BLOCKS 4
 #endif
 
 template <bool kAnyHit, bool kStats, int kMode, class Load, class Finish>
@@ -300,6 +300,14 @@ __device__ __forceinline__ void PersistentTraverse(const DevScene &s, int n, uin
   bool exhausted = false;
   RayPre r;
   TravState t;
+#if MUON_SHORT_STACK
+  __shared__ int short_stack[kShortStack * kBlock];
+  t.sh = short_stack + threadIdx.x;
+  t.stride = kBlock;
+#else
+  t.sh = nullptr;
+  t.stride = 0;
+#endif
   while (true) {
     const unsigned need = __ballot_sync(0xffffffffu, ray < 0 && !exhausted);
     if (need) {

@@ -23,6 +23,18 @@
 //     Output: int32 w, h, spp, then w*h*3 doubles of sums and of sums of
 //     squares, then uint64 primary, secondary, object tests, bounds tests.
 //
+//   ref_driver hitkeys scene.muon pixels.bin out.bin
+//     As `hits`, through the reference BVH (muon/acceleration.cc:65-142), for
+//     the listed pixels only (int32 x, y pairs), with a key of the primitive
+//     hit in place of an id (the BVH reorders its primitives): per pixel
+//       float ray[6]; int32 hit; int32 kind (0 triangle, 1 sphere);
+//       float distance; float pos[3]; float normal[3]; float albedo[3];
+//       float object_bounds[6] (min, max); float face_normal[3] (Tri::Normal,
+//       the unnormalised (v1-v0)x(v2-v0), muon/objects.cc:48-56; 0 for a
+//       sphere); float transform[16] (the primitive's object-to-world matrix,
+//       column-major)
+//     from which the fixture script recovers the parse-order id.
+//
 //   ref_driver pixels scene.muon pixels.bin out.bin spp seed
 //     The scene's integrator (reseeded as by `render`) traced spp times
 //     through each listed pixel (int32 x, y pairs): sample 0 at the pixel
@@ -101,6 +113,57 @@ int Hits(const char *scene, const char *out_path, bool linear) {
       out.write(reinterpret_cast<const char *>(head), sizeof(head));
       out.write(reinterpret_cast<const char *>(rec), sizeof(rec));
     }
+  }
+  return 0;
+}
+
+std::vector<int32_t> ReadPixels(const char *pix_path) {
+  std::ifstream pin(pix_path, std::ios::binary);
+  std::vector<int32_t> pix;
+  int32_t v;
+  while (pin.read(reinterpret_cast<char *>(&v), sizeof(v))) pix.push_back(v);
+  return pix;
+}
+
+int HitKeys(const char *scene, const char *pix_path, const char *out_path) {
+  const std::vector<int32_t> pix = ReadPixels(pix_path);
+  muon::Options options = MakeOptions(false);
+  muon::Parser parser(scene, options);
+  muon::SceneConfig sc = parser.Parse();
+  auto ws = sc.scene->root->CreateWorkspace();
+  std::ofstream out(out_path, std::ios::binary);
+  for (size_t i = 0; i + 1 < pix.size(); i += 2) {
+    muon::Ray r = sc.scene->camera->CastRay(pix[i] + 0.5f, pix[i + 1] + 0.5f);
+    auto hit = sc.scene->root->Intersect(ws.get(), r);
+    float ray[6];
+    for (int k = 0; k < 3; ++k) ray[k] = r.origin()[k], ray[3 + k] = r.direction()[k];
+    int32_t head[2] = {hit ? 1 : 0, 0};
+    float rec[10] = {0};
+    float key[25] = {0};
+    if (hit) {
+      rec[0] = hit->distance;
+      for (int k = 0; k < 3; ++k) {
+        rec[1 + k] = hit->pos[k];
+        rec[4 + k] = hit->normal[k];
+        rec[7 + k] = hit->obj->material->diffuse[k] + hit->obj->material->specular[k];
+      }
+      const auto *prim = dynamic_cast<const muon::Primitive *>(hit->obj);
+      const auto *tri = dynamic_cast<const muon::Tri *>(hit->obj);
+      head[1] = tri ? 0 : 1;
+      const muon::Bounds b = prim->ObjectBounds();
+      for (int k = 0; k < 3; ++k) key[k] = b.min_pos[k], key[3 + k] = b.max_pos[k];
+      if (tri) {
+        const glm::vec3 n = tri->Normal();
+        for (int k = 0; k < 3; ++k) key[6 + k] = n[k];
+      }
+      const glm::mat4 &m = *prim->transform;
+      for (int c = 0; c < 4; ++c)
+        for (int k = 0; k < 4; ++k) key[9 + 4 * c + k] = m[c][k];
+    }
+    out.write(reinterpret_cast<const char *>(ray), sizeof(ray));
+    out.write(reinterpret_cast<const char *>(head), sizeof(head));
+    out.write(reinterpret_cast<const char *>(rec), sizeof(rec));
+    out.write(reinterpret_cast<const char *>(key), sizeof(key));
   }
   return 0;
 }
@@ -203,9 +266,12 @@ int main(int argc, char **argv) {
     long long seed = argc > 5 ? std::atoll(argv[5]) : -1;
     return Render(argv[2], argv[3], spp, seed);
   }
+  if (argc >= 5 && std::string(argv[1]) == "hitkeys") {
+    return HitKeys(argv[2], argv[3], argv[4]);
+  }
   if (argc >= 7 && std::string(argv[1]) == "pixels") {
     return Pixels(argv[2], argv[3], argv[4], std::atoi(argv[5]), std::atoll(argv[6]));
   }
-  std::fprintf(stderr, "usage: ref_driver hits|render|pixels scene.muon ...\n");
+  std::fprintf(stderr, "usage: ref_driver hits|hitkeys|render|pixels scene.muon ...\n");
   return 2;
 }

@@ -1,0 +1,168 @@
+"""Parity on the benchmarked configurations themselves, not reduced stand-ins.
+
+* The dense mesh of the headline benchmark (1024x1024, 1,320,756 triangles):
+  65,536 seeded pixels of the reference BVH's sample-0 closest hits
+  (hits_dense_mesh_full.npz; ids recovered from a key of the primitive hit).
+  In the exact mode the GPU's ids agree on >= 99.99% of them, the rest exact
+  ties, and distance, normal and the normals / albedo / depth integrators'
+  values are bitwise equal (muon/acceleration.cc:65-142, muon/objects.cc:58-175,
+  muon/integration.cc:47-72). Its counted rays per sample match the
+  reference's 1-spp render of the full frame within 1%.
+* Scene 13 of the 64-scene batch (356,235 triangles, 256x256, depth 10): the
+  same hit comparison on every pixel, and path-traced convergence to 1,024
+  reference samples per pixel, rendered alone and inside a batch.
+
+The scenes are regenerated from their seeded generators (sha256 checked);
+camera rays come from the oracle, which reproduces the reference's camera
+bit for bit (crc32 of the reference's own rays checked).
+"""
+import hashlib
+import zlib
+
+import numpy as np
+import pytest
+
+import muon_gb300 as m
+from conftest import GOLDEN
+from muon_gb300 import native, scenes
+
+
+def _scene_text(fx, make):
+    text = make()
+    assert hashlib.sha256(text.encode()).hexdigest() == str(fx["scene_sha256"]), "scene generator changed"
+    return text
+
+
+def _rays(text, fx, width):
+    from oracle import port
+
+    pix = fx["pixels"]
+    rays = port.camera_rays(text)[pix[:, 1] * width + pix[:, 0]]
+    assert zlib.crc32(np.ascontiguousarray(rays, dtype=np.float32).tobytes()) == int(fx["ray_crc"])
+    return rays
+
+
+def _hit_parity(scene, text, fx, width, min_agree):
+    rays = _rays(text, fx, width)
+    dist, pid, _, nrm = scene.intersect(rays[:, :3], rays[:, 3:], native.ISECT_EXACT)
+    hit = fx["hit"] == 1
+    rid = np.where(hit, fx["prim_id"], -1)
+    assert np.array_equal(pid >= 0, hit)
+    keyed = rid != -3  # pixels whose primitive the key identifies uniquely
+    agree = (pid == rid) & keyed
+    tie = keyed & ~agree & hit & (dist == fx["distance"])
+    other = keyed & ~agree & ~tie
+    print(f"ids agree on {agree[keyed].mean() * 100:.4f}% of {int(keyed.sum())} keyed pixels, "
+          f"{int(tie.sum())} exact ties, {int((~keyed).sum())} unkeyed")
+    assert not other.any()
+    assert agree[keyed].mean() >= min_agree
+    # same primitive (or an unkeyed hit): bitwise equal values
+    same = (agree | ~keyed) & hit
+    assert np.array_equal(dist[same], fx["distance"][same])
+    assert np.array_equal(nrm[same], fx["normal"][same])
+    return same | ~hit
+
+
+def _debug_films(scene, fx, same, width):
+    """Normals / albedo / depth films at sample 0 against the reference's
+    values at the fixture's pixels."""
+    pix = fx["pixels"]
+    idx = pix[:, 1] * width + pix[:, 0]
+    hit = fx["hit"] == 1
+    f = np.float32
+    for integ in ("normals", "albedo", "depth"):
+        film = scene.render(integrator=integ, pixel_samples=1, intersect_mode=native.ISECT_EXACT)
+        got = film.sum.reshape(-1, 3)[idx].astype(np.float32)
+        if integ == "normals":
+            ref = np.where(hit[:, None], fx["normal"] * f(0.5) + f(0.5), f(0))
+        elif integ == "albedo":
+            ref = np.where(hit[:, None], fx["albedo"], f(0))
+        else:
+            ref = np.repeat(np.where(hit[:, None], f(1) / (f(1) + fx["distance"][:, None]), f(0)), 3, axis=1)
+        assert np.array_equal(got[same], ref[same].astype(np.float32)), integ
+
+
+def _zstats(mean_g, se2_g, mean_r, se2_r, ok):
+    from test_gpu_pathtracer import rmse_check
+
+    denom = np.sqrt(se2_g + se2_r)
+    z = np.where(denom > 0, (mean_g - mean_r) / np.where(denom > 0, denom, 1), 0.0)[ok]
+    img_g, img_r = mean_g[ok].mean(), mean_r[ok].mean()
+    se_img = np.sqrt(se2_g[ok].sum() + se2_r[ok].sum()) / se2_g[ok].size
+    # RMSE of the difference against what the two standard errors predict
+    rmse, rmse_pred, zms, dof = rmse_check((mean_g - mean_r)[ok], (se2_g + se2_r)[ok])
+    return (np.abs(z) > 4).mean(), img_g, img_r, se_img, rmse, rmse_pred, zms, dof
+
+
+@pytest.mark.gpu
+def test_dense_mesh_benchmark_hits_equal_the_reference():
+    fx = np.load(f"{GOLDEN}/hits_dense_mesh_full.npz")
+    text = _scene_text(fx, lambda: scenes.dense_mesh(1024, 1024, 256, 10))
+    scene = m.Scene.from_string(text)
+    same = _hit_parity(scene, text, fx, 1024, 0.9999)
+    _debug_films(scene, fx, same, 1024)
+    scene.close()
+
+
+@pytest.mark.gpu
+def test_dense_mesh_benchmark_counts_rays_as_the_reference():
+    """Secondary rays per primary ray (muon/integration.cc:34-38, 483) of the
+    full benchmark frame, against the reference's 1-spp render of it."""
+    fx = np.load(f"{GOLDEN}/hits_dense_mesh_full.npz")
+    text = scenes.dense_mesh(1024, 1024, 256, 10)
+    scene = m.Scene.from_string(text)
+    scene.render(pixel_samples=4, seed=3, intersect_mode=native.ISECT_EXACT)
+    st = scene.stats()
+    ref = fx["counters_1spp"].astype(np.float64)  # primary, secondary, object tests, bounds tests
+    assert st["primary_rays"] == 1024 * 1024 * 4 and ref[0] == 1024 * 1024
+    gpu_ratio, ref_ratio = st["secondary_rays"] / st["primary_rays"], ref[1] / ref[0]
+    print(f"secondary per primary: gpu {gpu_ratio:.4f} reference {ref_ratio:.4f}")
+    assert abs(gpu_ratio - ref_ratio) <= 0.01 * ref_ratio
+    scene.close()
+
+
+@pytest.mark.gpu
+def test_batch_scene_13_hits_equal_the_reference():
+    fx = np.load(f"{GOLDEN}/hits_batch13.npz")
+    text = _scene_text(fx, lambda: scenes.batch_scene(13, 1))
+    scene = m.Scene.from_string(text)
+    same = _hit_parity(scene, text, fx, scene.width, 0.999)
+    _debug_films(scene, fx, same, scene.width)
+    scene.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("batched", [False, True])
+def test_batch_scene_13_converges_to_the_reference(batched):
+    """Per-pixel z-test, image mean and RMSE of scene 13 (rendered alone, or
+    as one scene of a batched wavefront next to another scene) against 1,024
+    reference samples per pixel; the GPU renders 1,024 too. The RMSE of the
+    difference must be what the two standard errors predict, within 4
+    standard deviations of its own sampling spread."""
+    fx = np.load(f"{GOLDEN}/pt_batch13.npz")
+    text = scenes.batch_scene(13, 1)
+    spp = int(fx["spp"])
+    scene = m.Scene.from_string(text)
+    p = scene.params(pixel_samples=spp, seed=21, intersect_mode=native.ISECT_EXACT)
+    if batched:
+        other = m.Scene.from_string(scenes.batch_scene(10, 1))
+        batch = m.Batch([scene, other])
+        film = batch.render([p, other.params(seed=22)])[0]
+        batch.close()
+        other.close()
+    else:
+        film = scene.render(p)
+    mean_g, se2_g = film.mean(), film.variance_of_mean()
+    s, q = fx["sum"], fx["sum_sq"]
+    ok = np.isfinite(s).all(axis=-1) & np.isfinite(q).all(axis=-1)
+    n = float(spp)
+    mean_r = np.where(ok[..., None], s, 0.0) / n
+    se2_r = np.maximum(np.where(ok[..., None], q, 0.0) / n - mean_r * mean_r, 0.0) * n / (n - 1) / n
+    frac, img_g, img_r, se_img, rmse, rmse_pred, zms, dof = _zstats(mean_g, se2_g, mean_r, se2_r, ok)
+    print(f"batch13 batched={batched}: |z|>4 on {frac * 100:.3f}%, image mean gpu {img_g:.6f} ref {img_r:.6f} "
+          f"({(img_g - img_r) / se_img:+.2f} se), rmse {rmse:.5f} predicted {rmse_pred:.5f} ({zms:+.2f} sd, "
+          f"{dof:.0f} dof)")
+    assert abs(img_g - img_r) <= 4 * se_img
+    assert frac <= 0.01
+    assert abs(zms) <= 4
+    scene.close()

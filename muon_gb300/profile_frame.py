@@ -30,10 +30,14 @@ def main() -> None:
     ap.add_argument("--train-steps", type=int, default=4)
     ap.add_argument("--batch", type=int, default=1 << 18)
     ap.add_argument("--mixture-fraction", type=float, default=0.0, help="guided ray mixture fraction (0: default)")
+    ap.add_argument("--max-depth", type=int, default=None,
+                    help="override the scene's max_depth (a depth-limited frame gives the queue lengths of its "
+                         "first bounces: with next-event estimation, max depth d traces bounces 0..d-1)")
     a = ap.parse_args()
     text = scenes.WORKLOADS[a.workload](width=a.width, height=a.height, spp=a.spp)
     scene = Scene.from_string(text)
     mode = {"exact": native.ISECT_EXACT, "fast": native.ISECT_FAST, "watertight": native.ISECT_WATERTIGHT}[a.mode]
+    over = {} if a.max_depth is None else {"max_depth": a.max_depth}
     if a.guided:
         import torch
 
@@ -53,12 +57,18 @@ def main() -> None:
         scene.close()
         return
     for _ in range(a.warmup):
-        scene.render(intersect_mode=mode)
+        scene.render(intersect_mode=mode, **over)
     for _ in range(a.frames):
-        scene.render(intersect_mode=mode)
+        scene.render(intersect_mode=mode, **over)
     st = scene.stats()
     print(f"{a.workload} {a.width}x{a.height}x{a.spp}: {st['render_ms']:.3f} ms, "
           f"{st['kernel_launches']} launches, counted rays {st['primary_rays'] + st['secondary_rays']}")
+    # units per kernel class in one frame, for scaling per-launch profiler
+    # figures of this case to other sizes: extend traces (and shade / fold
+    # process) extend_rays queue entries over extend_launches launches;
+    # occlude traces occlude_rays over occlude_launches
+    print("units " + " ".join(f"{k}={st[k]}" for k in ("extend_rays", "extend_launches", "occlude_rays",
+                                                      "occlude_launches", "paths")))
     scene.close()
 
 

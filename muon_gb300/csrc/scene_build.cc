@@ -28,6 +28,24 @@ namespace muon_gpu {
 namespace {
 
 constexpr int kBins = 32;
+
+// Runs f(begin, end) over [0, n) in contiguous chunks on the host's threads
+// (on the calling thread alone below `grain` items per chunk). Every use
+// writes disjoint outputs or merges exact min / max / integer partials, so the
+// result does not depend on the number of threads.
+template <class F>
+void ParallelFor(int64_t n, int64_t grain, F f) {
+  const int64_t hw = std::max(1u, std::thread::hardware_concurrency());
+  const int64_t parts = std::max<int64_t>(1, std::min(hw, n / std::max<int64_t>(grain, 1)));
+  if (parts <= 1) {
+    f(int64_t(0), n);
+    return;
+  }
+  std::vector<std::thread> pool;
+  for (int64_t k = 1; k < parts; ++k) pool.emplace_back(f, n * k / parts, n * (k + 1) / parts);
+  f(int64_t(0), n / parts);
+  for (std::thread &t : pool) t.join();
+}
 constexpr float kTraversalCost = 1.0f;
 constexpr float kIntersectCost = 1.0f;
 
@@ -80,6 +98,9 @@ struct Subtree {
 class Builder {
  public:
   static constexpr int32_t kParallelRefs = 1 << 15;
+  // Nodes with at least this many references split their bounding and
+  // binning passes across the host's threads.
+  static constexpr int32_t kParallelPass = 1 << 15;
 
   Builder(const std::vector<Aabb> &boxes, int strategy, int max_leaf)
       : strategy_(strategy), max_leaf_(std::max(1, max_leaf)) {
@@ -89,18 +110,49 @@ class Builder {
     threads_left_ = static_cast<int>(hw > 1 ? hw - 1 : 0);
   }
 
+  // A subtree left for the thread pool: refs_[start, end) at `depth`, whose
+  // root goes to out.nodes[node].
+  struct Task {
+    int32_t node, start, end, depth;
+  };
+
   // Builds refs_[start, end) into `out`; returns the subtree root's index.
-  int32_t Build(Subtree &out, int32_t start, int32_t end, int depth) {
+  // With `tasks`, ranges below task_refs_ become placeholder nodes and tasks
+  // (built afterwards by BuildTasks) instead of being built here.
+  int32_t Build(Subtree &out, int32_t start, int32_t end, int depth, std::vector<Task> *tasks = nullptr) {
+    if (tasks && end - start < task_refs_ && end - start > max_leaf_) {
+      const int32_t id = static_cast<int32_t>(out.nodes.size());
+      out.nodes.push_back(BuildNode{});
+      tasks->push_back(Task{id, start, end, depth});
+      return id;
+    }
     BuildNode node;
     node.box = EmptyBox();
     Aabb cbox = EmptyBox();
-    for (int32_t i = start; i < end; ++i) {
-      Grow(node.box, refs_[i].box);
-      for (int k = 0; k < 3; ++k) {
-        float c = refs_[i].C(k);
-        cbox.lo[k] = std::min(cbox.lo[k], c);
-        cbox.hi[k] = std::max(cbox.hi[k], c);
+    auto bounds = [&](int32_t a, int32_t b, Aabb &box, Aabb &cb) {
+      for (int32_t i = a; i < b; ++i) {
+        Grow(box, refs_[i].box);
+        for (int k = 0; k < 3; ++k) {
+          float c = refs_[i].C(k);
+          cb.lo[k] = std::min(cb.lo[k], c);
+          cb.hi[k] = std::max(cb.hi[k], c);
+        }
       }
+    };
+    if (end - start >= kParallelPass) {
+      // the top of the tree, before subtrees run on threads of their own
+      const int parts = static_cast<int>(std::max(1u, std::thread::hardware_concurrency()));
+      std::vector<Aabb> pb(parts, EmptyBox()), pc(parts, EmptyBox());
+      std::vector<std::thread> pool;
+      for (int k = 0; k < parts; ++k) {
+        const int32_t a = start + static_cast<int32_t>(int64_t(end - start) * k / parts);
+        const int32_t b = start + static_cast<int32_t>(int64_t(end - start) * (k + 1) / parts);
+        pool.emplace_back([&, a, b, k] { bounds(a, b, pb[k], pc[k]); });
+      }
+      for (std::thread &t : pool) t.join();
+      for (int k = 0; k < parts; ++k) Grow(node.box, pb[k]), Grow(cbox, pc[k]);
+    } else {
+      bounds(start, end, node.box, cbox);
     }
     out.max_depth = std::max(out.max_depth, depth);
     int32_t n = end - start;
@@ -131,7 +183,7 @@ class Builder {
                        [&](const Ref &a, const Ref &b) { return a.C(axis) < b.C(axis); });
     }
     int32_t l, r;
-    if (end - mid >= kParallelRefs && TakeThread()) {
+    if (!tasks && end - mid >= kParallelRefs && TakeThread()) {
       Subtree right;
       std::thread t([&] { Build(right, mid, end, depth + 1); });
       l = Build(out, start, mid, depth + 1);
@@ -139,14 +191,46 @@ class Builder {
       threads_left_.fetch_add(1);
       r = Splice(out, right);
     } else {
-      l = Build(out, start, mid, depth + 1);
-      r = Build(out, mid, end, depth + 1);
+      l = Build(out, start, mid, depth + 1, tasks);
+      r = Build(out, mid, end, depth + 1, tasks);
     }
     out.nodes[id].left = l;
     out.nodes[id].right = r;
     return id;
   }
 
+  // Builds the tasks on all host threads (largest first), each into its own
+  // subtree, then splices them into `out` in task order and moves each
+  // subtree's root into its placeholder. The tree is the same whatever the
+  // number of threads.
+  void BuildTasks(Subtree &out, std::vector<Task> &tasks) {
+    std::vector<Subtree> subs(tasks.size());
+    std::vector<size_t> by_size(tasks.size());
+    for (size_t i = 0; i < tasks.size(); ++i) by_size[i] = i;
+    std::sort(by_size.begin(), by_size.end(), [&](size_t a, size_t b) {
+      return tasks[a].end - tasks[a].start > tasks[b].end - tasks[b].start;
+    });
+    const int saved = threads_left_.exchange(0);  // no nested spawning
+    std::atomic<size_t> next{0};
+    auto worker = [&] {
+      for (size_t k; (k = next.fetch_add(1)) < by_size.size();) {
+        const Task &t = tasks[by_size[k]];
+        Build(subs[by_size[k]], t.start, t.end, t.depth);
+      }
+    };
+    const int hw = static_cast<int>(std::max(1u, std::thread::hardware_concurrency()));
+    std::vector<std::thread> pool;
+    for (int i = 1; i < hw && i < static_cast<int>(tasks.size()); ++i) pool.emplace_back(worker);
+    worker();
+    for (std::thread &th : pool) th.join();
+    threads_left_ = saved;
+    for (size_t i = 0; i < tasks.size(); ++i) {
+      const int32_t off = Splice(out, subs[i]);
+      out.nodes[tasks[i].node] = out.nodes[off];  // the copy at `off` is no longer referenced
+    }
+  }
+
+  int32_t task_refs_ = 0;
   std::vector<Ref> refs_;
 
  private:
@@ -198,15 +282,40 @@ class Builder {
       scale[axis] = extent > 0.0f ? kBins / extent : 0.0f;
       for (int b = 0; b < kBins; ++b) bin_box[axis][b] = EmptyBox();
     }
-    for (int32_t i = start; i < end; ++i) {
-      const Aabb &bx = refs_[i].box;
-      for (int axis = 0; axis < 3; ++axis) {
-        int b = std::min(kBins - 1, static_cast<int>((refs_[i].C(axis) - cbox.lo[axis]) * scale[axis]));
-        b = std::max(0, b);
-        ++bin_n[axis][b];
-        Grow(bin_box[axis][b], bx);
+    struct Bins {
+      Aabb box[3][kBins];
+      int32_t n[3][kBins];
+    };
+    auto bin = [&](int32_t a, int32_t b, Bins &out) {
+      for (int32_t i = a; i < b; ++i) {
+        const Aabb &bx = refs_[i].box;
+        for (int axis = 0; axis < 3; ++axis) {
+          int k = std::min(kBins - 1, static_cast<int>((refs_[i].C(axis) - cbox.lo[axis]) * scale[axis]));
+          k = std::max(0, k);
+          ++out.n[axis][k];
+          Grow(out.box[axis][k], bx);
+        }
       }
+    };
+    const int parts = n >= kParallelPass ? static_cast<int>(std::max(1u, std::thread::hardware_concurrency())) : 1;
+    std::vector<Bins> part(parts);
+    for (Bins &pb : part)
+      for (int axis = 0; axis < 3; ++axis)
+        for (int b = 0; b < kBins; ++b) pb.box[axis][b] = EmptyBox(), pb.n[axis][b] = 0;
+    if (parts == 1) {
+      bin(start, end, part[0]);
+    } else {
+      std::vector<std::thread> pool;
+      for (int k = 0; k < parts; ++k) {
+        const int32_t a = start + static_cast<int32_t>(int64_t(n) * k / parts);
+        const int32_t b = start + static_cast<int32_t>(int64_t(n) * (k + 1) / parts);
+        pool.emplace_back([&, a, b, k] { bin(a, b, part[k]); });
+      }
+      for (std::thread &t : pool) t.join();
     }
+    for (const Bins &pb : part)
+      for (int axis = 0; axis < 3; ++axis)
+        for (int b = 0; b < kBins; ++b) bin_n[axis][b] += pb.n[axis][b], Grow(bin_box[axis][b], pb.box[axis][b]);
     for (int axis = 0; axis < 3; ++axis) {
       if (!(cbox.hi[axis] - cbox.lo[axis] > 0.0f)) continue;
       float right_area[kBins];
@@ -304,7 +413,13 @@ void BuildBvh(const std::vector<Aabb> &boxes, int accel, int strategy, int max_l
     tree.max_leaf = leaf.count;
     root = 0;
   } else {
-    root = b.Build(tree, 0, static_cast<int32_t>(boxes.size()), 0);
+    // The top of the tree on this thread (large nodes bin on all threads),
+    // subtrees of about n / (2 threads) references on a thread pool.
+    const int64_t hw = std::max(1u, std::thread::hardware_concurrency());
+    b.task_refs_ = static_cast<int32_t>(std::max<int64_t>(4096, static_cast<int64_t>(boxes.size()) / (2 * hw)));
+    std::vector<Builder::Task> tasks;
+    root = b.Build(tree, 0, static_cast<int32_t>(boxes.size()), 0, &tasks);
+    b.BuildTasks(tree, tasks);
   }
   order->resize(boxes.size());
   last->assign(boxes.size(), 0);
@@ -513,6 +628,14 @@ bool BuildSceneImage(const MuonSceneDesc &desc, SceneImage *img, std::string *er
       *error = "primitive id out of range";
       return false;
     }
+  }
+  // Per-triangle records, on all host threads (each triangle writes its own
+  // slots), then the boxes of the triangles that can be hit in input order.
+  std::vector<Aabb> tri_box(ntri);
+  std::vector<uint8_t> tri_keep(ntri, 0);
+  ParallelFor(ntri, 1 << 14, [&](int64_t i0, int64_t i1) {
+  for (int64_t i = i0; i < i1; ++i) {
+    const MuonTriangleDesc &t = desc.triangles[i];
     mm::v3 ov[3] = {V3(t.v[0]), V3(t.v[1]), V3(t.v[2])};
     mm::v3 wv[3];
     mm::m4 m = t.transform >= 0 ? ToM4(desc.transforms[t.transform].object_to_world) : mm::identity4();
@@ -559,12 +682,17 @@ bool BuildSceneImage(const MuonSceneDesc &desc, SceneImage *img, std::string *er
     }
     // |d.n| <= |n| for a unit direction, so such a triangle is never hit.
     if (!(len_obj >= 1e-4f)) continue;
-    Aabb b;
+    Aabb &b = tri_box[i];
     for (int k = 0; k < 3; ++k) {
       b.lo[k] = std::min(std::min(mm::comp(wv[0], k), mm::comp(wv[1], k)), mm::comp(wv[2], k));
       b.hi[k] = std::max(std::max(mm::comp(wv[0], k), mm::comp(wv[1], k)), mm::comp(wv[2], k));
     }
-    boxes.push_back(b);
+    tri_keep[i] = 1;
+  }
+  });
+  for (int64_t i = 0; i < ntri; ++i) {
+    if (!tri_keep[i]) continue;
+    boxes.push_back(tri_box[i]);
     source.push_back(i);
   }
   std::vector<PrimRecord> sph_rec(nsph);
@@ -632,7 +760,9 @@ bool BuildSceneImage(const MuonSceneDesc &desc, SceneImage *img, std::string *er
   img->prims_obj.resize(order.size());
   img->shade.resize(order.size());
   if (img->any_smooth) img->smooth_normals.resize(3 * order.size()), img->smooth_normals_obj.resize(3 * order.size());
-  for (size_t slot = 0; slot < order.size(); ++slot) {
+  // Records into leaf order, on all host threads (each slot is written once).
+  ParallelFor(static_cast<int64_t>(order.size()), 1 << 14, [&](int64_t s0, int64_t s1) {
+  for (size_t slot = static_cast<size_t>(s0); slot < static_cast<size_t>(s1); ++slot) {
     int64_t src = source[order[slot]];
     PrimRecord r = src < ntri ? tri_rec[src] : sph_rec[src - ntri];
     PrimRecord ro = src < ntri ? tri_obj[src] : sph_rec[src - ntri];
@@ -653,6 +783,7 @@ bool BuildSceneImage(const MuonSceneDesc &desc, SceneImage *img, std::string *er
       }
     }
   }
+  });
   return true;
 }
 

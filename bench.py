@@ -200,16 +200,19 @@ def algorithmic_bytes(probe: dict, st: dict, slots: int) -> dict:
     return {"extend": ext, "occlude": occ, "shade": shade, "fold": fold}
 
 
-def traffic(workload: str, kernel: str) -> dict | None:
-    """DRAM bytes per launch of a kernel class from the committed ncu summary
-    (profiles/traffic.json: the capture command and the scaling stated there)."""
+def traffic(workload: str, kernel: str, rays_per_launch: float) -> dict | None:
+    """DRAM bytes per launch of a traversal kernel: the bytes per ray of one
+    ncu-captured launch of a smaller case (profiles/traffic.json, which gives
+    the capture and its scaling) times this frame's rays per launch."""
     path = os.path.join(ROOT, "profiles", "traffic.json")
     if not os.path.exists(path):
         return None
     entry = json.load(open(path)).get(workload, {}).get(kernel)
-    if entry is None:
+    if not entry:
         return None
-    return entry if isinstance(entry, dict) else {"bytes_per_launch": entry}
+    return {"bytes_per_launch": entry["bytes_per_ray"] * rays_per_launch,
+            "source": f"profiles/traffic.json: {entry['bytes_per_ray']} DRAM bytes per ray (ncu, one launch of "
+                      f"a 2^23-path wavefront) x {rays_per_launch:.0f} rays per launch"}
 
 
 def cpu_baseline(text: str, w: dict, budget_s: float = 10.0, steps: int = 1) -> dict:
@@ -250,7 +253,9 @@ def roofline(name: str, probe: dict, probe_stats: dict, last: dict) -> dict:
     pk = peaks()
     ce = ceilings()
     achieved = per_launch_bytes / (per_launch_ms * 1e-3) / 1e9
-    tr = traffic(name, dom)
+    rays_per_launch = {"extend": probe_stats["extend_rays"] / max(1, probe_stats["extend_launches"]),
+                       "occlude": probe_stats["occlude_rays"] / max(1, probe_stats["occlude_launches"])}
+    tr = traffic(name, dom, rays_per_launch[dom]) if dom in rays_per_launch else None
     out = {"kernel": dom, "bound": "hbm", "achieved": round(achieved, 1), "peak": pk["hbm_gbs"], "unit": "GB/s",
            "frac": round(achieved / pk["hbm_gbs"], 4), "traffic": None, "peak_source": pk["source"],
            "per_launch_bytes": int(per_launch_bytes), "per_launch_ms": round(per_launch_ms, 4),
@@ -262,7 +267,7 @@ def roofline(name: str, probe: dict, probe_stats: dict, last: dict) -> dict:
         out["traffic"] = int(tr["bytes_per_launch"])
         dram_gbs = tr["bytes_per_launch"] / (per_launch_ms * 1e-3) / 1e9
         out["frac_hbm_dram"] = round(dram_gbs / pk["hbm_gbs"], 4)
-        out["traffic_source"] = tr.get("source", "profiles/traffic.json")
+        out["traffic_source"] = tr["source"]
     # the host walk against the traversal kernels' own counters of the same render
     out["walk_vs_gpu_counters"] = {
         "extend_box_tests": round(probe["extend_box_tests"] / max(1, probe_stats["extend_box_tests"]), 4),

@@ -101,6 +101,14 @@ def test_dense_mesh_benchmark_hits_equal_the_reference():
     scene = m.Scene.from_string(text)
     same = _hit_parity(scene, text, fx, 1024, 0.9999)
     _debug_films(scene, fx, same, 1024)
+    # any hit against the reference's closest-hit distances
+    rays = _rays(text, fx, 1024)
+    hit = fx["hit"] == 1
+    d = fx["distance"]
+    far = np.where(hit, d * np.float32(1.001), np.float32(1e30)).astype(np.float32)
+    near = np.where(hit, d * np.float32(0.999), np.float32(1e30)).astype(np.float32)
+    assert np.array_equal(scene.occluded(rays[:, :3], rays[:, 3:], far, native.ISECT_EXACT), hit)
+    assert not scene.occluded(rays[:, :3], rays[:, 3:], near, native.ISECT_EXACT)[hit].any()
     scene.close()
 
 

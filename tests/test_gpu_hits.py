@@ -85,6 +85,24 @@ def test_occlusion_matches_closest_hit(lib, name, mode):
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("name", SCENES)
+def test_occlusion_matches_the_reference_distances(lib, name):
+    """Any hit (Structure::HasIntersection, muon/acceleration.cc:144-202)
+    against the reference's own closest-hit distances: something lies within
+    1.001 x the reference's distance exactly where the reference hit, and
+    nothing lies within 0.999 x it."""
+    fx = load(name)
+    scene = m.Scene.from_string(str(fx["scene"]))
+    rays = fx["rays"]
+    hit = fx["hit"] == 1
+    d = fx["distance"]
+    far = np.where(hit, d * np.float32(1.001), np.float32(1e30)).astype(np.float32)
+    near = np.where(hit, d * np.float32(0.999), np.float32(1e30)).astype(np.float32)
+    assert np.array_equal(scene.occluded(rays[:, :3], rays[:, 3:], far, native.ISECT_EXACT), hit)
+    assert not scene.occluded(rays[:, :3], rays[:, 3:], near, native.ISECT_EXACT)[hit].any()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", SCENES)
 @pytest.mark.parametrize("integrator", ["normals", "albedo", "depth"])
 def test_debug_integrators_are_bitwise_equal(lib, name, integrator):
     """NormalsTracer/AlbedoTracer/DepthTracer (muon/integration.cc:47-72) at

@@ -18,6 +18,7 @@ import numpy as np
 import pytest
 
 from conftest import GOLDEN, REFERENCE, reference_available
+from muon_gb300 import scenes
 from muon_gb300.imageio import read_image
 from oracle import port
 
@@ -106,3 +107,32 @@ def test_fp64_rebuild_agrees_with_fp32(name):
     rel = np.abs(d32[same] - d64[same]) / np.maximum(d64[same], 1e-30)
     print(f"{name}: FP32 vs FP64 distance max rel {rel.max():.3g}, ids equal {same.sum()}/{(id32 >= 0).sum()}")
     assert rel.max() <= FP32_VS_FP64[name]
+
+
+# The same statement on the benchmark scenes at full size: the reference
+# build's FP32 BVH hits at the fixture pixels against the FP64 rebuild.
+FP32_VS_FP64_FULL = {"dense_mesh_full": (lambda: scenes.dense_mesh(1024, 1024, 256, 10), 1024, 1e-5),
+                     "batch13": (lambda: scenes.batch_scene(13, 1), 256, 1e-5)}
+
+
+@pytest.mark.parametrize("name", sorted(FP32_VS_FP64_FULL))
+def test_fp64_rebuild_agrees_with_fp32_on_benchmark_scenes(name):
+    import zlib
+
+    make, width, bound = FP32_VS_FP64_FULL[name]
+    fx = np.load(f"{GOLDEN}/hits_{name}.npz")
+    text = make()
+    pix = fx["pixels"]
+    rays = port.camera_rays(text)[pix[:, 1] * width + pix[:, 0]]
+    assert zlib.crc32(np.ascontiguousarray(rays, dtype=np.float32).tobytes()) == int(fx["ray_crc"])
+    d64, id64, _, _ = port.intersect(text, rays, precision=64, linear=False)
+    hit = fx["hit"] == 1
+    assert np.array_equal(id64 >= 0, hit)
+    keyed = hit & (fx["prim_id"] >= 0)
+    same = keyed & (id64 == fx["prim_id"])
+    assert same.sum() >= 0.999 * keyed.sum()  # ids differ only where primitives meet
+    d32 = fx["distance"].astype(np.float64)
+    rel = np.abs(d32[same] - d64[same]) / d64[same]
+    print(f"{name}: FP32 vs FP64 distance max rel {rel.max():.3g}, median {np.median(rel):.3g}, "
+          f"ids equal {same.sum()}/{keyed.sum()}")
+    assert rel.max() <= bound

@@ -32,8 +32,9 @@ namespace muon_gpu {
 constexpr uint32_t kPrimSphere = 1u;   // record is a sphere (else triangle)
 constexpr uint32_t kPrimLast = 2u;     // last record of its leaf
 constexpr uint32_t kPrimSmooth = 4u;   // triangle interpolates vertex normals
-// Shading class of a primitive (bits 8..10 of the shading record's flags):
-// 3 * (is sphere) + BRDF (MUON_BRDF_*). Hits are shaded grouped by class.
+// Shading class of a primitive (bits 8..10 of the shading record's flags,
+// and of the primitive records' flags): 3 * (is sphere) + BRDF (MUON_BRDF_*).
+// Hits are shaded grouped by class.
 constexpr int kClassShift = 8;
 constexpr int kNumClasses = 6;
 constexpr int32_t kEmptyLink = INT32_MIN;

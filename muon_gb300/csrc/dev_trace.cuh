@@ -215,8 +215,13 @@ __device__ __forceinline__ void ObjectRay(const DevScene &s, RayPre &r, int xf, 
   if (xf < 0) {
     *o = V(r.o);
     *d = r.dn;
-  } else if (MUON_XF_CACHE && xf == r.cxf) {
+  } else if (MUON_XF_CACHE == 1 && xf == r.cxf) {
     *o = r.co;
+    *d = r.cd;
+  } else if (MUON_XF_CACHE == 2 && xf == r.cxf) {
+    // direction only (the normalisation is the costly part); the origin is
+    // carried again
+    *o = XPointExact(s.transforms[xf].w2o, V(r.o));
     *d = r.cd;
   } else {
     const DevTransform &T = s.transforms[xf];
@@ -224,7 +229,7 @@ __device__ __forceinline__ void ObjectRay(const DevScene &s, RayPre &r, int xf, 
     *d = XDirExact(T.w2o, V(r.d));
     if (MUON_XF_CACHE) {
       r.cxf = xf;
-      r.co = *o;
+      if (MUON_XF_CACHE == 1) r.co = *o;
       r.cd = *d;
     }
   }
@@ -496,6 +501,95 @@ __device__ __forceinline__ bool TravRun(const DevScene &s, RayPre &r, TravState 
     }
     if (t.sp == 0) return true;
     t.node = StackPop(t);
+    if (__popc(__activemask()) < min_active) return false;
+  }
+}
+
+// Speculative variant of TravRun (Aila and Laine, HPG 2009, "while-while"
+// with postponed leaves): a lane that reaches a leaf keeps it aside and
+// descends further from its stack until every lane still descending holds a
+// leaf, so that the warp tests leaves together instead of serialising inner
+// nodes of some lanes against leaves of others. Every leaf reached is tested;
+// only the order changes (exact-distance ties may resolve differently).
+#ifndef MUON_SPECULATIVE
+#define MUON_SPECULATIVE 1
+#endif
+template <bool kAnyHit, bool kStats, int kTriTest>
+__device__ __forceinline__ bool TravRunSpeculative(const DevScene &s, RayPre &r, TravState &t, TraceCounters *cnt,
+                                                   bool *overflow, int min_active) {
+  if (s.num_nodes == 0) return true;
+  auto next = [&] { t.node = t.sp == 0 ? kEmptyLink : StackPop(t); };
+  const PrimRecord *recs = kTriTest == MUON_ISECT_EXACT ? s.prims_obj : s.prims;
+  while (true) {
+    int leaf = 0;  // postponed leaf link (leaf links are negative; 0 = none)
+    while (t.node >= 0) {
+      float4 n0, n1, n2, n3f;
+      Load64B(s.nodes + t.node, n0, n1, n2, n3f);
+      const int4 n3 = make_int4(__float_as_int(n3f.x), __float_as_int(n3f.y), 0, 0);
+      float c0lox = n0.x * r.idir.x - r.ood.x, c0hix = n0.y * r.idir.x - r.ood.x;
+      float c0loy = n0.z * r.idir.y - r.ood.y, c0hiy = n0.w * r.idir.y - r.ood.y;
+      float c0loz = n2.x * r.idir.z - r.ood.z, c0hiz = n2.y * r.idir.z - r.ood.z;
+      float c1lox = n1.x * r.idir.x - r.ood.x, c1hix = n1.y * r.idir.x - r.ood.x;
+      float c1loy = n1.z * r.idir.y - r.ood.y, c1hiy = n1.w * r.idir.y - r.ood.y;
+      float c1loz = n2.z * r.idir.z - r.ood.z, c1hiz = n2.w * r.idir.z - r.ood.z;
+      float c0min = Max3(fminf(c0lox, c0hix), fminf(c0loy, c0hiy), fmaxf(fminf(c0loz, c0hiz), 0.0f));
+      float c0max = Min3(fmaxf(c0lox, c0hix), fmaxf(c0loy, c0hiy), fminf(fmaxf(c0loz, c0hiz), t.tmax));
+      float c1min = Max3(fminf(c1lox, c1hix), fminf(c1loy, c1hiy), fmaxf(fminf(c1loz, c1hiz), 0.0f));
+      float c1max = Min3(fmaxf(c1lox, c1hix), fmaxf(c1loy, c1hiy), fminf(fmaxf(c1loz, c1hiz), t.tmax));
+      bool h0 = c0min <= c0max, h1 = c1min <= c1max;
+      if (kStats) {
+        cnt->box_tests += 2;
+        cnt->box_hits += (int)h0 + (int)h1;
+      }
+      if (!h0 && !h1) {
+        next();
+      } else {
+        int near = h0 ? n3.x : n3.y;
+        if (h0 && h1) {
+          int far = n3.y;
+          if (c1min < c0min) {
+            near = n3.y;
+            far = n3.x;
+          }
+          if (t.sp < kStackSize) StackPush(t, far);
+          else *overflow = true;
+        }
+        t.node = near;
+      }
+      if (t.node < 0 && t.node != kEmptyLink && leaf == 0) {
+        leaf = t.node;  // postpone this leaf and keep descending
+        next();
+      }
+      if (!__any_sync(__activemask(), leaf == 0)) break;
+    }
+    // the postponed leaf, then the current node for as long as it is a leaf
+    if (leaf == 0 && t.node < 0 && t.node != kEmptyLink) {
+      leaf = t.node;
+      next();
+    }
+    while (leaf != 0) {
+      for (int i = ~leaf;; ++i) {
+        PrimRecord p = LoadPrim(recs, i);
+        uint32_t flags = __float_as_uint(p.p3.w);
+        float t_obj = 0.0f;
+        float d = PrimTest<kTriTest>(s, r, p, flags, &t_obj);
+        if (kStats) cnt->prim_tests += 1;
+        if (d > 0.0f && d < t.tmax) {
+          if (kStats) cnt->prim_hits += 1;
+          t.tmax = d;
+          t.hit = i;
+          t.t_obj = t_obj;
+          if (kAnyHit) return true;
+        }
+        if (flags & kPrimLast) break;
+      }
+      leaf = 0;
+      if (t.node < 0 && t.node != kEmptyLink) {
+        leaf = t.node;
+        next();
+      }
+    }
+    if (t.node == kEmptyLink) return true;
     if (__popc(__activemask()) < min_active) return false;
   }
 }

@@ -331,12 +331,20 @@ __device__ __forceinline__ void PersistentTraverse(const DevScene &s, int n, uin
       }
     }
     if (!__any_sync(0xffffffffu, ray >= 0)) break;
-    if (ray >= 0 && TravRun<kAnyHit, kStats, kMode>(s, r, t, &c, &overflow, kRefillThreshold)) {
+    if (ray >= 0 && (MUON_SPECULATIVE ? TravRunSpeculative<kAnyHit, kStats, kMode>(s, r, t, &c, &overflow,
+                                                                                    kRefillThreshold)
+                                      : TravRun<kAnyHit, kStats, kMode>(s, r, t, &c, &overflow, kRefillThreshold))) {
       finish(ray, t);
       ray = -1;
     }
   }
 }
+
+// The extend kernel reads a hit's shading class from its primitive record (1)
+// or its shading record (0).
+#ifndef MUON_CLASS_FROM_PRIM
+#define MUON_CLASS_FROM_PRIM 1
+#endif
 
 template <bool kStats, int kTri>
 __global__ void __launch_bounds__(kBlock, MUON_TRAVERSAL_MIN_BLOCKS) ExtendKernel(DevScene s, PathBuffers b, WaveCounters wc, int bounce) {
@@ -359,7 +367,14 @@ __global__ void __launch_bounds__(kBlock, MUON_TRAVERSAL_MIN_BLOCKS) ExtendKerne
         // Group hits by shading class for the shading kernel (one atomic per
         // class per group of lanes finishing together); a miss ends its path.
         int cls = kNumClasses;
+#if MUON_CLASS_FROM_PRIM
+        // the hit's record was just tested, so its flags are likely in L1
+        if (t.hit >= 0)
+          cls = (__float_as_uint(__ldg(&(kTri == MUON_ISECT_EXACT ? s.prims_obj : s.prims)[t.hit].p3.w)) >>
+                 kClassShift) & 7;
+#else
         if (t.hit >= 0) cls = (__ldg(&s.shade[t.hit].s1.w) >> kClassShift) & 7;
+#endif
         const unsigned active = __activemask();
         const unsigned peers = __match_any_sync(active, cls);
         const int lane = threadIdx.x & 31;

@@ -666,7 +666,9 @@ bool BuildSceneImage(const MuonSceneDesc &desc, SceneImage *img, std::string *er
     std::memcpy(&brdf_eff, &img->materials[t.material].emission.w, 4);
     const uint32_t shade_flags = flags | (static_cast<uint32_t>(brdf_eff) << kClassShift);
     s.s1 = I4{t.light >= 0 ? quad_index[t.light] : -1, t.prim_id, t.transform, static_cast<int32_t>(shade_flags)};
-    std::memcpy(&r.p3.w, &flags, 4);
+    // the primitive record carries the shading class too (read by the extend
+    // kernel from the record it has just tested)
+    std::memcpy(&r.p3.w, &shade_flags, 4);
     ro.p3 = r.p3;
     ro.p3.x = n_obj.x, ro.p3.y = n_obj.y, ro.p3.z = n_obj.z;
     if (t.smooth) {
@@ -713,13 +715,13 @@ bool BuildSceneImage(const MuonSceneDesc &desc, SceneImage *img, std::string *er
     r.p1 = MakeF4(0.0f, IntBits(s.transform), 0.0f, 0.0f);
     r.p2 = MakeF4(0, 0, 0, 0);
     r.p3 = MakeF4(0, 0, 0, 0);
-    std::memcpy(&r.p3.w, &flags, 4);
     ShadeRecord &sh = sph_shade[j];
     sh.s0 = MakeF4(0, 0, 0, IntBits(s.material));
     int32_t sph_brdf;
     std::memcpy(&sph_brdf, &img->materials[s.material].emission.w, 4);
     const uint32_t sph_flags = flags | (static_cast<uint32_t>(3 + sph_brdf) << kClassShift);
     sh.s1 = I4{-1, s.prim_id, s.transform, static_cast<int32_t>(sph_flags)};
+    std::memcpy(&r.p3.w, &sph_flags, 4);
     // World bounds: the object box's 8 corners transformed (Bounds::Transform,
     // muon/bounds.cc:52-69).
     mm::v3 c = V3(s.center);

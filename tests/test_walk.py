@@ -63,9 +63,13 @@ def test_host_walk_rejects_watertight_mode(lib):
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("name,kwargs", [("cornell", {}), ("sphere_field", {}), ("dense_mesh", {"level": 4})])
-def test_probe_counts_equal_the_gpu_counters(lib, name, kwargs):
-    """Every queued ray of a small render walked on the host: box and
-    primitive tests equal what the traversal kernels counted."""
+def test_probe_counts_match_the_gpu_counters(lib, name, kwargs):
+    """Every queued ray of a small render walked on the host, in the ordered
+    visiting sequence: the traversal kernels count the same work plus what
+    their speculative descent adds (a lane that postpones a leaf descends
+    further before the leaf's hit shortens the ray), never less, and at most
+    a fifth more (13% on the sphere field, whose lanes often reach leaves
+    together)."""
     if name == "cornell":
         text = scenes.cornell(32, 32, 4, 5, 1)
     elif name == "sphere_field":
@@ -82,9 +86,10 @@ def test_probe_counts_equal_the_gpu_counters(lib, name, kwargs):
                       (pr["extend_prim_tests"], st["extend_prim_tests"]),
                       (pr["occlude_box_tests"], st["occlude_box_tests"]),
                       (pr["occlude_prim_tests"], st["occlude_prim_tests"])]:
-        assert abs(host - gpu) <= 1e-3 * gpu + 2
+        assert 0.8 * gpu <= host <= gpu * 1.001 + 2
     print(f"{name}: extend {st['extend_box_tests']} box / {st['extend_prim_tests']} prim tests, host "
-          f"{pr['extend_box_tests']:.0f} / {pr['extend_prim_tests']:.0f}")
+          f"{pr['extend_box_tests']:.0f} / {pr['extend_prim_tests']:.0f}; occlude {st['occlude_box_tests']} / "
+          f"{st['occlude_prim_tests']}, host {pr['occlude_box_tests']:.0f} / {pr['occlude_prim_tests']:.0f}")
 
 
 @pytest.mark.gpu
@@ -98,7 +103,7 @@ def test_probe_sample_estimates_the_whole_render(lib):
     assert pr["extend_walked"]["rays"] < st["extend_rays"]
     for host, gpu in [(pr["extend_box_tests"], st["extend_box_tests"]),
                       (pr["occlude_box_tests"], st["occlude_box_tests"])]:
-        assert abs(host / gpu - 1) < 0.05
+        assert 0.8 < host / gpu < 1.05
 
 
 @pytest.mark.gpu

@@ -284,7 +284,7 @@ __global__ void __launch_bounds__(kBlock) CameraBatchKernel(const BatchScene *sc
 // full while the work per ray varies (dynamic fetch, after Aila and Laine,
 // "Understanding the Efficiency of Ray Traversal on GPUs", HPG 2009).
 #ifndef MUON_REFILL_THRESHOLD
-#define MUON_REFILL_THRESHOLD 20
+#define MUON_REFILL_THRESHOLD 24
 #endif
 constexpr int kRefillThreshold = MUON_REFILL_THRESHOLD;
 // Minimum resident blocks per SM the traversal kernels are compiled for.

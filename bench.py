@@ -18,7 +18,8 @@ Metric: Mrays/s counted as the reference counts rays (primary + secondary,
 the MIS-sampled ray included; shadow rays excluded, muon/integration.cc:34-38,
 483), over device time with the scene resident and the film in device memory.
 `e2e` is the same metric through the public API with host buffers: scene
-upload (BVH build + copy) and the host film read-back inside every step.
+creation (records on the host, upload, BVH built on the device) and the host
+film read-back inside every step.
 
 Roofline of the dominant kernel class: algorithmic bytes per launch from the
 host walk of the flattened BVH over sampled queue rays
@@ -28,7 +29,7 @@ measured HBM copy peak; beside it the DRAM bytes the kernel moves (ncu, from
 profiles/traffic.json) and the L1 / L2 read ceilings measured live.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                  [--workload NAME] [--builder host|gpu]
+                  [--workload NAME] [--builder auto|gpu_sah|host|gpu]
 
 `--workload NAME` measures one configuration alone. With N > 1 (torchrun),
 every rank renders its own replica of each frame with a distinct seed (weak
@@ -362,7 +363,8 @@ def measure_frames(name: str, w: dict, steps: int, warmup: int, builder: str, wi
         "warmup": warmup, "counted_rays_per_step": counted // steps,
         "e2e": {"value": round(e2e_value, 2), "unit": METRIC, "h2d_bytes_per_step": int(desc_bytes),
                 "d2h_bytes_per_step": int(film_bytes),
-                "note": "scene upload (BVH build + copy) + render + film read-back into pinned host memory per step"},
+                "note": "scene create (host records, upload, BVH build) + render + film read-back into pinned "
+                        "host memory per step"},
         "gpu_launches": int(launches), "clocks": clocks.summary(), "wall_s": round(wall, 3),
     }
     if rank == 0:
@@ -705,8 +707,10 @@ def main() -> None:
     ap.add_argument("--workload", choices=["all"] + sorted(WORKLOADS), default="all",
                     help="all (default): the dense mesh as the headline with the other configurations as "
                          "sub-objects of the same line; or one configuration alone")
-    ap.add_argument("--builder", choices=["host", "gpu"], default="host",
-                    help="BVH builder: binned SAH on the host, or the linear BVH built on the GPU")
+    ap.add_argument("--builder", choices=["auto", "gpu_sah", "host", "gpu"], default="auto",
+                    help="BVH builder: binned SAH on the GPU (the same tree as the host's; 'auto', the default, "
+                         "builds scenes of fewer than 256 primitives on the host), binned SAH on the host threads, "
+                         "or the linear BVH built on the GPU")
     ap.add_argument("--guide-targets", choices=["direct", "all"], default=None,
                     help="guiding workload: what the network learns (default: direct light)")
     ap.add_argument("--mixture-fraction", type=float, default=None,

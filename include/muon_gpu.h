@@ -91,9 +91,14 @@ extern "C" {
 /* BVH builders (MuonSceneDesc.builder). HOST_SAH: binned SAH on the host
  * threads (acceleration and partition_strategy apply). GPU_LBVH: linear BVH
  * over Morton-sorted centroids on the device (Karras 2012), leaves of at most
- * 4 primitives; much faster to build, somewhat slower to traverse. */
+ * 4 primitives; much faster to build, somewhat slower to traverse. GPU_SAH:
+ * the host builder's binned SAH run on the device, with the same split
+ * decisions and so the same nodes and boxes (references inside a leaf keep
+ * their input order, nodes are numbered differently); partition_strategy
+ * must be SAH, max_leaf_size applies. */
 #define MUON_BUILDER_HOST_SAH 0
 #define MUON_BUILDER_GPU_LBVH 1
+#define MUON_BUILDER_GPU_SAH 2
 
 /* render flags */
 #define MUON_RENDER_STATS 1u      /* count bounds/object tests (slower)        */
@@ -428,6 +433,25 @@ int muon_gpu_render_batch(MuonScene *const *scenes, const MuonRenderParams *para
 /* The CUDA stream (cudaStream_t) all of this scene's work is launched on, for
  * callers that time or order work around it with CUDA events. */
 int muon_gpu_scene_stream(const MuonScene *scene, void **stream);
+
+/* The scene's BVH as its kernels read it, with the build's statistics
+ * (the BVH of Structure::Init, muon/acceleration.cc:204-458). */
+typedef struct MuonBvhInfo {
+  int64_t nodes;     /* 64-byte nodes (two child boxes and links; node 0 is the root) */
+  int64_t slots;     /* primitive records, in leaf order */
+  int64_t leaves;
+  int32_t max_depth; /* deepest node, the root at depth 0 (leaves included) */
+  int32_t max_leaf;  /* most primitives in one leaf */
+} MuonBvhInfo;
+/* Fills *info; then, where not null, copies info->nodes nodes into `nodes`
+ * (the device layout: per node the child boxes (c0.lo.x, c0.hi.x, c0.lo.y,
+ * c0.hi.y), (c1.lo.x, c1.hi.x, c1.lo.y, c1.hi.y), (c0.lo.z, c0.hi.z, c1.lo.z,
+ * c1.hi.z) as floats, then the links (link0, link1, 0, 0) as int32: >= 0 an
+ * interior node, < 0 a leaf whose first slot is ~link), and per slot the
+ * primitive's id (`slot_prim`, MuonTriangleDesc/MuonSphereDesc.prim_id) and
+ * whether the slot ends its leaf (`slot_last`). */
+int muon_gpu_scene_bvh(const MuonScene *scene, MuonBvhInfo *info, void *nodes, int32_t *slot_prim,
+                       uint8_t *slot_last);
 
 /* ---- learned path guiding --------------------------------------------
  * No counterpart in the reference (which has no learned component): a small

@@ -539,6 +539,7 @@ int muon_gpu_batch_create(MuonScene *const *scenes, int32_t n, MuonBatch **out) 
   std::unique_ptr<MuonBatch> b;
   try {
     b.reset(new MuonBatch());
+    for (int i = 0; i < n; ++i) SyncSceneImage(scenes[i]);
     b->n = n;
     b->device = views[0].device;
     CUDA_TRY(cudaSetDevice(b->device));

@@ -82,6 +82,13 @@ void Upload(DeviceBuffer &buf, const std::vector<T> &v, cudaStream_t st) {
   if (!v.empty()) CUDA_TRY(cudaMemcpyAsync(buf.ptr, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, st));
 }
 
+// Upload into a block of the device block cache (EnsurePooled).
+template <typename T>
+void UploadPooled(DeviceBuffer &buf, const std::vector<T> &v, cudaStream_t st, int device) {
+  EnsurePooled(buf, std::max<size_t>(v.size() * sizeof(T), 16), device);
+  if (!v.empty()) CUDA_TRY(cudaMemcpyAsync(buf.ptr, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, st));
+}
+
 struct EventPair {
   cudaEvent_t a = nullptr, b = nullptr;
   int kind = 0;  // 0 extend, 1 occlude, 2 other

@@ -86,6 +86,11 @@ int main(int argc, char **argv) {
     std::fprintf(stderr, "unknown value for partition_strategy\n");
     return 1;
   }
+  // the SAH tree is built on the device (the same tree as the host builder's)
+  // unless the scene is so small that the host is faster
+  desc.builder = desc.partition_strategy == MUON_PARTITION_SAH && desc.num_triangles + desc.num_spheres >= 256
+                     ? MUON_BUILDER_GPU_SAH
+                     : MUON_BUILDER_HOST_SAH;
   if (!samples.empty()) params.pixel_samples = std::atoi(samples.c_str());
   if (!seed.empty()) params.seed = std::strtoull(seed.c_str(), nullptr, 10);
   params.intersect_mode = tri == "watertight" ? MUON_ISECT_WATERTIGHT : (tri == "fast" ? MUON_ISECT_FAST : MUON_ISECT_EXACT);

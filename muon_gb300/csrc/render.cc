@@ -40,6 +40,10 @@ struct MuonScene {
   int device = 0;
   cudaStream_t stream = nullptr;
   SceneImage img;
+  // The leaf-order records of a scene whose BVH was built on the device live
+  // on the device only (img holds them in input order) until a host reader
+  // calls SyncSceneImage.
+  mutable bool host_records_stale = false;
   DevScene dev{};
   DevCamera cam{};
   // scene arrays
@@ -77,7 +81,7 @@ struct MuonScene {
         PoolGive(rad[k], device);
       }
       for (DeviceBuffer *b : {&hits, &link, &final_rad, &org, &contrib, &slot_dir, &shq, &order, &film_sum, &film_sq,
-                              &film_cnt})
+                              &film_cnt, &nodes, &prims, &prims_obj, &shade, &smooth, &smooth_obj})
         PoolGive(*b, device);
     }
     if (graph) cudaGraphExecDestroy(graph);
@@ -210,34 +214,56 @@ void ComputeCamera(const MuonCameraDesc &c, DevCamera *out) {
 }
 
 // Builds the BVH of a scene whose records BuildSceneImage left in input
-// order (defer_bvh): linear BVH on the device, records gathered into leaf
-// order in the scene's buffers, and the result copied back into the host
-// image so that host-side users (batch merge, scene box) see the same data.
-void BuildBvhOnGpu(MuonScene *sc, cudaStream_t st) {
+// order (defer_bvh) on the device (binned SAH or linear BVH), records
+// gathered into leaf order in the scene's buffers, and the result copied
+// back into the host image so that host-side users (batch merge, scene box)
+// see the same data. Returns MUON_OK or an error code (last error set).
+int BuildBvhOnGpu(MuonScene *sc, int builder, int max_leaf, cudaStream_t st) {
   SceneImage &im = sc->img;
   const int n = static_cast<int>(im.prims.size());
-  const int nn = std::max(n - 1, 1);
+  int nn = std::max(n - 1, 1);
+  // temporaries come from (and go back to) the device block cache
   DeviceBuffer boxes, in_prims, in_obj, in_shade, in_sn, in_sno, scratch, order, last;
-  Upload(boxes, im.boxes, st);
-  Upload(in_prims, im.prims, st);
-  Upload(in_obj, im.prims_obj, st);
-  Upload(in_shade, im.shade, st);
+  DeviceBuffer *const temps[] = {&boxes, &in_prims, &in_obj, &in_shade, &in_sn, &in_sno, &scratch, &order, &last};
+  struct GiveBack {
+    DeviceBuffer *const *bufs;
+    int count;
+    cudaStream_t st;
+    int device;
+    ~GiveBack() {
+      if (cudaStreamSynchronize(st) == cudaSuccess)
+        for (int i = 0; i < count; ++i) PoolGive(*bufs[i], device);
+    }
+  } give_back{temps, 9, st, sc->device};
+  UploadPooled(boxes, im.boxes, st, sc->device);
+  UploadPooled(in_prims, im.prims, st, sc->device);
+  UploadPooled(in_obj, im.prims_obj, st, sc->device);
+  UploadPooled(in_shade, im.shade, st, sc->device);
   if (im.any_smooth) {
-    Upload(in_sn, im.smooth_normals, st);
-    Upload(in_sno, im.smooth_normals_obj, st);
+    UploadPooled(in_sn, im.smooth_normals, st, sc->device);
+    UploadPooled(in_sno, im.smooth_normals_obj, st, sc->device);
   }
-  const size_t sbytes = GpuLbvhScratchBytes(n);
-  scratch.Ensure(sbytes);
-  order.Ensure(sizeof(int32_t) * n);
-  last.Ensure(static_cast<size_t>(n));
-  sc->nodes.Ensure(sizeof(BvhNode) * nn);
-  sc->prims.Ensure(sizeof(PrimRecord) * n);
-  sc->prims_obj.Ensure(sizeof(PrimRecord) * n);
-  sc->shade.Ensure(sizeof(ShadeRecord) * n);
-  sc->smooth.Ensure(im.any_smooth ? sizeof(F4) * 3 * n : 16);
-  sc->smooth_obj.Ensure(im.any_smooth ? sizeof(F4) * 3 * n : 16);
-  LaunchGpuLbvh(boxes.as<float>(), n, scratch.ptr, sbytes, sc->nodes.as<BvhNode>(), order.as<int32_t>(),
-                last.as<uint8_t>(), st);
+  const bool sah = builder == MUON_BUILDER_GPU_SAH;
+  const size_t sbytes = sah ? GpuSahScratchBytes(n) : GpuLbvhScratchBytes(n);
+  EnsurePooled(scratch, sbytes, sc->device);
+  EnsurePooled(order, sizeof(int32_t) * n, sc->device);
+  EnsurePooled(last, static_cast<size_t>(n), sc->device);
+  EnsurePooled(sc->nodes, sizeof(BvhNode) * nn, sc->device);
+  EnsurePooled(sc->prims, sizeof(PrimRecord) * n, sc->device);
+  EnsurePooled(sc->prims_obj, sizeof(PrimRecord) * n, sc->device);
+  EnsurePooled(sc->shade, sizeof(ShadeRecord) * n, sc->device);
+  EnsurePooled(sc->smooth, im.any_smooth ? sizeof(F4) * 3 * n : 16, sc->device);
+  EnsurePooled(sc->smooth_obj, im.any_smooth ? sizeof(F4) * 3 * n : 16, sc->device);
+  GpuSahResult sr;
+  if (sah) {
+    CUDA_TRY(BuildGpuSah(boxes.as<float>(), n, max_leaf, scratch.ptr, sc->nodes.as<BvhNode>(), order.as<int32_t>(),
+                         last.as<uint8_t>(), &sr, st));
+    if (sr.error) return Fail(MUON_ERR_CUDA, "device BVH build: internal list or stack limit reached");
+    nn = sr.nodes;
+  } else {
+    LaunchGpuLbvh(boxes.as<float>(), n, scratch.ptr, sbytes, sc->nodes.as<BvhNode>(), order.as<int32_t>(),
+                  last.as<uint8_t>(), st);
+  }
   LaunchGatherPrims(order.as<int32_t>(), last.as<uint8_t>(), n, in_prims.as<PrimRecord>(), in_obj.as<PrimRecord>(),
                     in_shade.as<ShadeRecord>(), im.any_smooth ? in_sn.as<F4>() : nullptr,
                     im.any_smooth ? in_sno.as<F4>() : nullptr, sc->prims.as<PrimRecord>(),
@@ -246,8 +272,23 @@ void BuildBvhOnGpu(MuonScene *sc, cudaStream_t st) {
                     st);
   CUDA_TRY(cudaGetLastError());
   im.nodes.resize(nn);
-  std::vector<int32_t> h_order(n);
   CUDA_TRY(cudaMemcpyAsync(im.nodes.data(), sc->nodes.ptr, sizeof(BvhNode) * nn, cudaMemcpyDeviceToHost, st));
+  if (sah) {
+    // the records stay on the device until a host reader asks for them
+    // (SyncSceneImage); the scene box and the node count come from the nodes
+    CUDA_TRY(cudaStreamSynchronize(st));
+    im.boxes.clear();
+    im.boxes.shrink_to_fit();
+    sc->host_records_stale = true;
+    BvhBuildStats &bs = im.bvh;
+    bs = BvhBuildStats();
+    bs.nodes = nn;
+    // the builder's own counts, with the host builder's depth convention
+    bs.leaves = sr.leaves;
+    bs.max_depth = sr.max_depth;
+    bs.max_leaf = sr.max_leaf;
+    return MUON_OK;
+  }
   CUDA_TRY(cudaMemcpyAsync(im.prims.data(), sc->prims.ptr, sizeof(PrimRecord) * n, cudaMemcpyDeviceToHost, st));
   CUDA_TRY(cudaMemcpyAsync(im.prims_obj.data(), sc->prims_obj.ptr, sizeof(PrimRecord) * n, cudaMemcpyDeviceToHost,
                            st));
@@ -258,15 +299,14 @@ void BuildBvhOnGpu(MuonScene *sc, cudaStream_t st) {
     CUDA_TRY(cudaMemcpyAsync(im.smooth_normals_obj.data(), sc->smooth_obj.ptr, sizeof(F4) * 3 * n,
                              cudaMemcpyDeviceToHost, st));
   }
-  CUDA_TRY(cudaMemcpyAsync(h_order.data(), order.ptr, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, st));
   CUDA_TRY(cudaStreamSynchronize(st));
   im.boxes.clear();
   im.boxes.shrink_to_fit();
   for (int slot = 0; slot < n; ++slot) im.leaf_of_prim_id[im.shade[slot].s1.y] = slot;
-  // statistics: depth (iterative walk from the root) and leaves
   BvhBuildStats &bs = im.bvh;
   bs = BvhBuildStats();
   bs.nodes = nn;
+  // statistics: depth (iterative walk from the root) and leaves
   std::vector<std::pair<int32_t, int32_t>> stack{{0, 1}};
   while (!stack.empty()) {
     auto [node, depth] = stack.back();
@@ -289,6 +329,7 @@ void BuildBvhOnGpu(MuonScene *sc, cudaStream_t st) {
       }
     }
   }
+  return MUON_OK;
 }
 
 // ShadeParams of a render (PathTracer settings and the shadow-slot layout of
@@ -773,9 +814,13 @@ int muon_gpu_scene_create(const MuonSceneDesc *desc, MuonScene **out) {
   try {
     sc.reset(new MuonScene());
     std::string err;
-    if (desc->builder != MUON_BUILDER_HOST_SAH && desc->builder != MUON_BUILDER_GPU_LBVH)
+    if (desc->builder != MUON_BUILDER_HOST_SAH && desc->builder != MUON_BUILDER_GPU_LBVH &&
+        desc->builder != MUON_BUILDER_GPU_SAH)
       return Fail(MUON_ERR_INVALID_ARG, "unknown BVH builder");
-    const bool gpu_bvh = desc->builder == MUON_BUILDER_GPU_LBVH && desc->acceleration == MUON_ACCEL_BVH;
+    if (desc->builder == MUON_BUILDER_GPU_SAH && desc->acceleration == MUON_ACCEL_BVH &&
+        desc->partition_strategy != MUON_PARTITION_SAH)
+      return Fail(MUON_ERR_INVALID_ARG, "the GPU SAH builder takes the SAH partition strategy only");
+    const bool gpu_bvh = desc->builder != MUON_BUILDER_HOST_SAH && desc->acceleration == MUON_ACCEL_BVH;
     if (!BuildSceneImage(*desc, &sc->img, &err, gpu_bvh)) return Fail(MUON_ERR_INVALID_ARG, err);
     if (sc->img.bvh.max_depth >= 60) return Fail(MUON_ERR_INVALID_ARG, "BVH too deep for the traversal stack");
     int ndev = 0;
@@ -797,15 +842,16 @@ int muon_gpu_scene_create(const MuonSceneDesc *desc, MuonScene **out) {
     cudaStream_t st = sc->stream;
     const SceneImage &im = sc->img;
     if (gpu_bvh && !im.prims.empty()) {
-      BuildBvhOnGpu(sc.get(), st);
+      const int rc = BuildBvhOnGpu(sc.get(), desc->builder, desc->max_leaf_size > 0 ? desc->max_leaf_size : 4, st);
+      if (rc != MUON_OK) return rc;
       if (sc->img.bvh.max_depth >= 60) return Fail(MUON_ERR_INVALID_ARG, "BVH too deep for the traversal stack");
     } else {
-      Upload(sc->nodes, im.nodes, st);
-      Upload(sc->prims, im.prims, st);
-      Upload(sc->prims_obj, im.prims_obj, st);
-      Upload(sc->shade, im.shade, st);
-      Upload(sc->smooth, im.smooth_normals, st);
-      Upload(sc->smooth_obj, im.smooth_normals_obj, st);
+      UploadPooled(sc->nodes, im.nodes, st, sc->device);
+      UploadPooled(sc->prims, im.prims, st, sc->device);
+      UploadPooled(sc->prims_obj, im.prims_obj, st, sc->device);
+      UploadPooled(sc->shade, im.shade, st, sc->device);
+      UploadPooled(sc->smooth, im.smooth_normals, st, sc->device);
+      UploadPooled(sc->smooth_obj, im.smooth_normals_obj, st, sc->device);
     }
     Upload(sc->transforms, im.transforms, st);
     Upload(sc->materials, im.materials, st);
@@ -971,6 +1017,7 @@ int muon_gpu_probe_traversal(MuonScene *scene, const MuonRenderParams *params, i
   *out = MuonTraversalProbe{};
   try {
     CUDA_TRY(cudaSetDevice(scene->device));
+    SyncSceneImage(scene);  // the host walk reads the scene's own leaf-order records
     const size_t np = static_cast<size_t>(scene->img.width) * scene->img.height;
     EnsurePooled(scene->film_sum, 3 * np * sizeof(double), scene->device);
     EnsurePooled(scene->film_sq, 3 * np * sizeof(double), scene->device);
@@ -1085,9 +1132,57 @@ int muon_gpu_scene_stream(const MuonScene *scene, void **stream) {
   return MUON_OK;
 }
 
+int muon_gpu_scene_bvh(const MuonScene *scene, MuonBvhInfo *info, void *nodes, int32_t *slot_prim,
+                       uint8_t *slot_last) {
+  if (!scene || !info) return Fail(MUON_ERR_INVALID_ARG, "null argument");
+  try {
+    SyncSceneImage(scene);
+  } catch (const CudaError &e) {
+    return FailCuda(e);
+  }
+  const SceneImage &im = scene->img;
+  info->nodes = static_cast<int64_t>(im.nodes.size());
+  info->slots = static_cast<int64_t>(im.shade.size());
+  info->leaves = im.bvh.leaves;
+  info->max_depth = im.bvh.max_depth;
+  info->max_leaf = im.bvh.max_leaf;
+  if (nodes && !im.nodes.empty()) std::memcpy(nodes, im.nodes.data(), sizeof(BvhNode) * im.nodes.size());
+  for (size_t slot = 0; slot < im.shade.size(); ++slot) {
+    if (slot_prim) slot_prim[slot] = im.shade[slot].s1.y;
+    if (slot_last) {
+      uint32_t flags;
+      std::memcpy(&flags, &im.prims[slot].p3.w, 4);
+      slot_last[slot] = (flags & kPrimLast) ? 1 : 0;
+    }
+  }
+  return MUON_OK;
+}
+
 }  // extern "C"
 
 namespace muon_gpu {
+
+void SyncSceneImage(const MuonScene *scene) {
+  if (!scene || !scene->host_records_stale) return;
+  MuonScene *sc = const_cast<MuonScene *>(scene);  // img is a host cache of the device arrays
+  SceneImage &im = sc->img;
+  const size_t n = im.prims.size();
+  cudaStream_t st = sc->stream;
+  CUDA_TRY(cudaSetDevice(sc->device));
+  CUDA_TRY(cudaMemcpyAsync(im.prims.data(), sc->prims.ptr, sizeof(PrimRecord) * n, cudaMemcpyDeviceToHost, st));
+  CUDA_TRY(cudaMemcpyAsync(im.prims_obj.data(), sc->prims_obj.ptr, sizeof(PrimRecord) * n, cudaMemcpyDeviceToHost,
+                           st));
+  CUDA_TRY(cudaMemcpyAsync(im.shade.data(), sc->shade.ptr, sizeof(ShadeRecord) * n, cudaMemcpyDeviceToHost, st));
+  if (im.any_smooth) {
+    CUDA_TRY(cudaMemcpyAsync(im.smooth_normals.data(), sc->smooth.ptr, sizeof(F4) * 3 * n, cudaMemcpyDeviceToHost,
+                             st));
+    CUDA_TRY(cudaMemcpyAsync(im.smooth_normals_obj.data(), sc->smooth_obj.ptr, sizeof(F4) * 3 * n,
+                             cudaMemcpyDeviceToHost, st));
+  }
+  CUDA_TRY(cudaStreamSynchronize(st));
+  for (size_t slot = 0; slot < n; ++slot) im.leaf_of_prim_id[im.shade[slot].s1.y] = static_cast<int32_t>(slot);
+  sc->host_records_stale = false;
+}
 
 bool GetSceneView(const MuonScene *scene, SceneView *out) {
   if (!scene || !out) return false;

@@ -20,6 +20,11 @@ struct SceneView {
 };
 
 // Fills `out` from a scene created by muon_gpu_scene_create; false if null.
+// The view's host image holds the leaf-order records only after
+// SyncSceneImage.
 bool GetSceneView(const MuonScene *scene, SceneView *out);
+// Copies a device-built scene's records back into its host image (once);
+// throws CudaError.
+void SyncSceneImage(const MuonScene *scene);
 
 }  // namespace muon_gpu

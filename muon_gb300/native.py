@@ -20,6 +20,8 @@ NEE = {"off": 0, "on": 1, "mis": 2}
 IMPORTANCE = {"hemisphere": 0, "cosine": 1, "brdf": 2}
 ISECT_FAST, ISECT_WATERTIGHT, ISECT_EXACT = 0, 1, 2
 ACCEL_LINEAR, ACCEL_BVH = 0, 1
+# MUON_BUILDER_*: host binned SAH, device linear BVH ("gpu"), device binned SAH
+BUILDER = {"host": 0, "gpu": 1, "gpu_lbvh": 1, "gpu_sah": 2}  # Scene also takes "auto"
 PARTITION = {"uniform": 0, "midpoint": 1, "sah": 2}
 RENDER_STATS, RENDER_ACCUMULATE, RENDER_TIMING, RENDER_NO_GRAPH = 1, 2, 4, 8
 NOALLOC_SCRATCH_BYTES = 64 << 20
@@ -122,6 +124,11 @@ class TraversalProbe(C.Structure):
                 ("occlude_box_tests", C.c_double), ("occlude_prim_tests", C.c_double)]
 
 
+class BvhInfo(C.Structure):
+    _fields_ = [("nodes", C.c_int64), ("slots", C.c_int64), ("leaves", C.c_int64), ("max_depth", C.c_int32),
+                ("max_leaf", C.c_int32)]
+
+
 class GuideConfig(C.Structure):
     _fields_ = [("batch", C.c_int32), ("wave_paths", C.c_int32), ("record_bounces", C.c_int32),
                 ("pool_capacity", C.c_int32), ("learning_rate", C.c_float), ("mixture_fraction", C.c_float),
@@ -162,6 +169,8 @@ SIGNATURES = {
                                            C.POINTER(TraversalProbe)]),
     "muon_gpu_measure_read_bandwidth": (C.c_int, [C.c_int32, C.c_int64, C.c_int32, C.POINTER(C.c_double)]),
     "muon_gpu_scene_stream": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p)]),
+    "muon_gpu_scene_bvh": (C.c_int, [C.c_void_p, C.POINTER(BvhInfo), C.c_void_p, C.POINTER(C.c_int32),
+                                     C.POINTER(C.c_uint8)]),
     "muon_gpu_last_error": (C.c_char_p, []),
     "muon_gpu_batch_create": (C.c_int, [C.POINTER(C.c_void_p), C.c_int32, C.POINTER(C.c_void_p)]),
     "muon_gpu_batch_destroy": (None, [C.c_void_p]),

@@ -21,7 +21,7 @@ OBJ = os.path.join(LIB, "obj")
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
-CUDA_UNITS = ["kernels.cu", "noalloc.cu", "guide.cu", "bvh_build.cu", "bvh_sah.cu"]
+CUDA_UNITS = ["kernels.cu", "noalloc.cu", "guide.cu", "bvh_build.cu", "bvh_sah.cu", "scene_records.cu"]
 HOST_UNITS = ["scene_parser.cc", "mesh_io.cc", "scene_build.cc", "host_api.cc", "render.cc", "batch.cc",
               "guide_host.cc", "bvh_walk.cc"]
 CXXFLAGS = ["-std=c++17", "-O2", "-fPIC", "-ffp-contract=off", "-Wall", "-Wno-unused-function"] + \

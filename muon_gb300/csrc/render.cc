@@ -25,6 +25,7 @@
 #include "kernels.cuh"
 #include "scene_access.h"
 #include "scene_build.h"
+#include "scene_records.h"
 
 using namespace muon_gpu;
 
@@ -44,6 +45,7 @@ struct MuonScene {
   // on the device only (img holds them in input order) until a host reader
   // calls SyncSceneImage.
   mutable bool host_records_stale = false;
+  int64_t num_slots = 0;  // primitive records on the device
   DevScene dev{};
   DevCamera cam{};
   // scene arrays
@@ -213,18 +215,22 @@ void ComputeCamera(const MuonCameraDesc &c, DevCamera *out) {
   out->height = c.height;
 }
 
-// Builds the BVH of a scene whose records BuildSceneImage left in input
-// order (defer_bvh) on the device (binned SAH or linear BVH), records
-// gathered into leaf order in the scene's buffers, and the result copied
-// back into the host image so that host-side users (batch merge, scene box)
-// see the same data. Returns MUON_OK or an error code (last error set).
-int BuildBvhOnGpu(MuonScene *sc, int builder, int max_leaf, cudaStream_t st) {
+// Builds the BVH of a scene on the device (binned SAH or linear BVH) from
+// input-order records: those BuildSceneImage left on the host (defer_bvh),
+// or, with `device_desc`, the hittable triangles' records computed on the
+// device from the scene description followed by the spheres' records from
+// the host (device_records). The records are gathered into leaf order in the
+// scene's buffers; the nodes are copied back into the host image, and so are
+// the records for the linear BVH (the binned-SAH path leaves them on the
+// device until SyncSceneImage). Returns MUON_OK or an error code (last error
+// set).
+int BuildBvhOnGpu(MuonScene *sc, int builder, int max_leaf, cudaStream_t st, const MuonSceneDesc *device_desc) {
   SceneImage &im = sc->img;
-  const int n = static_cast<int>(im.prims.size());
-  int nn = std::max(n - 1, 1);
   // temporaries come from (and go back to) the device block cache
-  DeviceBuffer boxes, in_prims, in_obj, in_shade, in_sn, in_sno, scratch, order, last;
-  DeviceBuffer *const temps[] = {&boxes, &in_prims, &in_obj, &in_shade, &in_sn, &in_sno, &scratch, &order, &last};
+  DeviceBuffer boxes, in_prims, in_obj, in_shade, in_sn, in_sno, scratch, order, last, tris, xfs, mats, qidx, keep,
+      pos, count, scan;
+  DeviceBuffer *const temps[] = {&boxes, &in_prims, &in_obj, &in_shade, &in_sn, &in_sno, &scratch, &order, &last,
+                                 &tris, &xfs, &mats, &qidx, &keep, &pos, &count, &scan};
   struct GiveBack {
     DeviceBuffer *const *bufs;
     int count;
@@ -234,15 +240,82 @@ int BuildBvhOnGpu(MuonScene *sc, int builder, int max_leaf, cudaStream_t st) {
       if (cudaStreamSynchronize(st) == cudaSuccess)
         for (int i = 0; i < count; ++i) PoolGive(*bufs[i], device);
     }
-  } give_back{temps, 9, st, sc->device};
-  UploadPooled(boxes, im.boxes, st, sc->device);
-  UploadPooled(in_prims, im.prims, st, sc->device);
-  UploadPooled(in_obj, im.prims_obj, st, sc->device);
-  UploadPooled(in_shade, im.shade, st, sc->device);
-  if (im.any_smooth) {
-    UploadPooled(in_sn, im.smooth_normals, st, sc->device);
-    UploadPooled(in_sno, im.smooth_normals_obj, st, sc->device);
+  } give_back{temps, static_cast<int>(sizeof(temps) / sizeof(temps[0])), st, sc->device};
+  int n = static_cast<int>(im.prims.size());
+  if (device_desc) {
+    const int64_t ntri = device_desc->num_triangles;
+    const int nsph = n;  // the host image holds the spheres alone
+    int32_t nkept = 0;
+    if (ntri > 0) {
+      EnsurePooled(tris, sizeof(MuonTriangleDesc) * ntri, sc->device);
+      CUDA_TRY(cudaMemcpyAsync(tris.ptr, device_desc->triangles, sizeof(MuonTriangleDesc) * ntri,
+                               cudaMemcpyHostToDevice, st));
+      EnsurePooled(xfs, sizeof(MuonTransformDesc) * std::max(device_desc->num_transforms, 1), sc->device);
+      if (device_desc->num_transforms > 0)
+        CUDA_TRY(cudaMemcpyAsync(xfs.ptr, device_desc->transforms,
+                                 sizeof(MuonTransformDesc) * device_desc->num_transforms, cudaMemcpyHostToDevice, st));
+      UploadPooled(mats, im.materials, st, sc->device);
+      UploadPooled(qidx, im.quad_index, st, sc->device);
+      EnsurePooled(keep, sizeof(int32_t) * ntri, sc->device);
+      EnsurePooled(pos, sizeof(int32_t) * ntri, sc->device);
+      EnsurePooled(count, 16, sc->device);
+      const size_t scan_bytes = HittableScanBytes(ntri);
+      EnsurePooled(scan, std::max<size_t>(scan_bytes, 16), sc->device);
+      CUDA_TRY(CountHittableTriangles(tris.as<MuonTriangleDesc>(), ntri, keep.as<int32_t>(), pos.as<int32_t>(),
+                                      count.as<int32_t>(), scan.ptr, scan_bytes, st));
+      CUDA_TRY(cudaMemcpyAsync(&nkept, count.ptr, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+      CUDA_TRY(cudaStreamSynchronize(st));
+    }
+    n = nkept + nsph;
+    sc->num_slots = n;
+    if (n == 0) {
+      for (DeviceBuffer *b : {&sc->nodes, &sc->prims, &sc->prims_obj, &sc->shade, &sc->smooth, &sc->smooth_obj})
+        EnsurePooled(*b, 16, sc->device);
+      im.nodes.clear();
+      im.boxes.clear();
+      im.bvh = BvhBuildStats();
+      return MUON_OK;
+    }
+    EnsurePooled(boxes, sizeof(float) * 6 * n, sc->device);
+    EnsurePooled(in_prims, sizeof(PrimRecord) * n, sc->device);
+    EnsurePooled(in_obj, sizeof(PrimRecord) * n, sc->device);
+    EnsurePooled(in_shade, sizeof(ShadeRecord) * n, sc->device);
+    if (im.any_smooth) {
+      EnsurePooled(in_sn, sizeof(F4) * 3 * n, sc->device);
+      EnsurePooled(in_sno, sizeof(F4) * 3 * n, sc->device);
+    }
+    LaunchTriangleRecords(tris.as<MuonTriangleDesc>(), ntri, xfs.as<MuonTransformDesc>(), mats.as<DevMaterial>(),
+                          qidx.as<int32_t>(), keep.as<int32_t>(), pos.as<int32_t>(), in_prims.as<PrimRecord>(),
+                          in_obj.as<PrimRecord>(), in_shade.as<ShadeRecord>(),
+                          im.any_smooth ? in_sn.as<F4>() : nullptr, im.any_smooth ? in_sno.as<F4>() : nullptr,
+                          boxes.as<float>(), st);
+    CUDA_TRY(cudaGetLastError());
+    if (nsph > 0) {
+      CUDA_TRY(cudaMemcpyAsync(in_prims.as<PrimRecord>() + nkept, im.prims.data(), sizeof(PrimRecord) * nsph,
+                               cudaMemcpyHostToDevice, st));
+      CUDA_TRY(cudaMemcpyAsync(in_obj.as<PrimRecord>() + nkept, im.prims_obj.data(), sizeof(PrimRecord) * nsph,
+                               cudaMemcpyHostToDevice, st));
+      CUDA_TRY(cudaMemcpyAsync(in_shade.as<ShadeRecord>() + nkept, im.shade.data(), sizeof(ShadeRecord) * nsph,
+                               cudaMemcpyHostToDevice, st));
+      CUDA_TRY(cudaMemcpyAsync(boxes.as<float>() + 6 * static_cast<size_t>(nkept), im.boxes.data(),
+                               sizeof(float) * 6 * nsph, cudaMemcpyHostToDevice, st));
+      if (im.any_smooth) {
+        CUDA_TRY(cudaMemsetAsync(in_sn.as<F4>() + 3 * static_cast<size_t>(nkept), 0, sizeof(F4) * 3 * nsph, st));
+        CUDA_TRY(cudaMemsetAsync(in_sno.as<F4>() + 3 * static_cast<size_t>(nkept), 0, sizeof(F4) * 3 * nsph, st));
+      }
+    }
+  } else {
+    sc->num_slots = n;
+    UploadPooled(boxes, im.boxes, st, sc->device);
+    UploadPooled(in_prims, im.prims, st, sc->device);
+    UploadPooled(in_obj, im.prims_obj, st, sc->device);
+    UploadPooled(in_shade, im.shade, st, sc->device);
+    if (im.any_smooth) {
+      UploadPooled(in_sn, im.smooth_normals, st, sc->device);
+      UploadPooled(in_sno, im.smooth_normals_obj, st, sc->device);
+    }
   }
+  int nn = std::max(n - 1, 1);
   const bool sah = builder == MUON_BUILDER_GPU_SAH;
   const size_t sbytes = sah ? GpuSahScratchBytes(n) : GpuLbvhScratchBytes(n);
   EnsurePooled(scratch, sbytes, sc->device);
@@ -821,7 +894,9 @@ int muon_gpu_scene_create(const MuonSceneDesc *desc, MuonScene **out) {
         desc->partition_strategy != MUON_PARTITION_SAH)
       return Fail(MUON_ERR_INVALID_ARG, "the GPU SAH builder takes the SAH partition strategy only");
     const bool gpu_bvh = desc->builder != MUON_BUILDER_HOST_SAH && desc->acceleration == MUON_ACCEL_BVH;
-    if (!BuildSceneImage(*desc, &sc->img, &err, gpu_bvh)) return Fail(MUON_ERR_INVALID_ARG, err);
+    // with the device SAH build the triangles' records are computed on the device too
+    const bool device_records = gpu_bvh && desc->builder == MUON_BUILDER_GPU_SAH;
+    if (!BuildSceneImage(*desc, &sc->img, &err, gpu_bvh, device_records)) return Fail(MUON_ERR_INVALID_ARG, err);
     if (sc->img.bvh.max_depth >= 60) return Fail(MUON_ERR_INVALID_ARG, "BVH too deep for the traversal stack");
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return Fail(MUON_ERR_CUDA, "no CUDA device available");
@@ -841,11 +916,13 @@ int muon_gpu_scene_create(const MuonSceneDesc *desc, MuonScene **out) {
     CUDA_TRY(cudaStreamCreateWithFlags(&sc->stream, cudaStreamNonBlocking));
     cudaStream_t st = sc->stream;
     const SceneImage &im = sc->img;
-    if (gpu_bvh && !im.prims.empty()) {
-      const int rc = BuildBvhOnGpu(sc.get(), desc->builder, desc->max_leaf_size > 0 ? desc->max_leaf_size : 4, st);
+    if (device_records || (gpu_bvh && !im.prims.empty())) {
+      const int rc = BuildBvhOnGpu(sc.get(), desc->builder, desc->max_leaf_size > 0 ? desc->max_leaf_size : 4, st,
+                                   device_records ? desc : nullptr);
       if (rc != MUON_OK) return rc;
       if (sc->img.bvh.max_depth >= 60) return Fail(MUON_ERR_INVALID_ARG, "BVH too deep for the traversal stack");
     } else {
+      sc->num_slots = static_cast<int64_t>(im.prims.size());
       UploadPooled(sc->nodes, im.nodes, st, sc->device);
       UploadPooled(sc->prims, im.prims, st, sc->device);
       UploadPooled(sc->prims_obj, im.prims_obj, st, sc->device);
@@ -1166,7 +1243,11 @@ void SyncSceneImage(const MuonScene *scene) {
   if (!scene || !scene->host_records_stale) return;
   MuonScene *sc = const_cast<MuonScene *>(scene);  // img is a host cache of the device arrays
   SceneImage &im = sc->img;
-  const size_t n = im.prims.size();
+  const size_t n = static_cast<size_t>(sc->num_slots);
+  im.prims.resize(n);
+  im.prims_obj.resize(n);
+  im.shade.resize(n);
+  if (im.any_smooth) im.smooth_normals.resize(3 * n), im.smooth_normals_obj.resize(3 * n);
   cudaStream_t st = sc->stream;
   CUDA_TRY(cudaSetDevice(sc->device));
   CUDA_TRY(cudaMemcpyAsync(im.prims.data(), sc->prims.ptr, sizeof(PrimRecord) * n, cudaMemcpyDeviceToHost, st));

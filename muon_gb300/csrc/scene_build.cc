@@ -15,6 +15,7 @@
 // (muon/acceleration.cc:241-458): binned SAH over all three axes with a
 // bounded leaf size. Closest hits do not depend on the tree shape.
 #include "scene_build.h"
+#include "tri_records.h"
 
 #include <algorithm>
 #include <atomic>
@@ -516,7 +517,9 @@ float Reflectiveness(const MuonMaterialDesc &m) {
 
 }  // namespace
 
-bool BuildSceneImage(const MuonSceneDesc &desc, SceneImage *img, std::string *error, bool defer_bvh) {
+bool BuildSceneImage(const MuonSceneDesc &desc, SceneImage *img, std::string *error, bool defer_bvh,
+                     bool device_records) {
+  defer_bvh = defer_bvh || device_records;
   if (desc.num_triangles < 0 || desc.num_spheres < 0 || desc.num_materials < 0 ||
       desc.num_lights < 0 || desc.num_transforms < 0) {
     *error = "negative array size in scene description";
@@ -609,12 +612,14 @@ bool BuildSceneImage(const MuonSceneDesc &desc, SceneImage *img, std::string *er
   std::vector<int64_t> source;  // box -> primitive (tri i, or ntri + sphere j)
   boxes.reserve(ntri + nsph);
   source.reserve(ntri + nsph);
-  std::vector<PrimRecord> tri_rec(ntri), tri_obj(ntri);
-  std::vector<ShadeRecord> tri_shade(ntri);
+  // triangles whose records this builds (none when the device builds them)
+  const int64_t ntri_host = device_records ? 0 : ntri;
+  std::vector<PrimRecord> tri_rec(ntri_host), tri_obj(ntri_host);
+  std::vector<ShadeRecord> tri_shade(ntri_host);
   std::vector<F4> tri_normals, tri_normals_obj;
   img->any_smooth = false;
   for (int64_t i = 0; i < ntri; ++i) img->any_smooth |= desc.triangles[i].smooth != 0;
-  if (img->any_smooth) tri_normals.resize(3 * ntri), tri_normals_obj.resize(3 * ntri);
+  if (img->any_smooth) tri_normals.resize(3 * ntri_host), tri_normals_obj.resize(3 * ntri_host);
   img->leaf_of_prim_id.assign(img->num_prims, -1);
 
   for (int64_t i = 0; i < ntri; ++i) {
@@ -631,68 +636,25 @@ bool BuildSceneImage(const MuonSceneDesc &desc, SceneImage *img, std::string *er
   }
   // Per-triangle records, on all host threads (each triangle writes its own
   // slots), then the boxes of the triangles that can be hit in input order.
-  std::vector<Aabb> tri_box(ntri);
-  std::vector<uint8_t> tri_keep(ntri, 0);
-  ParallelFor(ntri, 1 << 14, [&](int64_t i0, int64_t i1) {
-  for (int64_t i = i0; i < i1; ++i) {
-    const MuonTriangleDesc &t = desc.triangles[i];
-    mm::v3 ov[3] = {V3(t.v[0]), V3(t.v[1]), V3(t.v[2])};
-    mm::v3 wv[3];
-    mm::m4 m = t.transform >= 0 ? ToM4(desc.transforms[t.transform].object_to_world) : mm::identity4();
-    for (int k = 0; k < 3; ++k) wv[k] = t.transform >= 0 ? mm::xform_point(m, ov[k]) : ov[k];
-    mm::v3 n_obj = mm::cross(ov[1] - ov[0], ov[2] - ov[0]);
-    mm::v3 n_w = mm::cross(wv[1] - wv[0], wv[2] - wv[0]);
-    float len_obj = mm::length(n_obj);
-    float eps = 1e-4f;
-    if (t.transform >= 0) eps = 1e-4f * (mm::length(n_w) / len_obj);
-    PrimRecord &ro = tri_obj[i];
-    ro.p0 = MakeF4(ov[0].x, ov[0].y, ov[0].z, 0.0f);
-    ro.p1 = MakeF4(ov[1].x, ov[1].y, ov[1].z, IntBits(t.transform));
-    ro.p2 = MakeF4(ov[2].x, ov[2].y, ov[2].z, mm::dot(n_obj, n_obj));
-    PrimRecord &r = tri_rec[i];
-    r.p0 = MakeF4(wv[0].x, wv[0].y, wv[0].z, mm::dot(wv[0], n_w));
-    r.p1 = MakeF4(wv[1].x, wv[1].y, wv[1].z, eps);
-    r.p2 = MakeF4(wv[2].x, wv[2].y, wv[2].z, 0.0f);
-    uint32_t flags = t.smooth ? kPrimSmooth : 0u;
-    r.p3 = MakeF4(n_w.x, n_w.y, n_w.z, 0.0f);
-    // Shading normal as the reference forms it: the unit object-space normal
-    // carried by the inverse transpose and normalised again (muon/objects.cc:
-    // 40-41, 165-167); for a mirroring transform it points against n_w.
-    mm::m4 nt0 = t.transform >= 0 ? ToM4(desc.transforms[t.transform].normal_to_world) : mm::identity4();
-    mm::v3 un = mm::xform_dir(nt0, mm::normalize(n_obj));
-    ShadeRecord &s = tri_shade[i];
-    s.s0 = MakeF4(un.x, un.y, un.z, IntBits(t.material));
-    int32_t brdf_eff;
-    std::memcpy(&brdf_eff, &img->materials[t.material].emission.w, 4);
-    const uint32_t shade_flags = flags | (static_cast<uint32_t>(brdf_eff) << kClassShift);
-    s.s1 = I4{t.light >= 0 ? quad_index[t.light] : -1, t.prim_id, t.transform, static_cast<int32_t>(shade_flags)};
-    // the primitive record carries the shading class too (read by the extend
-    // kernel from the record it has just tested)
-    std::memcpy(&r.p3.w, &shade_flags, 4);
-    ro.p3 = r.p3;
-    ro.p3.x = n_obj.x, ro.p3.y = n_obj.y, ro.p3.z = n_obj.z;
-    if (t.smooth) {
-      // normalize(M^-T (w n0 + u n1 + v n2)) equals the normalised blend of
-      // the pre-transformed vertex normals, by linearity.
-      mm::m4 nt = t.transform >= 0 ? ToM4(desc.transforms[t.transform].normal_to_world) : mm::identity4();
-      for (int k = 0; k < 3; ++k) {
-        mm::v3 vn = V3(t.n[k]);
-        mm::v4 w4 = t.transform >= 0 ? mm::mul(nt, mm::v4{vn.x, vn.y, vn.z, 0.0f}) : mm::v4{vn.x, vn.y, vn.z, 0.0f};
-        tri_normals[3 * i + k] = MakeF4(w4.x, w4.y, w4.z, 0.0f);
-        tri_normals_obj[3 * i + k] = MakeF4(vn.x, vn.y, vn.z, 0.0f);
+  std::vector<Aabb> tri_box(ntri_host);
+  std::vector<uint8_t> tri_keep(ntri_host, 0);
+  ParallelFor(ntri_host, 1 << 14, [&](int64_t i0, int64_t i1) {
+    for (int64_t i = i0; i < i1; ++i) {
+      TriangleOut o;
+      const bool keep = TriangleRecords(desc.triangles[i], desc.transforms, img->materials.data(), quad_index.data(), &o);
+      tri_rec[i] = o.world;
+      tri_obj[i] = o.object;
+      tri_shade[i] = o.shade;
+      if (desc.triangles[i].smooth) {
+        for (int k = 0; k < 3; ++k) tri_normals[3 * i + k] = o.normals[k], tri_normals_obj[3 * i + k] = o.normals_obj[k];
       }
+      if (!keep) continue;
+      for (int k = 0; k < 3; ++k) tri_box[i].lo[k] = o.lo[k], tri_box[i].hi[k] = o.hi[k];
+      tri_keep[i] = 1;
     }
-    // |d.n| <= |n| for a unit direction, so such a triangle is never hit.
-    if (!(len_obj >= 1e-4f)) continue;
-    Aabb &b = tri_box[i];
-    for (int k = 0; k < 3; ++k) {
-      b.lo[k] = std::min(std::min(mm::comp(wv[0], k), mm::comp(wv[1], k)), mm::comp(wv[2], k));
-      b.hi[k] = std::max(std::max(mm::comp(wv[0], k), mm::comp(wv[1], k)), mm::comp(wv[2], k));
-    }
-    tri_keep[i] = 1;
-  }
   });
-  for (int64_t i = 0; i < ntri; ++i) {
+  img->quad_index = quad_index;
+  for (int64_t i = 0; i < ntri_host; ++i) {
     if (!tri_keep[i]) continue;
     boxes.push_back(tri_box[i]);
     source.push_back(i);

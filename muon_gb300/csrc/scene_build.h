@@ -48,6 +48,7 @@ struct SceneImage {
   int64_t num_prims = 0;                  // primitives in the scene, including never-hit ones
   bool any_smooth = false;
   std::vector<float> boxes;               // 6 per record, when the GPU builds the BVH
+  std::vector<int32_t> quad_index;        // light index -> quad-light index (-1: not a quad)
   MuonCameraDesc camera{};
   int32_t width = 0, height = 0;
   BvhBuildStats bvh;
@@ -55,7 +56,11 @@ struct SceneImage {
 
 // Flattens a scene description. Returns false with a message on invalid input.
 // With defer_bvh the BVH is left to the GPU builder: `nodes` stays empty, the
-// records are in input order and `boxes` holds their world bounds.
-bool BuildSceneImage(const MuonSceneDesc &desc, SceneImage *img, std::string *error, bool defer_bvh = false);
+// records are in input order and `boxes` holds their world bounds. With
+// device_records (which implies defer_bvh) the triangles are only validated:
+// the records and boxes hold the spheres alone, to follow the hittable
+// triangles' records that the device computes (scene_records.h).
+bool BuildSceneImage(const MuonSceneDesc &desc, SceneImage *img, std::string *error, bool defer_bvh = false,
+                     bool device_records = false);
 
 }  // namespace muon_gpu

@@ -1,5 +1,10 @@
 """The device binned-SAH builder (MUON_BUILDER_GPU_SAH) against the host one.
 
+With this builder the triangles' records are computed on the device too
+(scene_records.cu, the host builder's arithmetic), so the comparisons below
+also pin the device records: boxes, hit distances in the object-space exact
+mode, and normals (smooth ones included) must be the host's bits.
+
 It takes the host builder's split decisions with the same float operations,
 so the two trees must have the same nodes: the same multiset of (padded
 child box, child box, leaf contents) rows, the same partition of primitives
@@ -187,3 +192,43 @@ def test_device_sah_tree_of_the_benchmark_scenes(lib, which):
     _hits_agree(host, dev, rays)
     host.close()
     dev.close()
+
+
+def _smooth_scene():
+    """A smooth-shaded (compute_vertex_normals) wavy grid under a rotation
+    and scale, a second copy without smoothing, spheres and a quad light."""
+    import math
+
+    k = 40
+    verts = [f"vertex {x / k * 2 - 1:.5f} {y / k * 2 - 1:.5f} {0.15 * math.sin(5 * x / k) * math.cos(4 * y / k):.5f}"
+             for y in range(k + 1) for x in range(k + 1)]
+    tris = []
+    for y in range(k):
+        for x in range(k):
+            a = y * (k + 1) + x
+            tris += [f"tri {a} {a + 1} {a + k + 2}", f"tri {a} {a + k + 2} {a + k + 1}"]
+    mesh = "start_mesh\n" + "\n".join(verts + tris) + "\nend_mesh\n"
+    return ("camera 0 0 6  0 0 0  0 1 0  45\nfilm_size 96 96\n"
+            "quad_light 2 2 2  -1 3 1  0 0.5 0  0.5 0 0\n"
+            "push_transform\nrotate 1 0.3 0.2 35\nscale 1.2 0.9 1.1\ncompute_vertex_normals on\n" + mesh +
+            "pop_transform\ncompute_vertex_normals off\npush_transform\ntranslate 0 0 -1.5\n" + mesh +
+            "pop_transform\nsphere 1.5 1.5 0 0.4\nsphere -1.5 -1.2 0.5 0.3\n")
+
+
+@pytest.mark.gpu
+def test_device_records_of_a_smooth_transformed_scene(lib):
+    text = _smooth_scene()
+    parsed = m.parse_string(text)
+    assert any(parsed.desc.triangles[i].smooth for i in range(parsed.desc.num_triangles))
+    host, dev = _same_tree(text)
+    from oracle import port
+
+    rays = port.camera_rays(text)
+    _hits_agree(host, dev, rays)
+    # the normals film interpolates the smooth vertex normals
+    a = host.render(integrator="normals", pixel_samples=1)
+    b = dev.render(integrator="normals", pixel_samples=1)
+    _, p0, _, _ = host.intersect(rays[:, :3], rays[:, 3:], native.ISECT_EXACT)
+    _, p1, _, _ = dev.intersect(rays[:, :3], rays[:, 3:], native.ISECT_EXACT)
+    same = p0 == p1
+    assert np.array_equal(a.sum.reshape(-1, 3)[same], b.sum.reshape(-1, 3)[same])

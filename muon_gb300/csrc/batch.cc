@@ -25,6 +25,7 @@
 #include "host_scene.h"
 #include "kernels.cuh"
 #include "scene_access.h"
+#include "scene_records.h"
 #include "scene_build.h"
 
 using namespace muon_gpu;
@@ -32,25 +33,6 @@ using namespace muon_gpu;
 namespace {
 
 constexpr int kBatchDefaultWavePaths = 1 << 22;
-
-// Shifts a BVH link of a scene whose nodes and records start at the given
-// offsets in the merged arrays.
-int32_t ShiftLink(int32_t link, int32_t node_off, int32_t prim_off) {
-  if (link == kEmptyLink) return link;
-  if (link >= 0) return link + node_off;
-  return ~(~link + prim_off);
-}
-
-int32_t ShiftIndex(int32_t v, int32_t off) { return v >= 0 ? v + off : v; }
-
-float ShiftIndexBits(float bits, int32_t off) {
-  int32_t v;
-  std::memcpy(&v, &bits, 4);
-  v = ShiftIndex(v, off);
-  float out;
-  std::memcpy(&out, &v, 4);
-  return out;
-}
 
 struct WavePlan {
   int seg_begin = 0, nseg = 0;  // into the batch's segment table
@@ -155,21 +137,37 @@ struct MuonBatch {
 
 namespace {
 
-// Builds the merged image of `views` (creation order) into `b`.
+// Builds the merged scene of `views` (creation order) into `b`: the scenes'
+// device arrays are appended on the device (nodes with shifted links,
+// records with shifted transform / material / light indices); the small
+// tables (transforms, materials, lights) are merged on the host.
 void MergeScenes(MuonBatch *b, const std::vector<SceneView> &views) {
-  std::vector<BvhNode> nodes;
-  std::vector<PrimRecord> prims, prims_obj;
-  std::vector<ShadeRecord> shade;
-  std::vector<F4> smooth, smooth_obj;
   std::vector<DevTransform> transforms;
   std::vector<DevMaterial> materials;
   std::vector<DevLight> lights, other;
   bool any_smooth = false;
-  for (const SceneView &v : views) any_smooth |= v.img->any_smooth;
+  int64_t total_nodes = 0, total_prims = 0;
+  for (const SceneView &v : views) {
+    any_smooth |= v.img->any_smooth;
+    total_nodes += std::max<int64_t>(v.dev->num_nodes, 1);
+    total_prims += v.num_slots;
+    CUDA_TRY(cudaStreamSynchronize(v.stream));  // the scene's arrays are complete
+  }
+  if (total_nodes > INT32_MAX || total_prims > INT32_MAX) throw CudaError{cudaErrorInvalidValue, "batch too large"};
+  cudaStream_t st = b->stream;
+  b->nodes.Ensure(sizeof(BvhNode) * total_nodes);
+  b->prims.Ensure(sizeof(PrimRecord) * std::max<int64_t>(total_prims, 1));
+  b->prims_obj.Ensure(sizeof(PrimRecord) * std::max<int64_t>(total_prims, 1));
+  b->shade.Ensure(sizeof(ShadeRecord) * std::max<int64_t>(total_prims, 1));
+  b->smooth.Ensure(any_smooth ? sizeof(F4) * 3 * total_prims : 16);
+  b->smooth_obj.Ensure(any_smooth ? sizeof(F4) * 3 * total_prims : 16);
+  // No primitives: a root whose first child link is empty ends every
+  // traversal at once.
+  BvhNode empty{};
+  empty.d.x = empty.d.y = kEmptyLink;
+  int32_t node_off = 0, prim_off = 0;
   for (const SceneView &v : views) {
     const SceneImage &im = *v.img;
-    const int32_t node_off = static_cast<int32_t>(nodes.size());
-    const int32_t prim_off = static_cast<int32_t>(prims.size());
     const int32_t xf_off = static_cast<int32_t>(transforms.size());
     const int32_t mat_off = static_cast<int32_t>(materials.size());
     const int32_t light_off = static_cast<int32_t>(lights.size());
@@ -182,41 +180,17 @@ void MergeScenes(MuonBatch *b, const std::vector<SceneView> &views) {
     b->height.push_back(im.height);
     b->scene_prims.push_back(static_cast<uint64_t>(im.num_prims));
     b->cams.push_back(*v.cam);
-    if (im.nodes.empty()) {
-      // No primitives: a root whose first child link is empty ends every
-      // traversal at once.
-      BvhNode e{};
-      e.d.x = e.d.y = kEmptyLink;
-      nodes.push_back(e);
-    }
-    for (BvhNode nd : im.nodes) {
-      nd.d.x = ShiftLink(nd.d.x, node_off, prim_off);
-      nd.d.y = ShiftLink(nd.d.y, node_off, prim_off);
-      nodes.push_back(nd);
-    }
-    for (size_t i = 0; i < im.prims.size(); ++i) {
-      PrimRecord r = im.prims[i], ro = im.prims_obj[i];
-      uint32_t flags;
-      std::memcpy(&flags, &r.p3.w, 4);
-      if (flags & kPrimSphere) {
-        r.p1.y = ShiftIndexBits(r.p1.y, xf_off);
-        ro.p1.y = ShiftIndexBits(ro.p1.y, xf_off);
-      } else {
-        ro.p1.w = ShiftIndexBits(ro.p1.w, xf_off);
-      }
-      prims.push_back(r);
-      prims_obj.push_back(ro);
-      ShadeRecord s = im.shade[i];
-      s.s0.w = ShiftIndexBits(s.s0.w, mat_off);
-      s.s1.x = ShiftIndex(s.s1.x, light_off);
-      s.s1.z = ShiftIndex(s.s1.z, xf_off);
-      shade.push_back(s);
-      for (int k = 0; k < 3; ++k) {
-        if (!any_smooth) break;
-        smooth.push_back(im.any_smooth ? im.smooth_normals[3 * i + k] : F4{0, 0, 0, 0});
-        smooth_obj.push_back(im.any_smooth ? im.smooth_normals_obj[3 * i + k] : F4{0, 0, 0, 0});
-      }
-    }
+    const int64_t nn = v.dev->num_nodes;
+    if (nn == 0)
+      CUDA_TRY(cudaMemcpyAsync(b->nodes.as<BvhNode>() + node_off, &empty, sizeof(BvhNode), cudaMemcpyHostToDevice, st));
+    const MergeOffsets off{node_off, prim_off, xf_off, mat_off, light_off};
+    LaunchMergeScene(v.dev->nodes, nn, v.dev->prims, v.dev->prims_obj, v.dev->shade, v.dev->smooth_normals,
+                     v.dev->smooth_normals_obj, v.num_slots, off, b->nodes.as<BvhNode>(), b->prims.as<PrimRecord>(),
+                     b->prims_obj.as<PrimRecord>(), b->shade.as<ShadeRecord>(),
+                     any_smooth ? b->smooth.as<F4>() : nullptr, any_smooth ? b->smooth_obj.as<F4>() : nullptr, st);
+    CUDA_TRY(cudaGetLastError());
+    node_off += static_cast<int32_t>(std::max<int64_t>(nn, 1));
+    prim_off += static_cast<int32_t>(v.num_slots);
     transforms.insert(transforms.end(), im.transforms.begin(), im.transforms.end());
     materials.insert(materials.end(), im.materials.begin(), im.materials.end());
     lights.insert(lights.end(), im.lights.begin(), im.lights.end());
@@ -225,13 +199,6 @@ void MergeScenes(MuonBatch *b, const std::vector<SceneView> &views) {
   std::vector<PrimRecord> lt, lt_obj;
   std::vector<int32_t> lt_ok;
   BuildLightTris(lights, &lt, &lt_obj, &lt_ok);
-  cudaStream_t st = b->stream;
-  Upload(b->nodes, nodes, st);
-  Upload(b->prims, prims, st);
-  Upload(b->prims_obj, prims_obj, st);
-  Upload(b->shade, shade, st);
-  Upload(b->smooth, smooth, st);
-  Upload(b->smooth_obj, smooth_obj, st);
   Upload(b->transforms, transforms, st);
   Upload(b->materials, materials, st);
   Upload(b->lights, lights, st);
@@ -255,12 +222,12 @@ void MergeScenes(MuonBatch *b, const std::vector<SceneView> &views) {
   d.light_tri_ok = b->light_tri_ok.as<int32_t>();
   d.other_lights = b->other_lights.as<DevLight>();
   d.all_lights = nullptr;
-  d.num_nodes = static_cast<int32_t>(nodes.size());
+  d.num_nodes = static_cast<int32_t>(total_nodes);
   d.num_lights = static_cast<int32_t>(lights.size());
   d.num_other_lights = static_cast<int32_t>(other.size());
   d.num_all_lights = 0;
-  b->total_nodes = nodes.size();
-  b->total_prims = prims.size();
+  b->total_nodes = static_cast<size_t>(total_nodes);
+  b->total_prims = static_cast<size_t>(total_prims);
   CUDA_TRY(cudaStreamSynchronize(st));
 }
 
@@ -539,7 +506,6 @@ int muon_gpu_batch_create(MuonScene *const *scenes, int32_t n, MuonBatch **out) 
   std::unique_ptr<MuonBatch> b;
   try {
     b.reset(new MuonBatch());
-    for (int i = 0; i < n; ++i) SyncSceneImage(scenes[i]);
     b->n = n;
     b->device = views[0].device;
     CUDA_TRY(cudaSetDevice(b->device));

@@ -1274,6 +1274,7 @@ bool GetSceneView(const MuonScene *scene, SceneView *out) {
   out->width = scene->img.width;
   out->height = scene->img.height;
   out->img = &scene->img;
+  out->num_slots = scene->num_slots;
   return true;
 }
 

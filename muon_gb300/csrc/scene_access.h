@@ -17,6 +17,7 @@ struct SceneView {
   int device;
   int width, height;
   const SceneImage *img;  // host copy of the scene's device arrays
+  int64_t num_slots;      // primitive records on the device (dev->prims ...)
 };
 
 // Fills `out` from a scene created by muon_gpu_scene_create; false if null.

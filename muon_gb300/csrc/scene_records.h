@@ -27,4 +27,17 @@ void LaunchTriangleRecords(const MuonTriangleDesc *tris, int64_t n, const MuonTr
                            const int32_t *pos, PrimRecord *world, PrimRecord *object, ShadeRecord *shade,
                            F4 *normals, F4 *normals_obj, float *boxes, cudaStream_t st);
 
+// Index offsets of one scene inside a merged (batched) scene.
+struct MergeOffsets {
+  int32_t node_off, prim_off, xf_off, mat_off, light_off;
+};
+// Appends one scene's device arrays to merged ones: nodes at node_off (links
+// shifted), records at prim_off with their transform, material and light
+// indices shifted; smooth normals copied (zeros when the scene has none and
+// the merged scene has some: sn_out set, sn_in null).
+void LaunchMergeScene(const BvhNode *nodes_in, int64_t num_nodes, const PrimRecord *prims_in,
+                      const PrimRecord *obj_in, const ShadeRecord *shade_in, const F4 *sn_in, const F4 *sno_in,
+                      int64_t num_prims, MergeOffsets off, BvhNode *nodes_out, PrimRecord *prims_out,
+                      PrimRecord *obj_out, ShadeRecord *shade_out, F4 *sn_out, F4 *sno_out, cudaStream_t st);
+
 }  // namespace muon_gpu

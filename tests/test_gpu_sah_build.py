@@ -232,3 +232,26 @@ def test_device_records_of_a_smooth_transformed_scene(lib):
     _, p1, _, _ = dev.intersect(rays[:, :3], rays[:, 3:], native.ISECT_EXACT)
     same = p0 == p1
     assert np.array_equal(a.sum.reshape(-1, 3)[same], b.sum.reshape(-1, 3)[same])
+
+
+@pytest.mark.gpu
+def test_device_build_of_degenerate_and_sphere_only_scenes(lib):
+    """Only never-hit (zero-area) triangles: no tree and no hits, as with the
+    host build; only spheres: no triangle records, the same tree."""
+    from oracle import port
+
+    flat = ("film_size 16 16\ncamera 0 0 5  0 0 0  0 1 0  45\nstart_mesh\nvertex 0 0 0\nvertex 1 0 0\nvertex 2 0 0\n"
+            "tri 0 1 2\ntri 1 2 0\nend_mesh\n")
+    for builder in ("host", "gpu_sah"):
+        sc = m.Scene.from_string(flat, builder=builder)
+        info = sc.bvh()[0]
+        assert info["nodes"] == 0 and info["slots"] == 0
+        rays = port.camera_rays(flat)
+        _, pid, _, _ = sc.intersect(rays[:, :3], rays[:, 3:], native.ISECT_EXACT)
+        assert (pid < 0).all()
+        film = sc.render(integrator="depth", pixel_samples=1)
+        assert not film.sum.any()
+    spheres = "film_size 16 16\ncamera 0 0 9  0 0 0  0 1 0  45\n" + "".join(
+        f"sphere {x * 0.7 - 3} {(x * 37 % 11) * 0.5 - 2.5} {(x * 13 % 7) * 0.3} 0.3\n" for x in range(300))
+    host, dev = _same_tree(spheres)
+    _hits_agree(host, dev, port.camera_rays(spheres))

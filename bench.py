@@ -278,6 +278,20 @@ def roofline(name: str, probe: dict, probe_stats: dict, last: dict) -> dict:
     return out
 
 
+def desc_upload_bytes(parsed) -> int:
+    """Bytes of a scene description that scene creation copies to the device
+    (the description's arrays, as their C structs; the device computes the
+    triangles' records from them)."""
+    import ctypes as C
+
+    from muon_gb300 import native
+
+    d = parsed.desc
+    return (d.num_triangles * C.sizeof(native.TriangleDesc) + d.num_spheres * C.sizeof(native.SphereDesc) +
+            d.num_materials * C.sizeof(native.MaterialDesc) + d.num_lights * C.sizeof(native.LightDesc) +
+            d.num_transforms * C.sizeof(native.TransformDesc))
+
+
 def measure_frames(name: str, w: dict, steps: int, warmup: int, builder: str, with_cpu: bool) -> dict:
     """One step = one full frame of a single-scene workload (device time,
     film in device memory), then the same metric end to end through the
@@ -340,8 +354,7 @@ def measure_frames(name: str, w: dict, steps: int, warmup: int, builder: str, wi
     # end to end through the public API with host buffers
     e2e_steps = max(2, min(steps, 5))
     parsed = m.parse_string(text)
-    desc_bytes = (parsed.desc.num_triangles * 80 + parsed.desc.num_spheres * 32 + parsed.desc.num_materials * 56 +
-                  parsed.desc.num_lights * 52 + parsed.desc.num_transforms * 192)
+    desc_bytes = desc_upload_bytes(parsed)
     film_bytes = h * wd * (3 * 8 * 2 + 4)
     # the step's film comes back into pinned host memory, reused across steps
     host_film = m.FilmResult(torch.zeros((h, wd, 3), dtype=torch.float64).pin_memory().numpy(),
@@ -469,8 +482,7 @@ def measure_batch(w: dict, steps: int, warmup: int, builder: str, with_cpu: bool
     torch.cuda.synchronize()
     # end to end: scene uploads (BVH builds), batch merge, render, host films back
     e2e_steps = 2
-    h2d = sum(p.desc.num_triangles * 80 + p.desc.num_spheres * 32 + p.desc.num_materials * 56 +
-              p.desc.num_lights * 52 + p.desc.num_transforms * 192 for p in parsed)
+    h2d = sum(desc_upload_bytes(p) for p in parsed)
     d2h = sum(s.width * s.height * (3 * 8 * 2 + 4) for s in sc)
     t0 = time.perf_counter()
     e2e_counted = 0

@@ -128,7 +128,7 @@ struct MuonBatch {
     contrib.Ensure(sl * sizeof(float4));
     slot_dir.Ensure(sl * sizeof(float4));
     shq.Ensure(sl * sizeof(uint32_t));
-    order.Ensure(static_cast<size_t>(p) * kNumClasses * sizeof(int32_t));
+    order.Ensure(static_cast<size_t>(OrderInts(p)) * sizeof(int32_t));
     wave_cap = p;
     slots_cap = s;
     return true;

@@ -345,6 +345,15 @@ __device__ __forceinline__ void PersistentTraverse(const DevScene &s, int n, uin
 #ifndef MUON_CLASS_FROM_PRIM
 #define MUON_CLASS_FROM_PRIM 1
 #endif
+// Class lists of the shading kernel in queue order (1): the extend kernel
+// leaves each hit's class in link[] and a stable partition (per-tile counts,
+// a scan per class, a scatter) builds the lists, so that queue order, and the
+// pixel locality the camera gave it, carries over from bounce to bounce; or
+// in the order rays finish (0): the extend kernel appends each hit as its
+// lane finishes.
+#ifndef MUON_STABLE_CLASSES
+#define MUON_STABLE_CLASSES 1
+#endif
 
 template <bool kStats, int kTri>
 __global__ void __launch_bounds__(kBlock, MUON_TRAVERSAL_MIN_BLOCKS) ExtendKernel(DevScene s, PathBuffers b, WaveCounters wc, int bounce) {
@@ -375,6 +384,9 @@ __global__ void __launch_bounds__(kBlock, MUON_TRAVERSAL_MIN_BLOCKS) ExtendKerne
 #else
         if (t.hit >= 0) cls = (__ldg(&s.shade[t.hit].s1.w) >> kClassShift) & 7;
 #endif
+#if MUON_STABLE_CLASSES
+        b.link[j] = cls < kNumClasses ? cls : -1;
+#else
         const unsigned active = __activemask();
         const unsigned peers = __match_any_sync(active, cls);
         const int lane = threadIdx.x & 31;
@@ -387,6 +399,7 @@ __global__ void __launch_bounds__(kBlock, MUON_TRAVERSAL_MIN_BLOCKS) ExtendKerne
         } else {
           b.link[j] = -1;
         }
+#endif
       },
       c, overflow);
   if (kStats) {
@@ -396,6 +409,107 @@ __global__ void __launch_bounds__(kBlock, MUON_TRAVERSAL_MIN_BLOCKS) ExtendKerne
     AddStat(b.stats, kStatPrimHits, c.prim_hits);
   }
   if (overflow) atomicAdd(b.stats + kStatOverflow, 1ull);
+}
+
+// ---- stable class partition (MUON_STABLE_CLASSES) ---------------------------------
+// Tile t holds queue entries [t * kClassTile, (t + 1) * kClassTile); its
+// class counts, then their exclusive prefix over tiles, live in the ints
+// after the class lists of b.order.
+constexpr int kClassThreads = 256;
+static_assert(kClassTile % kClassThreads == 0, "a tile is a whole number of block passes");
+
+__device__ __forceinline__ int32_t *ClassTiles(const PathBuffers &b) {
+  return b.order + static_cast<int64_t>(b.order_cap) * kNumClasses;
+}
+
+__global__ void __launch_bounds__(kClassThreads) ClassCountKernel(PathBuffers b, WaveCounters wc, int bounce) {
+  const int n = static_cast<int>(*wc.count(bounce));
+  const int base = blockIdx.x * kClassTile;
+  if (base >= n) return;
+  __shared__ int cnt[kNumClasses];
+  if (threadIdx.x < kNumClasses) cnt[threadIdx.x] = 0;
+  __syncthreads();
+  for (int k = 0; k < kClassTile / kClassThreads; ++k) {
+    const int j = base + k * kClassThreads + threadIdx.x;
+    const int c = j < n ? b.link[j] : -1;
+    if (c >= 0 && c < kNumClasses) atomicAdd(&cnt[c], 1);
+  }
+  __syncthreads();
+  if (threadIdx.x < kNumClasses) ClassTiles(b)[blockIdx.x * 8 + threadIdx.x] = cnt[threadIdx.x];
+}
+
+// One block per class: the exclusive prefix of the class's tile counts, and
+// the class total for the shading kernel.
+__global__ void __launch_bounds__(1024) ClassScanKernel(PathBuffers b, WaveCounters wc, int bounce) {
+  const int n = static_cast<int>(*wc.count(bounce));
+  const int tiles = (n + kClassTile - 1) / kClassTile;
+  const int c = blockIdx.x, lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  int32_t *t8 = ClassTiles(b);
+  const int per = (tiles + 1023) / 1024;
+  const int t0 = threadIdx.x * per, t1 = min(t0 + per, tiles);
+  int sum = 0;
+  for (int t = t0; t < t1; ++t) sum += t8[t * 8 + c];
+  __shared__ int warp_sums[32];
+  int x = sum;
+  for (int o = 1; o < 32; o <<= 1) {
+    const int y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) warp_sums[w] = x;
+  __syncthreads();
+  if (w == 0) {
+    const int v = warp_sums[lane];
+    int y = v;
+    for (int o = 1; o < 32; o <<= 1) {
+      const int z = __shfl_up_sync(0xffffffffu, y, o);
+      if (lane >= o) y += z;
+    }
+    warp_sums[lane] = y - v;  // exclusive over warps
+  }
+  __syncthreads();
+  int acc = warp_sums[w] + x - sum;
+  for (int t = t0; t < t1; ++t) {
+    const int v = t8[t * 8 + c];
+    t8[t * 8 + c] = acc;
+    acc += v;
+  }
+  if (threadIdx.x == 1023) wc.classes(bounce)[c] = static_cast<uint32_t>(acc);
+}
+
+// Each hit entry to its class list, in queue order.
+__global__ void __launch_bounds__(kClassThreads) ClassScatterKernel(PathBuffers b, WaveCounters wc, int bounce) {
+  const int n = static_cast<int>(*wc.count(bounce));
+  const int base = blockIdx.x * kClassTile;
+  if (base >= n) return;
+  constexpr int kW = kClassThreads / 32;
+  __shared__ int running[kNumClasses];
+  __shared__ int warp_cnt[kW][kNumClasses];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if (threadIdx.x < kNumClasses) running[threadIdx.x] = ClassTiles(b)[blockIdx.x * 8 + threadIdx.x];
+  for (int k = 0; k < kClassTile / kClassThreads; ++k) {
+    const int j = base + k * kClassThreads + threadIdx.x;
+    int c = j < n ? b.link[j] : -1;
+    if (c >= kNumClasses) c = -1;
+    unsigned mine = 0;
+    for (int q = 0; q < kNumClasses; ++q) {
+      const unsigned m = __ballot_sync(0xffffffffu, c == q);
+      if (lane == 0) warp_cnt[w][q] = __popc(m);
+      if (c == q) mine = m;
+    }
+    __syncthreads();
+    if (c >= 0) {
+      int pos = running[c] + __popc(mine & ((1u << lane) - 1u));
+      for (int v = 0; v < w; ++v) pos += warp_cnt[v][c];
+      if (pos < b.order_cap) b.order[static_cast<int64_t>(c) * b.order_cap + pos] = j;
+    }
+    __syncthreads();
+    if (threadIdx.x < kNumClasses) {
+      int tot = 0;
+      for (int v = 0; v < kW; ++v) tot += warp_cnt[v][threadIdx.x];
+      running[threadIdx.x] += tot;
+    }
+    __syncthreads();
+  }
 }
 
 // Shadow queue entries are slot indices (entry * S + slot). A blocked slot's
@@ -1389,6 +1503,12 @@ void LaunchExtend(const DevScene &s, const PathBuffers &b, WaveCounters wc, int 
     if (stats) ExtendKernel<true, M><<<g, kBlock, 0, st>>>(s, b, wc, bounce);
     else ExtendKernel<false, M><<<g, kBlock, 0, st>>>(s, b, wc, bounce);
   });
+  if (MUON_STABLE_CLASSES) {
+    const unsigned tiles = static_cast<unsigned>((bound + kClassTile - 1) / kClassTile);
+    ClassCountKernel<<<tiles, kClassThreads, 0, st>>>(b, wc, bounce);
+    ClassScanKernel<<<kNumClasses, 1024, 0, st>>>(b, wc, bounce);
+    ClassScatterKernel<<<tiles, kClassThreads, 0, st>>>(b, wc, bounce);
+  }
 }
 
 void LaunchShadeDebug(const DevScene &s, const PathBuffers &b, WaveCounters wc, int integrator, int bound, int isect,

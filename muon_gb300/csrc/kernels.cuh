@@ -85,6 +85,12 @@ struct PathBuffers {
   unsigned long long *stats;
 };
 
+// The `order` array of a wavefront of `cap` paths: kNumClasses class lists
+// of cap entries each, then 8 class counts per tile of kClassTile queue
+// entries (the stable class partition's, MUON_STABLE_CLASSES in kernels.cu).
+constexpr int kClassTile = 1024;
+inline int64_t OrderInts(int64_t cap) { return cap * kNumClasses + (cap / kClassTile + 1) * 8; }
+
 struct ShadeParams {
   int32_t integrator;
   int32_t nee, is_mode, rr;

@@ -91,7 +91,7 @@ size_t Carve(unsigned char *base, int64_t paths, int slots, int bounces, PathBuf
   pb.contrib = c.Take<float4>(sl);
   pb.slot_dir = c.Take<float4>(sl);
   pb.shq = c.Take<uint32_t>(sl);
-  pb.order = c.Take<int32_t>(static_cast<size_t>(paths) * kNumClasses);
+  pb.order = c.Take<int32_t>(static_cast<size_t>(OrderInts(paths)));
   pb.order_cap = static_cast<int32_t>(paths);
   uint32_t *ctr = c.Take<uint32_t>(WaveCounterWords(bounces));
   pb.stats = c.Take<unsigned long long>(kNumStats);

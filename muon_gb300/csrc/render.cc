@@ -149,7 +149,7 @@ struct MuonScene {
     EnsurePooled(contrib, sl * sizeof(float4), device);
     EnsurePooled(slot_dir, sl * sizeof(float4), device);
     EnsurePooled(shq, sl * sizeof(uint32_t), device);
-    EnsurePooled(order, static_cast<size_t>(p) * kNumClasses * sizeof(int32_t), device);
+    EnsurePooled(order, static_cast<size_t>(OrderInts(p)) * sizeof(int32_t), device);
     wave_cap = p;
     slots_cap = s;
     return true;

@@ -18,8 +18,8 @@ Metric: Mrays/s counted as the reference counts rays (primary + secondary,
 the MIS-sampled ray included; shadow rays excluded, muon/integration.cc:34-38,
 483), over device time with the scene resident and the film in device memory.
 `e2e` is the same metric through the public API with host buffers: scene
-creation (records on the host, upload, BVH built on the device) and the host
-film read-back inside every step.
+creation (the description uploaded, records and BVH built on the device)
+and the host film read-back inside every step.
 
 Roofline of the dominant kernel class: algorithmic bytes per launch from the
 host walk of the flattened BVH over sampled queue rays
@@ -376,8 +376,8 @@ def measure_frames(name: str, w: dict, steps: int, warmup: int, builder: str, wi
         "warmup": warmup, "counted_rays_per_step": counted // steps,
         "e2e": {"value": round(e2e_value, 2), "unit": METRIC, "h2d_bytes_per_step": int(desc_bytes),
                 "d2h_bytes_per_step": int(film_bytes),
-                "note": "scene create (host records, upload, BVH build) + render + film read-back into pinned "
-                        "host memory per step"},
+                "note": "scene create (description upload; records and BVH built on the device) + render + film "
+                        "read-back into pinned host memory per step"},
         "gpu_launches": int(launches), "clocks": clocks.summary(), "wall_s": round(wall, 3),
     }
     if rank == 0:

@@ -44,6 +44,13 @@ __device__ __forceinline__ void AddStat(unsigned long long *stats, int idx, unsi
   if ((threadIdx.x & 31) == 0 && s) atomicAdd(stats + idx, s);
 }
 
+// Continuation rays of a shading block are queued grouped by direction
+// octant (1: BlockReserveGrouped) or in thread order (0: BlockReserve).
+#ifndef MUON_CONT_OCTANTS
+#define MUON_CONT_OCTANTS 1
+#endif
+
+#if !MUON_CONT_OCTANTS
 // Exclusive block-wide scan of a (count_a, count_b) pair; returns this
 // thread's offsets into two global queues whose tails are reserved with one
 // atomicAdd each per block. All threads of the block must call it.
@@ -80,6 +87,53 @@ __device__ __forceinline__ void BlockReserve(uint32_t a, uint32_t b, uint32_t *c
   *off_a = static_cast<uint32_t>(base >> 32) + static_cast<uint32_t>(excl >> 32);
   *off_b = static_cast<uint32_t>(base & 0xffffffffu) + static_cast<uint32_t>(excl & 0xffffffffu);
 }
+
+#else
+// Like BlockReserve, with the block's `a` items laid out by group (0..7,
+// each group in thread order; -1: no item) instead of in thread order.
+constexpr int kReserveGroups = 8;
+__device__ __forceinline__ void BlockReserveGrouped(int group, uint32_t nb, uint32_t *ctr_a, uint32_t *ctr_b,
+                                                    uint32_t *off_a, uint32_t *off_b) {
+  __shared__ uint32_t cnt[kWarps][kReserveGroups + 1];  // per warp: a per group, then b
+  __shared__ uint32_t group_base[kReserveGroups];
+  __shared__ uint32_t base_a, base_b;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const unsigned below = (1u << lane) - 1u;
+  unsigned mine = 0;
+  for (int g = 0; g < kReserveGroups; ++g) {
+    const unsigned m = __ballot_sync(0xffffffffu, group == g);
+    if (lane == 0) cnt[warp][g] = static_cast<uint32_t>(__popc(m));
+    if (group == g) mine = m;
+  }
+  uint32_t incl = nb;
+  for (int off = 1; off < 32; off <<= 1) {
+    const uint32_t y = __shfl_up_sync(0xffffffffu, incl, off);
+    if (lane >= off) incl += y;
+  }
+  if (lane == 31) cnt[warp][kReserveGroups] = incl;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    uint32_t ta = 0, tb = 0;
+    for (int g = 0; g < kReserveGroups; ++g) {
+      group_base[g] = ta;
+      for (int w = 0; w < kWarps; ++w) ta += cnt[w][g];
+    }
+    for (int w = 0; w < kWarps; ++w) tb += cnt[w][kReserveGroups];
+    base_a = ta ? atomicAdd(ctr_a, ta) : 0u;
+    base_b = tb ? atomicAdd(ctr_b, tb) : 0u;
+  }
+  __syncthreads();
+  uint32_t pa = 0, pb = base_b + incl - nb;
+  if (group >= 0) {
+    pa = base_a + group_base[group] + static_cast<uint32_t>(__popc(mine & below));
+    for (int w = 0; w < warp; ++w) pa += cnt[w][group];
+  }
+  for (int w = 0; w < warp; ++w) pb += cnt[w][kReserveGroups];
+  *off_a = pa;
+  *off_b = pb;
+  __syncthreads();  // cnt and the bases are written again by the next call
+}
+#endif
 
 // Surface point, shading normal and material of a hit (Primitive::Intersect,
 // muon/objects.cc:29-46, and the normals of Tri/Sphere::IntersectObjectSpace).
@@ -747,6 +801,7 @@ constexpr int kMaskSlots = 64;
 #define MUON_SHADE_SORTED 1
 #endif
 
+
 // ---- guided sampling ----------------------------------------------------------------
 // Direction sampling of a guided render: with probability alpha from the
 // learned mixture of the vertex, else from the render's own sampler
@@ -1025,7 +1080,15 @@ __global__ void __launch_bounds__(kBlock, MUON_SHADE_MIN_BLOCKS)
     }
 
     uint32_t off_c, off_s;
+#if MUON_CONT_OCTANTS
+    // a block's continuation rays grouped by direction octant
+    const int octant = so.want_cont ? (so.cont_d.x < 0.0f ? 1 : 0) | (so.cont_d.y < 0.0f ? 2 : 0) |
+                                          (so.cont_d.z < 0.0f ? 4 : 0)
+                                    : -1;
+    BlockReserveGrouped(octant, so.nshadow, wc.count(bounce + 1), wc.shadow(bounce), &off_c, &off_s);
+#else
     BlockReserve(so.want_cont, so.nshadow, wc.count(bounce + 1), wc.shadow(bounce), &off_c, &off_s);
+#endif
     if (active) b.link[jj] = so.want_cont ? static_cast<int32_t>(off_c) : -1;
     if (so.want_cont) {
       Pick(b.ray_o, nxt)[off_c] = make_float4(so.cont_o.x, so.cont_o.y, so.cont_o.z, id);

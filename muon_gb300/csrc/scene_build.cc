@@ -617,23 +617,44 @@ bool BuildSceneImage(const MuonSceneDesc &desc, SceneImage *img, std::string *er
   std::vector<PrimRecord> tri_rec(ntri_host), tri_obj(ntri_host);
   std::vector<ShadeRecord> tri_shade(ntri_host);
   std::vector<F4> tri_normals, tri_normals_obj;
-  img->any_smooth = false;
-  for (int64_t i = 0; i < ntri; ++i) img->any_smooth |= desc.triangles[i].smooth != 0;
-  if (img->any_smooth) tri_normals.resize(3 * ntri_host), tri_normals_obj.resize(3 * ntri_host);
-  img->leaf_of_prim_id.assign(img->num_prims, -1);
-
-  for (int64_t i = 0; i < ntri; ++i) {
-    const MuonTriangleDesc &t = desc.triangles[i];
+  // One pass over the triangles on all host threads: whether any is smooth,
+  // and the first one with an index out of range (reported as the serial
+  // check would report it).
+  auto triangle_ok = [&](const MuonTriangleDesc &t) {
+    return t.transform >= -1 && t.transform < desc.num_transforms && t.material >= 0 &&
+           t.material < desc.num_materials && t.light >= -1 && t.light < desc.num_lights && t.prim_id >= 0 &&
+           t.prim_id < img->num_prims;
+  };
+  std::atomic<int64_t> first_bad{ntri};
+  std::atomic<bool> any_smooth{false};
+  ParallelFor(ntri, 1 << 16, [&](int64_t i0, int64_t i1) {
+    bool smooth = false;
+    for (int64_t i = i0; i < i1; ++i) {
+      const MuonTriangleDesc &t = desc.triangles[i];
+      smooth |= t.smooth != 0;
+      if (!triangle_ok(t)) {
+        int64_t cur = first_bad.load();
+        while (i < cur && !first_bad.compare_exchange_weak(cur, i)) {
+        }
+        break;
+      }
+    }
+    if (smooth) any_smooth = true;
+  });
+  if (first_bad.load() < ntri) {
+    const MuonTriangleDesc &t = desc.triangles[first_bad.load()];
     if (!check_index(t.transform, desc.num_transforms, "transform") ||
         !check_index(t.material, desc.num_materials, "material") || t.material < 0 ||
         !check_index(t.light, desc.num_lights, "light")) {
+      if (t.material < 0) *error = "primitive refers to a missing material";
       return false;
     }
-    if (t.prim_id < 0 || t.prim_id >= img->num_prims) {
-      *error = "primitive id out of range";
-      return false;
-    }
+    *error = "primitive id out of range";
+    return false;
   }
+  img->any_smooth = any_smooth.load();
+  if (img->any_smooth) tri_normals.resize(3 * ntri_host), tri_normals_obj.resize(3 * ntri_host);
+  img->leaf_of_prim_id.assign(img->num_prims, -1);
   // Per-triangle records, on all host threads (each triangle writes its own
   // slots), then the boxes of the triangles that can be hit in input order.
   std::vector<Aabb> tri_box(ntri_host);

@@ -115,3 +115,25 @@ def test_read_bandwidth_ceilings_are_ordered(lib):
     dram = m.measure_read_bandwidth(2, 4 << 30, 3)
     print(f"read GB/s: L1 {l1:.0f}, L2 {l2:.0f}, DRAM {dram:.0f}")
     assert l1 > l2 > dram > 1000
+
+
+def test_scene_validation_reports_the_first_bad_triangle(lib):
+    """Triangle indices are checked on all host threads; the error names the
+    first bad triangle in input order, as a serial check would."""
+    parsed = m.parse_string(scenes.dense_mesh(16, 16, 1, 2, level=6, clutter=2000, seed=3))
+    d = parsed.desc
+    assert d.num_triangles > 1 << 16
+    tris = d.triangles
+    k1, k2 = d.num_triangles // 3, 2 * d.num_triangles // 3
+    saved = (tris[k1].material, tris[k2].transform)
+    tris[k2].transform = d.num_transforms + 5  # later: a missing transform
+    tris[k1].material = d.num_materials       # first: a missing material
+    with pytest.raises(m.MuonError, match="missing material"):
+        m.walk_rays(parsed, np.zeros((1, 3)), np.array([[0, 0, -1.0]]))
+    tris[k1].material = saved[0]
+    with pytest.raises(m.MuonError, match="missing transform"):
+        m.walk_rays(parsed, np.zeros((1, 3)), np.array([[0, 0, -1.0]]))
+    tris[k2].transform = saved[1]
+    tris[k2].prim_id = d.num_triangles + d.num_spheres
+    with pytest.raises(m.MuonError, match="primitive id out of range"):
+        m.walk_rays(parsed, np.zeros((1, 3)), np.array([[0, 0, -1.0]]))

@@ -46,7 +46,6 @@ struct MuonScene {
   // calls SyncSceneImage.
   mutable bool host_records_stale = false;
   int64_t num_slots = 0;  // primitive records on the device
-  bool l2_window_set = false;
   DevScene dev{};
   DevCamera cam{};
   // scene arrays
@@ -537,41 +536,8 @@ struct QueueProbe {
 // CUDA graph and replayed; the host synchronises once per frame. Unbounded
 // depth (max_depth -1): the host reads the queue length after every bounce and
 // stops when no path continues.
-// Keeps the BVH nodes in the persisting part of L2 while the scene's kernels
-// run (1): an access-policy window over the nodes on the scene's stream,
-// everything else streaming through the rest of L2. The persisting size is a
-// limit of this process's context.
-#ifndef MUON_L2_PERSIST
-#define MUON_L2_PERSIST 0
-#endif
-void SetNodeWindow(MuonScene *sc) {
-  if (!MUON_L2_PERSIST || sc->l2_window_set || sc->dev.num_nodes <= 0) return;
-  sc->l2_window_set = true;
-  int max_persist = 0, max_window = 0;
-  if (cudaDeviceGetAttribute(&max_persist, cudaDevAttrMaxPersistingL2CacheSize, sc->device) != cudaSuccess ||
-      cudaDeviceGetAttribute(&max_window, cudaDevAttrMaxAccessPolicyWindowSize, sc->device) != cudaSuccess ||
-      max_persist <= 0 || max_window <= 0) {
-    cudaGetLastError();
-    return;
-  }
-  const size_t bytes = std::min<size_t>(sizeof(BvhNode) * static_cast<size_t>(sc->dev.num_nodes), max_window);
-  const size_t persist = std::min<size_t>(bytes, max_persist);
-  if (cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, persist) != cudaSuccess) {
-    cudaGetLastError();
-    return;
-  }
-  cudaStreamAttrValue v{};
-  v.accessPolicyWindow.base_ptr = sc->nodes.ptr;
-  v.accessPolicyWindow.num_bytes = bytes;
-  v.accessPolicyWindow.hitRatio = std::min(1.0f, static_cast<float>(persist) / static_cast<float>(bytes));
-  v.accessPolicyWindow.hitProp = cudaAccessPropertyPersisting;
-  v.accessPolicyWindow.missProp = cudaAccessPropertyStreaming;
-  if (cudaStreamSetAttribute(sc->stream, cudaStreamAttributeAccessPolicyWindow, &v) != cudaSuccess) cudaGetLastError();
-}
-
 void RenderDevice(MuonScene *sc, const MuonRenderParams &p, double *d_sum, double *d_sq, uint32_t *d_cnt,
                   const GuideDev *guide = nullptr, QueueProbe *probe = nullptr) {
-  SetNodeWindow(sc);
   cudaStream_t st = sc->stream;
   const bool pt = p.integrator == MUON_INTEGRATOR_PATHTRACER;
   // Raytracer / AnalyticDirect: one kernel follows each path to its end.

@@ -37,9 +37,76 @@ constexpr int kMaxEventPairs = 16384;
 
 }  // namespace
 
+// The path arrays of one wavefront in flight (PathBuffers).
+struct WorkSet {
+  DeviceBuffer ray_o[2], ray_d[2], tp[2], rad[2], hits, link, final_rad, org, contrib, slot_dir, shq, order;
+  int64_t cap = 0;
+  int slots = -1;
+
+  // Grows the arrays (the scene's streams are idle); true if any moved.
+  bool Ensure(int64_t paths, int slots_wanted, int device) {
+    if (paths <= cap && slots_wanted <= slots) return false;
+    const int64_t p = std::max(paths, cap);
+    const int sl_count = std::max(slots_wanted, slots);
+    for (int k = 0; k < 2; ++k) {
+      EnsurePooled(ray_o[k], p * sizeof(float4), device);
+      EnsurePooled(ray_d[k], p * sizeof(float4), device);
+      EnsurePooled(tp[k], p * sizeof(float4), device);
+      EnsurePooled(rad[k], p * sizeof(float4), device);
+    }
+    EnsurePooled(hits, p * sizeof(int2), device);
+    EnsurePooled(link, p * sizeof(int32_t), device);
+    EnsurePooled(final_rad, p * sizeof(float4), device);
+    EnsurePooled(org, p * sizeof(float4), device);
+    const size_t sl = static_cast<size_t>(p) * std::max(sl_count, 1);
+    EnsurePooled(contrib, sl * sizeof(float4), device);
+    EnsurePooled(slot_dir, sl * sizeof(float4), device);
+    EnsurePooled(shq, sl * sizeof(uint32_t), device);
+    EnsurePooled(order, static_cast<size_t>(OrderInts(p)) * sizeof(int32_t), device);
+    cap = p;
+    slots = sl_count;
+    return true;
+  }
+
+  PathBuffers Buffers(const DeviceBuffer &stats) const {
+    PathBuffers b;
+    for (int k = 0; k < 2; ++k) {
+      b.ray_o[k] = ray_o[k].as<float4>();
+      b.ray_d[k] = ray_d[k].as<float4>();
+      b.tp[k] = tp[k].as<float4>();
+      b.rad[k] = rad[k].as<float4>();
+    }
+    b.hits = hits.as<int2>();
+    b.link = link.as<int32_t>();
+    b.final_rad = final_rad.as<float4>();
+    b.org = org.as<float4>();
+    b.contrib = contrib.as<float4>();
+    b.slot_dir = slot_dir.as<float4>();
+    b.shq = shq.as<uint32_t>();
+    b.order = order.as<int32_t>();
+    b.order_cap = static_cast<int32_t>(cap);
+    b.stats = stats.as<unsigned long long>();
+    return b;
+  }
+
+  // To the process-wide cache (the streams are idle).
+  void Give(int device) {
+    for (int k = 0; k < 2; ++k) {
+      PoolGive(ray_o[k], device);
+      PoolGive(ray_d[k], device);
+      PoolGive(tp[k], device);
+      PoolGive(rad[k], device);
+    }
+    for (DeviceBuffer *b : {&hits, &link, &final_rad, &org, &contrib, &slot_dir, &shq, &order}) PoolGive(*b, device);
+  }
+};
+
 struct MuonScene {
   int device = 0;
   cudaStream_t stream = nullptr;
+  // A second stream and its events, for wavefronts in flight two at a time.
+  cudaStream_t stream2 = nullptr;
+  cudaEvent_t fork_ev = nullptr, join_ev = nullptr, film_ev[2] = {nullptr, nullptr};
   SceneImage img;
   // The leaf-order records of a scene whose BVH was built on the device live
   // on the device only (img holds them in input order) until a host reader
@@ -51,12 +118,11 @@ struct MuonScene {
   // scene arrays
   DeviceBuffer nodes, prims, prims_obj, shade, smooth, smooth_obj, transforms, materials, lights, light_tris,
       light_tris_obj, light_tri_ok, other_lights, all_lights;
-  // work arrays
-  DeviceBuffer ray_o[2], ray_d[2], tp[2], rad[2], hits, link, final_rad, org, contrib, slot_dir, shq, order, counters,
-      stats;
+  // work arrays: the path arrays of up to two wavefronts in flight, their
+  // counters and the statistics
+  WorkSet work[2];
+  DeviceBuffer counters, stats;
   DeviceBuffer film_sum, film_sq, film_cnt, ray_in, ray_out, ray_aux;
-  int64_t wave_cap = 0;
-  int slots_cap = -1;
   uint32_t *h_counters = nullptr;  // pinned, one WaveCounters block per wave
   size_t h_counters_len = 0;
   std::vector<EventPair> events;
@@ -75,17 +141,15 @@ struct MuonScene {
 
   ~MuonScene() {
     // The work arrays go to the process-wide cache once the stream is idle.
-    if (stream && cudaStreamSynchronize(stream) == cudaSuccess) {
-      for (int k = 0; k < 2; ++k) {
-        PoolGive(ray_o[k], device);
-        PoolGive(ray_d[k], device);
-        PoolGive(tp[k], device);
-        PoolGive(rad[k], device);
-      }
-      for (DeviceBuffer *b : {&hits, &link, &final_rad, &org, &contrib, &slot_dir, &shq, &order, &film_sum, &film_sq,
-                              &film_cnt, &nodes, &prims, &prims_obj, &shade, &smooth, &smooth_obj})
+    if (stream && cudaStreamSynchronize(stream) == cudaSuccess &&
+        (!stream2 || cudaStreamSynchronize(stream2) == cudaSuccess)) {
+      for (WorkSet &ws : work) ws.Give(device);
+      for (DeviceBuffer *b : {&film_sum, &film_sq, &film_cnt, &nodes, &prims, &prims_obj, &shade, &smooth, &smooth_obj})
         PoolGive(*b, device);
     }
+    for (cudaEvent_t e : {fork_ev, join_ev, film_ev[0], film_ev[1]})
+      if (e) cudaEventDestroy(e);
+    if (stream2) cudaStreamDestroy(stream2);
     if (graph) cudaGraphExecDestroy(graph);
     for (EventPair &e : events) {
       if (e.a) cudaEventDestroy(e.a);
@@ -108,51 +172,21 @@ struct MuonScene {
     return e;
   }
 
-  PathBuffers Buffers() const {
-    PathBuffers b;
-    for (int k = 0; k < 2; ++k) {
-      b.ray_o[k] = ray_o[k].as<float4>();
-      b.ray_d[k] = ray_d[k].as<float4>();
-      b.tp[k] = tp[k].as<float4>();
-      b.rad[k] = rad[k].as<float4>();
-    }
-    b.hits = hits.as<int2>();
-    b.link = link.as<int32_t>();
-    b.final_rad = final_rad.as<float4>();
-    b.org = org.as<float4>();
-    b.contrib = contrib.as<float4>();
-    b.slot_dir = slot_dir.as<float4>();
-    b.shq = shq.as<uint32_t>();
-    b.order = order.as<int32_t>();
-    b.order_cap = static_cast<int32_t>(wave_cap);
-    b.stats = stats.as<unsigned long long>();
-    return b;
+  PathBuffers Buffers(int set = 0) const { return work[set].Buffers(stats); }
+
+  // Grows the path arrays of `sets` wavefronts in flight; true if any moved.
+  bool EnsureWork(int64_t paths, int slots, int sets = 1) {
+    bool moved = false;
+    for (int k = 0; k < sets; ++k) moved |= work[k].Ensure(paths, slots, device);
+    return moved;
   }
 
-  // Grows the per-wavefront arrays; returns true if any pointer changed.
-  bool EnsureWork(int64_t paths, int slots) {
-    if (paths <= wave_cap && slots <= slots_cap) return false;
-    int64_t p = std::max(paths, wave_cap);
-    int s = std::max(slots, slots_cap);
-    // the stream is idle here (every render synchronises before returning)
-    for (int k = 0; k < 2; ++k) {
-      EnsurePooled(ray_o[k], p * sizeof(float4), device);
-      EnsurePooled(ray_d[k], p * sizeof(float4), device);
-      EnsurePooled(tp[k], p * sizeof(float4), device);
-      EnsurePooled(rad[k], p * sizeof(float4), device);
-    }
-    EnsurePooled(hits, p * sizeof(int2), device);
-    EnsurePooled(link, p * sizeof(int32_t), device);
-    EnsurePooled(final_rad, p * sizeof(float4), device);
-    EnsurePooled(org, p * sizeof(float4), device);
-    size_t sl = static_cast<size_t>(p) * std::max(s, 1);
-    EnsurePooled(contrib, sl * sizeof(float4), device);
-    EnsurePooled(slot_dir, sl * sizeof(float4), device);
-    EnsurePooled(shq, sl * sizeof(uint32_t), device);
-    EnsurePooled(order, static_cast<size_t>(OrderInts(p)) * sizeof(int32_t), device);
-    wave_cap = p;
-    slots_cap = s;
-    return true;
+  // The second stream and the events that order two wavefronts in flight.
+  void EnsureStream2() {
+    if (stream2) return;
+    CUDA_TRY(cudaStreamCreateWithFlags(&stream2, cudaStreamNonBlocking));
+    for (cudaEvent_t *e : {&fork_ev, &join_ev, &film_ev[0], &film_ev[1]})
+      CUDA_TRY(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
   }
 
   // Grows the device and pinned host counter arrays; returns true if the
@@ -536,6 +570,11 @@ struct QueueProbe {
 // CUDA graph and replayed; the host synchronises once per frame. Unbounded
 // depth (max_depth -1): the host reads the queue length after every bounce and
 // stops when no path continues.
+// Wavefronts in flight at a time in a render (1 or 2).
+#ifndef MUON_WAVES_IN_FLIGHT
+#define MUON_WAVES_IN_FLIGHT 2
+#endif
+
 void RenderDevice(MuonScene *sc, const MuonRenderParams &p, double *d_sum, double *d_sq, uint32_t *d_cnt,
                   const GuideDev *guide = nullptr, QueueProbe *probe = nullptr) {
   cudaStream_t st = sc->stream;
@@ -567,10 +606,18 @@ void RenderDevice(MuonScene *sc, const MuonRenderParams &p, double *d_sum, doubl
   const bool traces = bp.traces, bounded = bp.bounded;
   const int bounces = bp.bounces;
   const size_t stride = WaveCounterWords(bounces);
-  bool moved = sc->EnsureWork(std::min<int64_t>(plan.pix_per_wave, npix_total) * plan.ns, slots);
+  // Two wavefronts in flight, on two streams with their own path arrays:
+  // while one wavefront's kernels drain (the last rays of a persistent
+  // traversal launch, the last blocks of a pass), the other's fill the SMs.
+  // Films are still added in wave order. Per-kernel timing, probes, guiding
+  // and host-driven unbounded loops run the wavefronts one after another.
+  const bool concurrent = MUON_WAVES_IN_FLIGHT > 1 && bounded && !timing && !probe && !guide && waves.size() > 1;
+  bool moved = sc->EnsureWork(std::min<int64_t>(plan.pix_per_wave, npix_total) * plan.ns, slots, concurrent ? 2 : 1);
   moved |= sc->EnsureCounters(stride * waves.size());
   sc->stats.Ensure(sizeof(unsigned long long) * kNumStats);
-  PathBuffers b = sc->Buffers();
+  if (concurrent) sc->EnsureStream2();
+  const PathBuffers bsets[2] = {sc->Buffers(0), sc->Buffers(concurrent ? 1 : 0)};
+  const PathBuffers &b = bsets[0];
   if (probe) {
     probe->waves = waves.size();
     probe->bounces = bounces;
@@ -591,9 +638,18 @@ void RenderDevice(MuonScene *sc, const MuonRenderParams &p, double *d_sum, doubl
     sc->events_used = 1;  // pair 0 brackets the frame
     CUDA_TRY(cudaMemsetAsync(sc->counters.ptr, 0, stride * waves.size() * sizeof(uint32_t), st));
     CUDA_TRY(cudaMemsetAsync(sc->stats.ptr, 0, sizeof(unsigned long long) * kNumStats, st));
+    const cudaStream_t main_st = st;
+    if (concurrent) {  // the second stream joins after the clears
+      CUDA_TRY(cudaEventRecord(sc->fork_ev, main_st));
+      CUDA_TRY(cudaStreamWaitEvent(sc->stream2, sc->fork_ev, 0));
+    }
     for (size_t wi = 0; wi < waves.size(); ++wi) {
       const WaveInfo &w = waves[wi];
       WaveCounters wc{sc->counters.as<uint32_t>() + wi * stride};
+      // this wavefront's path arrays and stream
+      const int set = concurrent ? static_cast<int>(wi & 1) : 0;
+      const PathBuffers &b = bsets[set];
+      const cudaStream_t st = set ? sc->stream2 : main_st;
       LaunchCamera(sc->cam, w, b, wc, st);
       ++launches;
       auto timed = [&](int kind, auto &&launch) {
@@ -651,12 +707,19 @@ void RenderDevice(MuonScene *sc, const MuonRenderParams &p, double *d_sum, doubl
           if (sc->h_counters[0] == 0) break;
         }
       }
+      // films in wave order (wavefronts may share pixels)
+      if (concurrent && wi > 0) CUDA_TRY(cudaStreamWaitEvent(st, sc->film_ev[(wi - 1) & 1], 0));
       LaunchFilm(w, b, d_sum, d_sq, d_cnt, st);
+      if (concurrent) CUDA_TRY(cudaEventRecord(sc->film_ev[wi & 1], st));
       ++launches;
       if (guide && !guide->direct_only) {
         LaunchGuideCollect(b, wc, std::min(bounces, guide->rec_bounces), w.n, guide_local, st);
         ++launches;
       }
+    }
+    if (concurrent) {  // the second stream's work ends before the frame does
+      CUDA_TRY(cudaEventRecord(sc->join_ev, sc->stream2));
+      CUDA_TRY(cudaStreamWaitEvent(main_st, sc->join_ev, 0));
     }
     timed_pairs = sc->events_used;
   };

@@ -103,7 +103,8 @@ extern "C" {
 /* render flags */
 #define MUON_RENDER_STATS 1u      /* count bounds/object tests (slower)        */
 #define MUON_RENDER_ACCUMULATE 2u /* add into the caller's film, do not zero   */
-#define MUON_RENDER_TIMING 4u     /* time every kernel with CUDA events        */
+#define MUON_RENDER_TIMING 4u     /* time every kernel with CUDA events (the   */
+                                  /* wavefronts then run one at a time)         */
 #define MUON_RENDER_NO_GRAPH 8u   /* launch kernel by kernel, no CUDA graph    */
 
 /* ---- scene description (flattened muon::Scene, muon/scene.h:22-95) ---- */

@@ -196,7 +196,9 @@ typedef struct MuonRenderParams {
   int32_t sample_offset; /* index of the first sample (progressive runs) */
   uint64_t seed;
   int32_t intersect_mode; /* MUON_ISECT_* */
-  int32_t wave_paths;    /* paths in flight per wavefront; 0 = tuned     */
+  int32_t wave_paths;    /* paths per wavefront (0 = 2^24); a render     */
+                         /* keeps two wavefronts in flight, each with  */
+                         /* about 200 + 36 x shadow slots bytes a path */
   uint32_t flags;        /* MUON_RENDER_*                               */
   int32_t pad;
 } MuonRenderParams;
